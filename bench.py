@@ -1,0 +1,292 @@
+"""Benchmark: MD bead-steps/s of the SOUFFLE force-and-integrate path on one GB300.
+
+Workload (default): 2000 two-layer 42-bead capsomeres (84,000 beads) at 800 uM, reference
+options -s 1000 -b 1000 -E 2.1 -e 5 -L 0.3 -B 10 -t 0.005 -q 5 -Q 10 -K 298 -c 94.27, FP32
+forces with 64-bit fixed-point accumulation, FP64 integration and thermostat.  A step is one
+iteration of the reference MD loop (src/md.cpp:400-514): thermostat half steps, velocity
+Verlet, the pair-list rebuild every 10th step, forces, centre-of-mass velocity removal.
+
+  value  device time of K single steps with inputs resident in HBM; the working set (~30 MB)
+         fits in L2, so L2 is flushed (a 256 MB write) before every timed step, outside the
+         timed region.
+  e2e    the same K steps through the C ABI from host buffers: state uploaded from pinned host
+         memory, run in rebuild windows with the thermostat scalars read back after each
+         window, final state downloaded.
+  cpu_baseline / --impl reference: the oracle port of the reference algorithm (long double,
+         OpenMP over subunits, all host cores) on a bounded sample of the same workload.
+
+Multi-GPU (torchrun): every rank runs an independent replica of the workload (replicas only;
+the path has no exchange step), value = total bead-steps / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "capsid-souffle_gb300"))
+
+PROFILE_SUMMARY = os.path.join(REPO, "profiles", "k_forces_plain_large.txt")
+
+
+def _clock_sampler():
+    """Sample SM clocks and throttle reasons with nvidia-smi during the timed region."""
+    q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+    samples, stop = [], threading.Event()
+
+    def run():
+        while not stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", "0", f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip().splitlines()
+                if out:
+                    samples.append([x.strip() for x in out[0].split(",")])
+            except Exception:
+                pass
+            stop.wait(0.2)
+
+    th = threading.Thread(target=run, daemon=True)
+    return samples, stop, th
+
+
+def _summarize_clocks(samples):
+    if not samples:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+    import statistics
+    sm = [float(s[0]) for s in samples if s[0].replace(".", "").isdigit()]
+    mx = [float(s[1]) for s in samples if s[1].replace(".", "").isdigit()]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({names[k] for s in samples for k in range(4) if len(s) > 2 + k and
+                      s[2 + k].lower().startswith("active")})
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons, "samples": len(samples)}
+
+
+def _profile_traffic():
+    """DRAM bytes per k_forces launch from the committed ncu summary, if present."""
+    try:
+        for line in open(PROFILE_SUMMARY):
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_reference(w, seconds: float = 10.0, max_steps: int = 30, threads: int = 0):
+    """Time the oracle port (long double, OpenMP) on the workload: bead-steps/s."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    threads = threads or os.cpu_count()
+    o = pyoracle.Oracle(w.template, int(w.opt.S), w.derived, w.opt.s, w.opt.b, w.opt.E,
+                        w.center_local)
+    o.set_threads(threads)
+    o.set_state(w.state.pos, w.state.vel)
+    o.forces(True)
+    ke = o.kinetic_energy()
+    o.nhc_init(int(w.opt.q), w.opt.Q, w.opt.K)
+    ke, _, _ = o.md_step(0, w.opt.t, int(w.opt.B), ke)  # warm-up step (with a rebuild)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps and (steps < 3 or time.perf_counter() - t0 < seconds):
+        ke, _, _ = o.md_step(1 + steps, w.opt.t, int(w.opt.B), ke)
+        steps += 1
+    dt = time.perf_counter() - t0
+    import platform
+    return {"value": w.n_beads * steps / dt, "unit": "bead-steps/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{steps} MD steps (rebuild every {int(w.opt.B)}) of the {w.n_beads}-bead "
+                      f"workload after one warm-up step; long double = "
+                      f"{'x87 80-bit' if platform.machine() in ('x86_64', 'AMD64') else 'IEEE binary128 (software)'}"
+                      f" on {platform.machine()}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--subunits", type=int, default=2000)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from souffle_gb300 import workloads
+    w = workloads.plain_large(args.subunits, seed=12345 + rank)
+    config = {"workload": f"plain_large: {args.subunits} bilayer capsomeres x 42 beads = "
+                          f"{w.n_beads} beads, 800 uM, -e 5 -L 0.3 -B 10 -t 0.005 -q 5",
+              "l2": "flushed (256 MB write) before every timed step; working set < L2",
+              "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_reference(w, seconds=args.cpu_seconds)
+        steps_ms = w.n_beads / cb["value"] * 1e3
+        print(json.dumps({
+            "impl": "reference", "metric": "bead-steps/s", "value": cb["value"],
+            "unit": "bead-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": steps_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "long double (f80/f128)",
+            "data": "synthetic (seeded random capsomere states)", "config": config,
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}))
+        return
+
+    import numpy as np
+    import torch
+    from souffle_gb300 import gpu
+
+    torch.cuda.set_device(0)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_
+        dist_.init_process_group("gloo")
+        dist = dist_
+
+    p = gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local)
+    s = gpu.GpuSystem(w.template, [p])
+    s.set_state(w.state.pos, w.state.vel)
+    s.md_begin()
+    stats = s.pairlist_stats()
+    n_bar = stats["mean_length"]
+    ext = torch.cuda.ExternalStream(s.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    B = int(w.opt.B)
+
+    a = 0
+    s.md_steps(a, args.warmup)
+    a += args.warmup
+
+    # timed region: K single steps, L2 flushed before each, CUDA events on the handle's stream
+    samples, stop, th = _clock_sampler()
+    th.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    launches = 0
+    for k in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+        evs[k][0].record(ext)
+        s.md_steps(a, 1)
+        evs[k][1].record(ext)
+        launches += 2 + (5 if a % B == 0 else 0)
+        a += 1
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    stop.set()
+    th.join()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    total_ms = float(sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * w.n_beads * args.steps / (total_ms / 1e3)
+
+    # warm-L2 throughput: the same K steps as whole graph windows, no flush
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0 = ((a + B - 1) // B) * B
+    if a0 > a:
+        s.md_steps(a, a0 - a)
+    a = a0
+    kw = max(B, (args.steps // B) * B)
+    start.record(ext)
+    s.md_steps(a, kw)
+    end.record(ext)
+    torch.cuda.synchronize()
+    a += kw
+    warm_value = w.n_beads * kw / (start.elapsed_time(end) / 1e3)
+
+    # per-kernel times (events between launches, direct launches)
+    prof = s.md_profile(a, 20)
+    a += 20
+    forces_ms = prof["forces_ms"] / prof["steps"]
+    drift_ms = prof["drift_ms"] / prof["steps"]
+    rebuild_ms = prof["rebuild_ms"] / max(1, prof["rebuilds"])
+
+    # e2e through the C ABI with host buffers
+    pos_h = torch.from_numpy(np.ascontiguousarray(w.state.pos)).pin_memory()
+    vel_h = torch.from_numpy(np.ascontiguousarray(w.state.vel)).pin_memory()
+    pos_o = torch.empty_like(pos_h).pin_memory()
+    vel_o = torch.empty_like(vel_h).pin_memory()
+    import ctypes as C
+    lib = gpu.load()
+    dp = C.POINTER(C.c_double)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gpu._check(lib.souffle_gpu_set_state(s.h, C.cast(pos_h.data_ptr(), dp), C.cast(vel_h.data_ptr(), dp)))
+    s.md_begin()
+    e2e_steps = max(B, (args.steps // B) * B)
+    reads = 0
+    for k in range(0, e2e_steps, B):
+        s.md_steps(k, B)
+        s.md_scalars()
+        reads += 1
+    gpu._check(lib.souffle_gpu_get_state(s.h, C.cast(pos_o.data_ptr(), dp), C.cast(vel_o.data_ptr(), dp)))
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": w.n_beads * e2e_steps / e2e_s, "unit": "bead-steps/s",
+           "h2d_bytes_per_step": 48 * w.n_beads / e2e_steps,
+           "d2h_bytes_per_step": (48 * w.n_beads + 24 * reads) / e2e_steps,
+           "note": "set_state from pinned host + md_begin + steps in rebuild windows with the "
+                   "thermostat scalars read after each window + get_state, wall clock"}
+
+    # roofline of the dominant kernel (k_forces): its share of the algorithmic bytes per bead
+    # step: pos32 tile 16 B + neighbour-index stream 4 n_bar + force write 24 B + velocity
+    # read/write 48 B + per-bead constants 16 B
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    kern_bytes = (16 + 4 * n_bar + 24 + 48 + 16) * w.n_beads
+    achieved = kern_bytes / (forces_ms / 1e3) / 1e9
+    step_bytes = (112 + 4 * n_bar + (4 * n_bar + 16) / B) * w.n_beads
+    traffic = _profile_traffic()
+    out = {
+        "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64 fixed / f64",
+        "data": "synthetic (seeded random capsomere states, random orientations, Maxwell-Boltzmann velocities)",
+        "config": config,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "warm_l2_value": warm_value,
+        "kernels_ms": {"k_forces": forces_ms, "k_drift": drift_ms, "rebuild": rebuild_ms},
+        "pairlist": {"mean_length": n_bar, "max_length": stats["max_length"],
+                     "max_inter": stats["max_inter"]},
+        "roofline": {"bound": "hbm", "kernel": "k_forces", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800"},
+        "roofline_step": {"achieved": step_bytes * value / w.n_beads / 1e9, "peak": peak,
+                          "unit": "GB/s", "frac": step_bytes * value / w.n_beads / 1e9 / peak,
+                          "bytes_per_bead_step": step_bytes / w.n_beads},
+        "clocks": _summarize_clocks(samples),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_reference(w, seconds=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,143 @@
+// Kernel argument blocks and launch wrappers of the SOUFFLE GPU path (definitions in
+// pairlist.cu, forces.cu, energies.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "souffle_dev.cuh"
+
+namespace souffle {
+
+struct CellArgs {
+  const long long* px;
+  const long long* py;
+  const long long* pz;
+  const SysParams* sys;
+  const int* sub_sys;     // [S_total] system of each subunit
+  int np, n_sub_total;
+  int* cell_count;        // [total cells]
+  int* cell_start;        // [total cells + 1]
+  int* sub_rank;          // [S_total]
+  int* sub_cell;          // [S_total]
+  int* cell_subs;         // [S_total]
+  int total_cells;
+};
+
+struct CandArgs {
+  CellArgs c;
+  int cap;
+  int* cand;        // [S_total * cap] candidate subunits (global ids), ascending
+  int* cand_count;  // [S_total]
+  unsigned int* err;
+};
+
+struct PairArgs {
+  const long long* px;
+  const long long* py;
+  const long long* pz;
+  const int4* pos32;
+  const SysParams* sys;
+  const int* sub_sys;
+  const float* q;       // [np] template charges (only q != 0 matters)
+  int np, words, n_beads_total;
+  const int* cand;
+  const int* cand_count;
+  int cand_cap;
+  unsigned int* intra_mask;  // [S_total * np * words]
+  int* inter_ids;            // [cap * N]
+  int* inter_count;          // [N]
+  int* ref_len;              // [N] reference list length (intra + inter)
+  int inter_cap;
+  unsigned int* err;
+};
+
+struct ForceArgs {
+  TplLayout L;
+  const int* tpl_i;
+  const float* tpl_f;
+  const SysParams* sys;
+  SysState* state;
+  const WorkItem* work;
+  const int2* sys_slots;     // per system: first partial slot, slot count
+  const int4* pos32;
+  const unsigned int* intra_mask;
+  const int* inter_ids;
+  const int* inter_count;
+  const float* dh_w;         // [n_sys * np] q * exp(kappa sigma/2)/(1 + kappa sigma/2) * sqrt(lb)
+  const PairTable* pt;
+  const double* inv_mass;    // [np]
+  double* fx; double* fy; double* fz;
+  double* vx; double* vy; double* vz;
+  double* sfx; double* sfy; double* sfz;   // optional stretching force out
+  double* bfx; double* bfy; double* bfz;   // optional bending force out
+  double* partial;           // [slots * 4]
+  unsigned int* err;
+  int n_beads_total;
+  int max_sub;               // subunits per CTA (shared-memory sizing)
+  int mode;                  // 0: forces only, 1: MD step (kick + reductions), 2: begin (KE only)
+};
+
+struct DriftArgs {
+  const SysParams* sys;
+  const SysState* state;
+  const WorkItem* work;
+  const double* inv_mass;
+  int np;
+  const double* fx; const double* fy; const double* fz;
+  double* vx; double* vy; double* vz;
+  long long* px; long long* py; long long* pz;
+  int4* pos32;
+};
+
+struct StateArgs {
+  const SysParams* sys;
+  SysState* state;
+  const int* bead_sys;   // [N]
+  int np, n;
+  const double* pos_in;  // [N*3] xyz interleaved (device staging), may be null
+  const double* vel_in;
+  long long* px; long long* py; long long* pz;
+  int4* pos32;
+  double* vx; double* vy; double* vz;
+  double* pos_out;       // [N*3]
+  double* vel_out;
+};
+
+struct EnergyArgs {
+  TplLayout L;
+  const int* tpl_i;
+  const SysParams* sys;
+  const SysState* state;
+  const long long* px; const long long* py; const long long* pz;
+  const int4* pos32;
+  const double* vx; const double* vy; const double* vz;
+  const double* len0;      // [ne]
+  const double* mass;      // [np]
+  const double* q;         // [np]
+  const double* sigma;     // [np]
+  const int* type;         // [np]
+  const int* lj_t;         // [2 * n_lj]
+  int n_lj;
+  double ecut;
+  double elj_att;
+  double lb, kappa, ecut_el;
+  double sigma_max;        // largest bead diameter (pair pruning)
+  int sysid;
+  int n0, n;               // first bead of the system, beads in it
+  double* se; double* be; double* ne; double* ce; double* ke;  // [n] (system-local)
+  double* totals;          // [8] per call
+};
+
+void launch_cells_count(const CellArgs& a, int grid, int block, cudaStream_t s);
+void launch_cells_scan(const CellArgs& a, cudaStream_t s);
+void launch_cells_scatter(const CellArgs& a, int grid, int block, cudaStream_t s);
+void launch_candidates(const CandArgs& a, int grid, int block, cudaStream_t s);
+void launch_pairs(const PairArgs& a, int n_sub, size_t smem, cudaStream_t s);
+void launch_forces(const ForceArgs& a, int grid, int block, size_t smem, cudaStream_t s);
+void launch_drift(const DriftArgs& a, int grid, int block, cudaStream_t s);
+void launch_state_in(const StateArgs& a, int grid, int block, cudaStream_t s);
+void launch_state_out(const StateArgs& a, int grid, int block, cudaStream_t s);
+void launch_energies(const EnergyArgs& a, int n, cudaStream_t s);
+cudaError_t set_kernel_smem(size_t force_smem, size_t pair_smem);
+cudaError_t set_pairs_smem(size_t smem);
+
+}  // namespace souffle

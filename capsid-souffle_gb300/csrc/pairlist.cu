@@ -1,0 +1,331 @@
+// Pair-list rebuild: counting-sort grid of subunit centres, candidate subunits, bead pairs.
+//
+// Reference: update_pairlist (src/functions.cpp:69-117), called per subunit from
+// forceCalculation when step % B == 0 (src/forces.cpp:63-65, src/md.cpp:435-438).  The
+// reference tests every subunit pair's centre beads against 1.5 x the list radius
+// (|c_i - c_j|^2 < 2.25 r^2), then every bead pair of a passing subunit pair against r^2,
+// appending neighbour ids in ascending order.  Here the O(S^2) centre scan becomes a
+// counting-sort cell grid (cell edge >= 1.5 r, 27-cell stencil) that yields the same
+// candidate set; candidates are sorted so lists come out in the reference's order.
+//
+// Decisions are exact: a float test on the rounded high words settles every pair farther than
+// a safety margin from the cut-off, and the rest are decided in double from the exact 64-bit
+// fixed-point differences, matching the reference up to long double vs double ties.
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace souffle {
+
+
+__device__ __forceinline__ int cell_coord(long long x, int ncell) {
+  unsigned long long u = (unsigned long long)x + 0x8000000000000000ull;  // [0, 2^64) over [-L/2, L/2)
+  return (int)__umul64hi(u, (unsigned long long)ncell);
+}
+
+__global__ void k_cells_count(CellArgs a) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n_sub_total) return;
+  const SysParams& p = a.sys[a.sub_sys[s]];
+  int c = s * a.np + p.center_local;
+  int n = p.ncell;
+  int cx = cell_coord(a.px[c], n), cy = cell_coord(a.py[c], n), cz = cell_coord(a.pz[c], n);
+  int cell = p.cell0 + (cx * n + cy) * n + cz;
+  a.sub_cell[s] = cell;
+  a.sub_rank[s] = atomicAdd(&a.cell_count[cell], 1);
+}
+
+// Single-CTA exclusive scan over all cells (a few thousand to a few hundred thousand).
+__global__ void k_cells_scan(CellArgs a) {
+  __shared__ int warp_sums[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int base = 0; base < a.total_cells; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    int v = (i < a.total_cells) ? a.cell_count[i] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int w = (lane < nw) ? warp_sums[lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_sums[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    int excl = x - v + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
+    if (i < a.total_cells) a.cell_start[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) a.cell_start[a.total_cells] = carry;
+}
+
+__global__ void k_cells_scatter(CellArgs a) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n_sub_total) return;
+  a.cell_subs[a.cell_start[a.sub_cell[s]] + a.sub_rank[s]] = s;
+}
+
+
+// One thread per subunit: centre-distance test over the 27-cell stencil (src/functions.cpp:80-91).
+__global__ void k_candidates(CandArgs a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.c.n_sub_total) return;
+  const int sysid = a.c.sub_sys[i];
+  const SysParams& p = a.c.sys[sysid];
+  const int np = a.c.np, cl = p.center_local;
+  const int ci = i * np + cl;
+  const long long xi = a.c.px[ci], yi = a.c.py[ci], zi = a.c.pz[ci];
+  const int n = p.ncell;
+  const int cx = cell_coord(xi, n), cy = cell_coord(yi, n), cz = cell_coord(zi, n);
+  int* out = a.cand + (size_t)i * a.cap;
+  int cnt = 0;
+  // iterate over distinct neighbouring cells; with fewer than 3 cells per side every cell is a
+  // neighbour, so loop over all of them once
+  const int span = (n < 3) ? n : 3;
+  for (int dx = 0; dx < span; dx++) {
+    int gx = (n < 3) ? dx : (cx + dx - 1 + n) % n;
+    for (int dy = 0; dy < span; dy++) {
+      int gy = (n < 3) ? dy : (cy + dy - 1 + n) % n;
+      for (int dz = 0; dz < span; dz++) {
+        int gz = (n < 3) ? dz : (cz + dz - 1 + n) % n;
+        int cell = p.cell0 + (gx * n + gy) * n + gz;
+        int s0 = a.c.cell_start[cell], s1 = a.c.cell_start[cell + 1];
+        for (int k = s0; k < s1; k++) {
+          int j = a.c.cell_subs[k];
+          bool take;
+          if (j == i) {
+            take = true;  // r2 = 0 for i == j (src/functions.cpp:90)
+          } else {
+            int cj = j * np + cl;
+            double ddx = fixed_diff(xi, a.c.px[cj], p.fx_to_len);
+            double ddy = fixed_diff(yi, a.c.py[cj], p.fx_to_len);
+            double ddz = fixed_diff(zi, a.c.pz[cj], p.fx_to_len);
+            double r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            take = r2 < p.pre2;
+          }
+          if (take) {
+            if (cnt < a.cap) out[cnt] = j;
+            cnt++;
+          }
+        }
+      }
+    }
+  }
+  if (cnt > a.cap) {
+    atomicOr(a.err, kErrCandOverflow);
+    cnt = a.cap;
+  }
+  // insertion sort: candidate lists are short (a few to a few dozen)
+  for (int x = 1; x < cnt; x++) {
+    int v = out[x];
+    int y = x - 1;
+    while (y >= 0 && out[y] > v) {
+      out[y + 1] = out[y];
+      y--;
+    }
+    out[y + 1] = v;
+  }
+  a.cand_count[i] = cnt;
+}
+
+
+// Margin (in length^2) within which the float test defers to the exact double test.
+__device__ __forceinline__ float pair_margin(float nl2) { return 1e-4f * (1.0f + nl2); }
+
+// One CTA per subunit i; thread t owns bead rows t, t + blockDim, ...  Candidate subunit j's
+// positions are staged in shared memory, in ascending j, so each row's entries come out in
+// ascending global id.
+__global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int4* s32 = reinterpret_cast<int4*>(smem_raw);                   // [np] 16-byte entries first
+  long long* sx = reinterpret_cast<long long*>(s32 + a.np);
+  long long* sy = sx + a.np;
+  long long* sz = sy + a.np;
+  double* row_last = reinterpret_cast<double*>(sz + a.np);         // [np] quirk pass
+  int* row_has = reinterpret_cast<int*>(row_last + a.np);          // [np]
+  float* sq = reinterpret_cast<float*>(row_has + a.np);           // [np]
+
+  const int i = blockIdx.x;
+  const int sysid = a.sub_sys[i];
+  const SysParams& p = a.sys[sysid];
+  const int np = a.np;
+  const int i_local = i - p.sub0;  // subunit index inside its system
+  const float unit = p.unit32;
+  const float nl2f = p.nl2_f;
+  const float margin = pair_margin(nl2f);
+  const int ncand = a.cand_count[i];
+  const int* cand = a.cand + (size_t)i * a.cand_cap;
+
+  for (int t = threadIdx.x; t < np; t += blockDim.x) sq[t] = a.q[t];
+
+  // per-row state held in registers for up to 2 rows per thread (np <= 256, blockDim 128)
+  int inter_n[2] = {0, 0};
+  unsigned int* mask_rows = a.intra_mask + (size_t)i * np * a.words;
+  for (int t = threadIdx.x; t < np * a.words; t += blockDim.x) mask_rows[t] = 0u;
+
+  const int ci_global = i * np + p.center_local;
+  const long long cxi = a.px[ci_global], cyi = a.py[ci_global], czi = a.pz[ci_global];
+
+  for (int c = 0; c < ncand; c++) {
+    const int j = cand[c];
+    __syncthreads();
+    for (int t = threadIdx.x; t < np; t += blockDim.x) {
+      int g = j * np + t;
+      sx[t] = a.px[g];
+      sy[t] = a.py[g];
+      sz[t] = a.pz[g];
+      s32[t] = a.pos32[g];
+    }
+    __syncthreads();
+    const int j_local = j - p.sub0;
+    const bool same = (j == i);
+    // The stale-r2 reuse of src/functions.cpp:97 can only trigger when subunit 0 of the system
+    // is involved; those blocks take the exact sequential-semantics path below.
+    const bool quirk = p.quirks && (i_local == 0 || j_local == 0);
+    if (!quirk) {
+      for (int r = 0, ii = threadIdx.x; ii < np; ii += blockDim.x, r++) {
+        const int gi = i * np + ii;
+        const int4 pi = a.pos32[gi];
+        const long long xi = a.px[gi], yi = a.py[gi], zi = a.pz[gi];
+        const bool qi = sq[ii] != 0.0f;
+        for (int jj = 0; jj < np; jj++) {
+          if (same) {
+            if (!(jj != ii && qi && sq[jj] != 0.0f)) continue;  // electrostatic only (:94-96)
+          }
+          const int4 pj = s32[jj];
+          float dx = hi_diff(pi.x, pj.x, unit), dy = hi_diff(pi.y, pj.y, unit),
+                dz = hi_diff(pi.z, pj.z, unit);
+          float r2f = dx * dx + dy * dy + dz * dz;
+          bool in;
+          if (fabsf(r2f - nl2f) > margin) {
+            in = r2f < nl2f;
+          } else {
+            double ex = fixed_diff(xi, sx[jj], p.fx_to_len), ey = fixed_diff(yi, sy[jj], p.fx_to_len),
+                   ez = fixed_diff(zi, sz[jj], p.fx_to_len);
+            in = (ex * ex + ey * ey + ez * ez) < p.nl2;
+          }
+          if (!in) continue;
+          if (same) {
+            mask_rows[ii * a.words + (jj >> 5)] |= 1u << (jj & 31);
+          } else {
+            int k = inter_n[r];
+            if (k < a.inter_cap) a.inter_ids[(size_t)k * a.n_beads_total + gi] = j * np + jj;
+            inter_n[r] = k + 1;
+          }
+        }
+      }
+    } else {
+      // Exact semantics of the reference loop for this (i, j) block, in double.  The test at
+      // src/functions.cpp:97 compares a local index with a global id, so a distance is
+      // recomputed only when not (i is subunit 0 and ii is its centre) and not (j is subunit 0
+      // and jj is its centre); otherwise the r2 of the most recent computed pair (in row-major
+      // order over the block) is reused, starting from the centre distance (or 0 when i == j).
+      const int cl = p.center_local;
+      const bool i0 = (i_local == 0), j0 = (j_local == 0);
+      double init_r2 = 0.0;
+      if (!same) {
+        int cj = j * np + cl;
+        double ex = fixed_diff(cxi, a.px[cj], p.fx_to_len), ey = fixed_diff(cyi, a.py[cj], p.fx_to_len),
+               ez = fixed_diff(czi, a.pz[cj], p.fx_to_len);
+        init_r2 = ex * ex + ey * ey + ez * ez;
+      }
+      // pass 1: last computed r2 of every row
+      for (int ii = threadIdx.x; ii < np; ii += blockDim.x) {
+        const int gi = i * np + ii;
+        const bool qi = sq[ii] != 0.0f;
+        double last = 0.0;
+        int has = 0;
+        if (!(i0 && ii == cl)) {
+          for (int jj = 0; jj < np; jj++) {
+            bool cond = same ? (jj != ii && qi && sq[jj] != 0.0f) : true;
+            if (!cond || (j0 && jj == cl)) continue;
+            double ex = fixed_diff(a.px[gi], sx[jj], p.fx_to_len),
+                   ey = fixed_diff(a.py[gi], sy[jj], p.fx_to_len),
+                   ez = fixed_diff(a.pz[gi], sz[jj], p.fx_to_len);
+            last = ex * ex + ey * ey + ez * ez;
+            has = 1;
+          }
+        }
+        row_last[ii] = last;
+        row_has[ii] = has;
+      }
+      __syncthreads();
+      // pass 2: each row starts from the carried value of the nearest earlier computing row
+      for (int r = 0, ii = threadIdx.x; ii < np; ii += blockDim.x, r++) {
+        const int gi = i * np + ii;
+        const bool qi = sq[ii] != 0.0f;
+        double r2 = init_r2;
+        for (int k = ii - 1; k >= 0; k--)
+          if (row_has[k]) {
+            r2 = row_last[k];
+            break;
+          }
+        const bool row_stale = (i0 && ii == cl);
+        for (int jj = 0; jj < np; jj++) {
+          bool cond = same ? (jj != ii && qi && sq[jj] != 0.0f) : true;
+          if (!cond) continue;
+          if (!row_stale && !(j0 && jj == cl)) {
+            double ex = fixed_diff(a.px[gi], sx[jj], p.fx_to_len),
+                   ey = fixed_diff(a.py[gi], sy[jj], p.fx_to_len),
+                   ez = fixed_diff(a.pz[gi], sz[jj], p.fx_to_len);
+            r2 = ex * ex + ey * ey + ez * ez;
+          }
+          if (!(r2 < p.nl2)) continue;
+          if (same) {
+            mask_rows[ii * a.words + (jj >> 5)] |= 1u << (jj & 31);
+          } else {
+            int k = inter_n[r];
+            if (k < a.inter_cap) a.inter_ids[(size_t)k * a.n_beads_total + gi] = j * np + jj;
+            inter_n[r] = k + 1;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int r = 0, ii = threadIdx.x; ii < np; ii += blockDim.x, r++) {
+    const int gi = i * np + ii;
+    int n_inter = inter_n[r];
+    if (n_inter > a.inter_cap) {
+      atomicOr(a.err, kErrInterOverflow);
+    }
+    a.inter_count[gi] = n_inter < a.inter_cap ? n_inter : a.inter_cap;
+    int n_intra = 0;
+    for (int w = 0; w < a.words; w++) n_intra += __popc(mask_rows[ii * a.words + w]);
+    a.ref_len[gi] = n_intra + n_inter;
+  }
+}
+
+}  // namespace souffle
+
+namespace souffle {
+void launch_cells_count(const CellArgs& a, int grid, int block, cudaStream_t s) {
+  k_cells_count<<<grid, block, 0, s>>>(a);
+}
+void launch_cells_scan(const CellArgs& a, cudaStream_t s) { k_cells_scan<<<1, 1024, 0, s>>>(a); }
+void launch_cells_scatter(const CellArgs& a, int grid, int block, cudaStream_t s) {
+  k_cells_scatter<<<grid, block, 0, s>>>(a);
+}
+void launch_candidates(const CandArgs& a, int grid, int block, cudaStream_t s) {
+  k_candidates<<<grid, block, 0, s>>>(a);
+}
+void launch_pairs(const PairArgs& a, int n_sub, size_t smem, cudaStream_t s) {
+  k_pairs<<<n_sub, 128, smem, s>>>(a);
+}
+cudaError_t set_pairs_smem(size_t smem) {
+  return cudaFuncSetAttribute(k_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+}  // namespace souffle

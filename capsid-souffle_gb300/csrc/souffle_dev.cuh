@@ -1,0 +1,142 @@
+// Device-side data layout shared by the kernels of the SOUFFLE force-and-integrate path.
+//
+// Layout in HBM (structure of arrays, systems concatenated):
+//   pos_fx[3][N]   int64 fixed-point positions: coordinate = value * L / 2^64, so the periodic
+//                  box maps onto the full int64 range and the minimum image of a difference is
+//                  plain two's-complement wrap-around (the reference's single-shift image,
+//                  src/functions.h:42-56, for any |d| < L/2).
+//   pos32[N]       int4 {x>>32, y>>32, z>>32, meta}: the rounded high words read by the pair
+//                  kernels with one 16-byte load; meta = template-local bead index.
+//   vel[3][N]      double velocities.
+//   force[3][N]    double total force (written from the 64-bit fixed-point sum).
+//   intra_mask     per subunit, np rows of ceil(np/32) words: bit jj of row ii is set when the
+//                  intra-subunit pair (ii, jj) is on bead ii's reference pair list.
+//   inter_ids      [cap][N] column-major global ids of inter-subunit neighbours, ascending.
+#pragma once
+#include <cstdint>
+
+namespace souffle {
+
+constexpr int kMaxNp = 256;        // beads per subunit
+constexpr int kMaxChain = 16;      // Nose-Hoover chain links
+constexpr int kMaxSpecies = 16;
+constexpr double kTwo32 = 4294967296.0;
+
+// Template tables, packed into one int buffer and one float buffer so a CTA can stage them into
+// shared memory with two bulk copies.  Offsets are in elements.
+struct TplLayout {
+  int np, ne, nf, nbend;
+  int words;          // 32-bit words per intra-mask row
+  int maxdeg;         // max edges per bead
+  int maxrole;        // max bending roles per bead
+  // int buffer offsets
+  int o_edge;         // [ne] packed (b0 | b1 << 16)
+  int o_face;         // [nf*3]
+  int o_bend;         // [nbend*4] b0, b1, across0, across1
+  int o_bendf;        // [nbend*2] face0, face1
+  int o_bead_edges;   // [np*maxdeg] edge index or -1
+  int o_bead_roles;   // [np*maxrole] bend*4+role or -1
+  int o_type;         // [np]
+  int o_species;      // [np]
+  int n_int;          // total ints
+  // float buffer offsets
+  int o_len0;         // [ne]
+  int o_q;            // [np]
+  int o_sigma;        // [np]
+  int n_float;
+  int nspecies;
+  int lj_att_bits[kMaxSpecies];  // bit js of row is: (species is -> js) attractive
+  int type7_bits;                // bit js: species js has type 7 (attractive epsilon 50)
+};
+
+// Per-system constants (one entry per replica).
+struct SysParams {
+  double box;          // L
+  double fx_to_len;    // L / 2^64
+  double len_to_fx;    // 2^64 / L (applied through split conversion)
+  float unit32;        // L / 2^32: length of one unit of the high word
+  float ks, kb;
+  float kappa;
+  float ecut2;         // LJ cut-off squared
+  float ecut_el2;      // DH cut-off squared (+inf when the reference has no cut-off)
+  float elj_att;
+  float nl2_f;         // pair-list radius squared (float)
+  double nl2;          // pair-list radius squared, exactly the reference's double
+  double pre2;         // prefilter: 2.25 * nl2 (src/functions.cpp:91)
+  int bead0, sub0, n_sub;   // first bead / subunit, subunit count
+  int cell0, ncell;         // first cell, cells per dimension (subunit-centre grid)
+  int quirks;               // reproduce src/functions.cpp:97
+  int center_local;         // template-local centre bead (src/initialize.cpp:266-288)
+  double dt;
+  double ks_d, kb_d;        // double copies for the FP64 energy pass
+};
+
+// Thermostat chain and step scalars of one system, updated on the device.
+// xi/eta is the chain after the forward half of the last step (what energy output reads);
+// xi_b/eta_b is the chain after the backward half of the next step (what the next step
+// integrates with).  Both halves only need particle_ke, so the backward half of step a+1 is
+// applied right after the forward half of step a.
+struct SysState {
+  int m;                 // chain length
+  int n_beads;           // beads in this system
+  double q[kMaxChain], t[kMaxChain], dof[kMaxChain];
+  double xi[kMaxChain], eta[kMaxChain];
+  double xi_b[kMaxChain], eta_b[kMaxChain];
+  double ke;             // particle_ke carried between steps (src/md.cpp:456)
+  double expfac;         // exp(-dt xi0 / 2) for the next step (src/md.cpp:406)
+  double vcom[3];        // mean velocity still to subtract from vel (0 once applied)
+  double vcom_mag;       // |mean velocity| removed at the last step (src/md.cpp:623)
+  unsigned int done;     // arrival counter for the last-block reduction
+  unsigned int steps;    // MD steps completed since md_begin
+};
+
+// Work item: a run of subunits of one system handled by one CTA.
+struct WorkItem {
+  int sys, sub_begin, nsub, slot;
+};
+
+// Pair-species tables for the LJ/WCA branch of src/forces.cpp:112-138.
+struct PairTable {
+  float sig6[kMaxSpecies * kMaxSpecies];   // sigma_i^6 (attractive) or shc^6 (WCA)
+  float cut2[kMaxSpecies * kMaxSpecies];   // ecut^2 (attractive) or (1.12246205 shc)^2
+  float skip2[kMaxSpecies * kMaxSpecies];  // max(ecut^2, (1.12246205 shc)^2): beyond it no LJ
+};
+
+// Error flags raised by kernels and read by the host.
+enum : unsigned int {
+  kErrInterOverflow = 1u,
+  kErrCandOverflow = 2u,
+  kErrNonFinite = 4u,
+};
+
+__host__ __device__ inline long long fixed_from_fraction(double f) {
+  // round(f * 2^64) modulo 2^64, for |f| < 2^20: split so no step overflows
+  double a = f * kTwo32;
+#ifdef __CUDA_ARCH__
+  double ip = rint(a);
+#else
+  double ip = __builtin_rint(a);
+#endif
+  double rem = a - ip;  // exact, |rem| <= 0.5
+#ifdef __CUDA_ARCH__
+  long long lo = __double2ll_rn(rem * kTwo32);
+#else
+  long long lo = (long long)__builtin_llrint(rem * kTwo32);
+#endif
+  unsigned long long hi = (unsigned long long)(long long)ip;
+  return (long long)((hi << 32) + (unsigned long long)lo);
+}
+
+__host__ __device__ inline int hi_word(long long x) {
+  return (int)(unsigned int)(((unsigned long long)x + 0x80000000ull) >> 32);
+}
+
+__host__ __device__ inline double fixed_diff(long long a, long long b, double fx_to_len) {
+  return (double)(long long)((unsigned long long)a - (unsigned long long)b) * fx_to_len;
+}
+
+__device__ inline float hi_diff(int a, int b, float unit) {
+  return (float)(int)((unsigned int)a - (unsigned int)b) * unit;
+}
+
+}  // namespace souffle

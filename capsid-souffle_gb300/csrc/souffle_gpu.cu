@@ -1,0 +1,992 @@
+// Host side of the C ABI in include/souffle_gpu.h: template derivation, device buffers, launch
+// sequences and CUDA-graph windows for the MD loop.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "souffle_dev.cuh"
+#include "souffle_gpu.h"
+
+#include "kernels.cuh"
+
+using namespace souffle;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+souffle_status fail(souffle_status s, const std::string& msg) {
+  g_last_error = msg;
+  return s;
+}
+
+#define CUDA_TRY(x)                                                                         \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(SOUFFLE_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));     \
+  } while (0)
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    free();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, sizeof(T) * count);
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DevBuf() { free(); }
+};
+
+// Template tables derived on the host, following generate_lattice (src/initialize.cpp:317-401).
+struct HostTemplate {
+  int np = 0, ne = 0, nf = 0, n_lj = 0;
+  std::vector<int> type, edge, edge_type, face, lj;
+  std::vector<double> q, sigma, mass, len0;
+  std::vector<int> edge_f0, edge_f1;   // faces of each edge, face order
+  std::vector<int> bend_edge;          // bending edges in template order
+  std::vector<int> bend;               // [nb*4] b0, b1, across0, across1
+  std::vector<int> bendf;              // [nb*2]
+  std::vector<int> species;            // per bead
+  int nspecies = 0;
+  std::vector<double> sp_sigma;
+  std::vector<int> sp_type;
+  int maxdeg = 1, maxrole = 1;
+  std::vector<int> bead_edges, bead_roles;
+};
+
+souffle_status derive_template(const souffle_template* t, HostTemplate& h) {
+  if (!t || t->np <= 0 || t->np > kMaxNp || t->ne < 0 || t->nf < 0 || t->n_lj < 0)
+    return fail(SOUFFLE_ERR_BAD_INPUT, "template sizes out of range (np must be 1..256)");
+  h.np = t->np;
+  h.ne = t->ne;
+  h.nf = t->nf;
+  h.n_lj = t->n_lj;
+  h.type.assign(t->bead_type, t->bead_type + h.np);
+  h.q.assign(t->bead_charge, t->bead_charge + h.np);
+  h.sigma.assign(t->bead_sigma, t->bead_sigma + h.np);
+  h.mass.assign(t->bead_mass, t->bead_mass + h.np);
+  h.edge.assign(t->edge_beads, t->edge_beads + 2 * h.ne);
+  h.edge_type.assign(t->edge_type, t->edge_type + h.ne);
+  h.len0.assign(t->edge_len0, t->edge_len0 + h.ne);
+  h.face.assign(t->face_beads, t->face_beads + 3 * h.nf);
+  h.lj.assign(t->lj_types, t->lj_types + 2 * h.n_lj);
+  for (int v : h.edge)
+    if (v < 0 || v >= h.np) return fail(SOUFFLE_ERR_BAD_INPUT, "edge bead index out of range");
+  for (int v : h.face)
+    if (v < 0 || v >= h.np) return fail(SOUFFLE_ERR_BAD_INPUT, "face bead index out of range");
+  for (double m : h.mass)
+    if (!(m > 0)) return fail(SOUFFLE_ERR_BAD_INPUT, "bead masses must be positive");
+  // face <-> edge matching: a face joins an edge's face list (in face order) when any of its
+  // three sides is the edge, in either orientation (src/initialize.cpp:370-401)
+  h.edge_f0.assign(h.ne, -1);
+  h.edge_f1.assign(h.ne, -1);
+  std::vector<int> nfe(h.ne, 0);
+  for (int f = 0; f < h.nf; f++) {
+    int a = h.face[3 * f], b = h.face[3 * f + 1], c = h.face[3 * f + 2];
+    for (int e = 0; e < h.ne; e++) {
+      int e0 = h.edge[2 * e], e1 = h.edge[2 * e + 1];
+      int hits = 0;
+      if (a == e0 && b == e1) hits++;
+      else if (a == e1 && b == e0) hits++;
+      if (a == e0 && c == e1) hits++;
+      else if (a == e1 && c == e0) hits++;
+      if (b == e1 && c == e0) hits++;
+      else if (b == e0 && c == e1) hits++;
+      for (int k = 0; k < hits; k++) {
+        if (nfe[e] == 0) h.edge_f0[e] = f;
+        else if (nfe[e] == 1) h.edge_f1[e] = f;
+        nfe[e]++;
+      }
+    }
+  }
+  // bending quads: itsB[0], itsB[1], FACE::across of each face (src/face.cpp:27-34)
+  auto across = [&](int f, int b0, int b1) {
+    for (int k = 0; k < 3; k++) {
+      int b = h.face[3 * f + k];
+      if (b != b0 && b != b1) return b;
+    }
+    return -1;
+  };
+  for (int e = 0; e < h.ne; e++) {
+    if (h.edge_type[e] == 0) continue;
+    if (nfe[e] < 2)
+      return fail(SOUFFLE_ERR_BAD_INPUT,
+                  "bending edge " + std::to_string(e) + " does not have two faces");
+    int b0 = h.edge[2 * e], b1 = h.edge[2 * e + 1];
+    int r2 = across(h.edge_f0[e], b0, b1), r3 = across(h.edge_f1[e], b0, b1);
+    if (r2 < 0 || r3 < 0 || r2 == r3)
+      return fail(SOUFFLE_ERR_BAD_INPUT, "degenerate bending quad at edge " + std::to_string(e));
+    h.bend_edge.push_back(e);
+    h.bend.insert(h.bend.end(), {b0, b1, r2, r3});
+    h.bendf.insert(h.bendf.end(), {h.edge_f0[e], h.edge_f1[e]});
+  }
+  // BEAD::itsE order = template edge order (src/initialize.cpp:328-329)
+  std::vector<std::vector<int>> be(h.np), br(h.np);
+  for (int e = 0; e < h.ne; e++) {
+    be[h.edge[2 * e]].push_back(e);
+    be[h.edge[2 * e + 1]].push_back(e);
+  }
+  const int nb = (int)h.bend_edge.size();
+  for (int k = 0; k < nb; k++)
+    for (int r = 0; r < 4; r++) br[h.bend[4 * k + r]].push_back(4 * k + r);
+  for (int i = 0; i < h.np; i++) {
+    h.maxdeg = std::max<int>(h.maxdeg, (int)be[i].size() + 1);
+    h.maxrole = std::max<int>(h.maxrole, (int)br[i].size() + 1);
+  }
+  h.bead_edges.assign(h.np * h.maxdeg, -1);
+  h.bead_roles.assign(h.np * h.maxrole, -1);
+  for (int i = 0; i < h.np; i++) {
+    for (size_t k = 0; k < be[i].size(); k++) h.bead_edges[i * h.maxdeg + k] = be[i][k];
+    for (size_t k = 0; k < br[i].size(); k++) h.bead_roles[i * h.maxrole + k] = br[i][k];
+  }
+  // species: distinct (type, sigma) pairs
+  h.species.assign(h.np, 0);
+  for (int i = 0; i < h.np; i++) {
+    int s = -1;
+    for (int k = 0; k < h.nspecies; k++)
+      if (h.sp_type[k] == h.type[i] && h.sp_sigma[k] == h.sigma[i]) s = k;
+    if (s < 0) {
+      if (h.nspecies == kMaxSpecies)
+        return fail(SOUFFLE_ERR_BAD_INPUT, "more than 16 distinct (type, diameter) bead species");
+      s = h.nspecies++;
+      h.sp_type.push_back(h.type[i]);
+      h.sp_sigma.push_back(h.sigma[i]);
+    }
+    h.species[i] = s;
+  }
+  return SOUFFLE_OK;
+}
+
+}  // namespace
+
+struct souffle_gpu_system {
+  HostTemplate tpl;
+  TplLayout L{};
+  std::vector<souffle_params> prm;
+  std::vector<SysParams> sp;
+  souffle_options opt{};
+  int n_sys = 0;
+  int64_t N = 0;
+  int S = 0;
+  int subs_per_cta = 1;
+  int threads = 128;
+  int total_cells = 0;
+  std::vector<WorkItem> work;
+  std::vector<int2> slots;
+  int inter_cap = 96, cand_cap = 128;
+  size_t force_smem = 0, pair_smem = 0;
+  cudaStream_t stream = nullptr;
+  bool began = false, have_state = false;
+  // device
+  DevBuf<int> tpl_i;
+  DevBuf<float> tpl_f;
+  DevBuf<SysParams> d_sys;
+  DevBuf<SysState> d_state;
+  DevBuf<WorkItem> d_work;
+  DevBuf<int2> d_slots;
+  DevBuf<int> d_sub_sys, d_bead_sys;
+  DevBuf<long long> pos_fx;
+  DevBuf<int4> pos32;
+  DevBuf<double> vel, force, sbforce, partial, staging;
+  DevBuf<unsigned int> intra_mask;
+  DevBuf<int> inter_ids, inter_count, ref_len;
+  DevBuf<int> cand, cand_count;
+  DevBuf<int> cell_count, cell_start, sub_rank, sub_cell, cell_subs;
+  DevBuf<float> dh_w;
+  DevBuf<PairTable> pt;
+  DevBuf<double> inv_mass, mass_d, q_d, sigma_d, len0_d;
+  DevBuf<int> type_d, lj_d;
+  DevBuf<double> e_bead, e_tot;
+  DevBuf<unsigned int> err;
+  // graphs keyed by window length
+  std::map<int, cudaGraphExec_t> graphs;
+  ~souffle_gpu_system() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+souffle_status upload(souffle_gpu_system* h) {
+  HostTemplate& T = h->tpl;
+  TplLayout& L = h->L;
+  std::vector<int> ti;
+  std::vector<float> tf;
+  L.np = T.np;
+  L.ne = T.ne;
+  L.nf = T.nf;
+  L.nbend = (int)T.bend_edge.size();
+  L.words = (T.np + 31) / 32;
+  L.maxdeg = T.maxdeg;
+  L.maxrole = T.maxrole;
+  L.o_edge = (int)ti.size();
+  for (int e = 0; e < T.ne; e++) ti.push_back(T.edge[2 * e] | (T.edge[2 * e + 1] << 16));
+  L.o_face = (int)ti.size();
+  ti.insert(ti.end(), T.face.begin(), T.face.end());
+  L.o_bend = (int)ti.size();
+  ti.insert(ti.end(), T.bend.begin(), T.bend.end());
+  L.o_bendf = (int)ti.size();
+  ti.insert(ti.end(), T.bendf.begin(), T.bendf.end());
+  L.o_bead_edges = (int)ti.size();
+  ti.insert(ti.end(), T.bead_edges.begin(), T.bead_edges.end());
+  L.o_bead_roles = (int)ti.size();
+  ti.insert(ti.end(), T.bead_roles.begin(), T.bead_roles.end());
+  L.o_type = (int)ti.size();
+  ti.insert(ti.end(), T.type.begin(), T.type.end());
+  L.o_species = (int)ti.size();
+  ti.insert(ti.end(), T.species.begin(), T.species.end());
+  while (ti.size() % 4) ti.push_back(0);
+  L.n_int = (int)ti.size();
+  L.o_len0 = (int)tf.size();
+  for (double v : T.len0) tf.push_back((float)v);
+  L.o_q = (int)tf.size();
+  for (double v : T.q) tf.push_back((float)v);
+  L.o_sigma = (int)tf.size();
+  for (double v : T.sigma) tf.push_back((float)v);
+  while (tf.size() % 4) tf.push_back(0.f);
+  L.n_float = (int)tf.size();
+  L.nspecies = T.nspecies;
+  // directed attraction (src/forces.cpp:119-125) and the type-7 epsilon (src/forces.cpp:127)
+  L.type7_bits = 0;
+  for (int a = 0; a < T.nspecies; a++) {
+    L.lj_att_bits[a] = 0;
+    if (T.sp_type[a] == 7) L.type7_bits |= 1 << a;
+    for (int b = 0; b < T.nspecies; b++)
+      for (int k = 0; k < T.n_lj; k++)
+        if (T.sp_type[a] == T.lj[2 * k] && T.sp_type[b] == T.lj[2 * k + 1]) L.lj_att_bits[a] |= 1 << b;
+  }
+  CUDA_TRY(h->tpl_i.alloc(ti.size()));
+  CUDA_TRY(h->tpl_f.alloc(tf.size()));
+  CUDA_TRY(cudaMemcpy(h->tpl_i.p, ti.data(), ti.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(h->tpl_f.p, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice));
+
+  // pair-species tables (ecut is common to all systems: it depends only on sigma in nm)
+  PairTable pt{};
+  const double replj2 = 1.12246205 * 1.12246205;
+  const double ecut = h->prm[0].ecut;
+  for (int a = 0; a < T.nspecies; a++)
+    for (int b = 0; b < T.nspecies; b++) {
+      const int idx = a * kMaxSpecies + b;
+      const double s1 = T.sp_sigma[a], s2 = T.sp_sigma[b], shc = (s1 + s2) / 2;
+      const bool att = (L.lj_att_bits[a] >> b) & 1;
+      pt.sig6[idx] = (float)(att ? std::pow(s1, 6) : std::pow(shc, 6));
+      pt.cut2[idx] = (float)(att ? ecut * ecut : replj2 * shc * shc);
+      pt.skip2[idx] = (float)std::max(ecut * ecut, replj2 * shc * shc);
+    }
+  CUDA_TRY(h->pt.alloc(1));
+  CUDA_TRY(cudaMemcpy(h->pt.p, &pt, sizeof(pt), cudaMemcpyHostToDevice));
+
+  // per-system DH weights w = q exp(kappa s/2) / (1 + kappa s/2) sqrt(lb): w_i w_j reproduces
+  // q_i q_j lb exp(kappa shc) / ((1 + kappa s_i/2)(1 + kappa s_j/2)) of src/forces.cpp:98-103
+  std::vector<float> w(h->n_sys * T.np);
+  for (int s = 0; s < h->n_sys; s++) {
+    const double k = h->prm[s].kappa, lb = h->prm[s].lb;
+    for (int i = 0; i < T.np; i++)
+      w[s * T.np + i] = (float)(T.q[i] * std::exp(k * T.sigma[i] / 2) / (1 + k * T.sigma[i] / 2) * std::sqrt(lb));
+  }
+  CUDA_TRY(h->dh_w.alloc(w.size()));
+  CUDA_TRY(cudaMemcpy(h->dh_w.p, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+
+  std::vector<double> im(T.np);
+  for (int i = 0; i < T.np; i++) im[i] = 1.0 / T.mass[i];
+  CUDA_TRY(h->inv_mass.alloc(T.np));
+  CUDA_TRY(cudaMemcpy(h->inv_mass.p, im.data(), T.np * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->mass_d.alloc(T.np));
+  CUDA_TRY(cudaMemcpy(h->mass_d.p, T.mass.data(), T.np * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->q_d.alloc(T.np));
+  CUDA_TRY(cudaMemcpy(h->q_d.p, T.q.data(), T.np * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->sigma_d.alloc(T.np));
+  CUDA_TRY(cudaMemcpy(h->sigma_d.p, T.sigma.data(), T.np * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->len0_d.alloc(std::max(1, T.ne)));
+  if (T.ne) CUDA_TRY(cudaMemcpy(h->len0_d.p, T.len0.data(), T.ne * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->type_d.alloc(T.np));
+  CUDA_TRY(cudaMemcpy(h->type_d.p, T.type.data(), T.np * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->lj_d.alloc(std::max(2, 2 * T.n_lj)));
+  if (T.n_lj) CUDA_TRY(cudaMemcpy(h->lj_d.p, T.lj.data(), 2 * T.n_lj * sizeof(int), cudaMemcpyHostToDevice));
+  return SOUFFLE_OK;
+}
+
+souffle_status check_err(souffle_gpu_system* h) {
+  unsigned int e = 0;
+  CUDA_TRY(cudaMemcpyAsync(&e, h->err.p, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (e) {
+    CUDA_TRY(cudaMemsetAsync(h->err.p, 0, sizeof(unsigned int), h->stream));
+    if (e & kErrNonFinite) return fail(SOUFFLE_ERR_NONFINITE, "non-finite force or kinetic energy");
+    if (e & kErrInterOverflow)
+      return fail(SOUFFLE_ERR_NL_OVERFLOW, "inter-subunit pair list exceeded inter_capacity");
+    if (e & kErrCandOverflow)
+      return fail(SOUFFLE_ERR_NL_OVERFLOW, "candidate subunit list exceeded cand_capacity");
+  }
+  return SOUFFLE_OK;
+}
+
+CellArgs cell_args(souffle_gpu_system* h) {
+  CellArgs a{};
+  a.px = h->pos_fx.p;
+  a.py = h->pos_fx.p + h->N;
+  a.pz = h->pos_fx.p + 2 * h->N;
+  a.sys = h->d_sys.p;
+  a.sub_sys = h->d_sub_sys.p;
+  a.np = h->tpl.np;
+
+  a.n_sub_total = h->S;
+  a.cell_count = h->cell_count.p;
+  a.cell_start = h->cell_start.p;
+  a.sub_rank = h->sub_rank.p;
+  a.sub_cell = h->sub_cell.p;
+  a.cell_subs = h->cell_subs.p;
+  a.total_cells = h->total_cells;
+  return a;
+}
+
+void launch_rebuild(souffle_gpu_system* h) {
+  cudaStream_t st = h->stream;
+  CellArgs c = cell_args(h);
+  cudaMemsetAsync(h->cell_count.p, 0, sizeof(int) * h->total_cells, st);
+  const int tb = 128, gb = (h->S + tb - 1) / tb;
+  launch_cells_count(c, gb, tb, st);
+  launch_cells_scan(c, st);
+  launch_cells_scatter(c, gb, tb, st);
+  CandArgs ca{};
+  ca.c = c;
+  ca.cap = h->cand_cap;
+  ca.cand = h->cand.p;
+  ca.cand_count = h->cand_count.p;
+  ca.err = h->err.p;
+  launch_candidates(ca, gb, tb, st);
+  PairArgs pa{};
+  pa.px = c.px;
+  pa.py = c.py;
+  pa.pz = c.pz;
+  pa.pos32 = h->pos32.p;
+  pa.sys = h->d_sys.p;
+  pa.sub_sys = h->d_sub_sys.p;
+  pa.q = h->tpl_f.p + h->L.o_q;
+  pa.np = h->tpl.np;
+  pa.words = h->L.words;
+
+  pa.n_beads_total = (int)h->N;
+  pa.cand = h->cand.p;
+  pa.cand_count = h->cand_count.p;
+  pa.cand_cap = h->cand_cap;
+  pa.intra_mask = h->intra_mask.p;
+  pa.inter_ids = h->inter_ids.p;
+  pa.inter_count = h->inter_count.p;
+  pa.ref_len = h->ref_len.p;
+  pa.inter_cap = h->inter_cap;
+  pa.err = h->err.p;
+  launch_pairs(pa, h->S, h->pair_smem, st);
+}
+
+ForceArgs force_args(souffle_gpu_system* h, int mode, bool want_parts) {
+  ForceArgs a{};
+  a.L = h->L;
+  a.tpl_i = h->tpl_i.p;
+  a.tpl_f = h->tpl_f.p;
+  a.sys = h->d_sys.p;
+  a.state = h->d_state.p;
+  a.work = h->d_work.p;
+  a.sys_slots = h->d_slots.p;
+  a.pos32 = h->pos32.p;
+  a.intra_mask = h->intra_mask.p;
+  a.inter_ids = h->inter_ids.p;
+  a.inter_count = h->inter_count.p;
+  a.dh_w = h->dh_w.p;
+  a.pt = h->pt.p;
+  a.inv_mass = h->inv_mass.p;
+  const int64_t N = h->N;
+  a.fx = h->force.p;
+  a.fy = h->force.p + N;
+  a.fz = h->force.p + 2 * N;
+  a.vx = h->vel.p;
+  a.vy = h->vel.p + N;
+  a.vz = h->vel.p + 2 * N;
+  if (want_parts) {
+    a.sfx = h->sbforce.p;
+    a.sfy = h->sbforce.p + N;
+    a.sfz = h->sbforce.p + 2 * N;
+    a.bfx = h->sbforce.p + 3 * N;
+    a.bfy = h->sbforce.p + 4 * N;
+    a.bfz = h->sbforce.p + 5 * N;
+  }
+  a.partial = h->partial.p;
+  a.err = h->err.p;
+  a.n_beads_total = (int)N;
+  a.max_sub = h->subs_per_cta;
+  a.mode = mode;
+  return a;
+}
+
+DriftArgs drift_args(souffle_gpu_system* h) {
+  DriftArgs a{};
+  const int64_t N = h->N;
+  a.sys = h->d_sys.p;
+  a.state = h->d_state.p;
+  a.work = h->d_work.p;
+  a.inv_mass = h->inv_mass.p;
+  a.np = h->tpl.np;
+  a.fx = h->force.p;
+  a.fy = h->force.p + N;
+  a.fz = h->force.p + 2 * N;
+  a.vx = h->vel.p;
+  a.vy = h->vel.p + N;
+  a.vz = h->vel.p + 2 * N;
+  a.px = h->pos_fx.p;
+  a.py = h->pos_fx.p + N;
+  a.pz = h->pos_fx.p + 2 * N;
+  a.pos32 = h->pos32.p;
+  return a;
+}
+
+void launch_step(souffle_gpu_system* h, bool rebuild) {
+  launch_drift(drift_args(h), (int)h->work.size(), h->threads, h->stream);
+  if (rebuild) launch_rebuild(h);
+  launch_forces(force_args(h, 1, false), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* souffle_gpu_last_error(void) { return g_last_error.c_str(); }
+
+souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_params* params,
+                                  int32_t n_systems, const souffle_options* opts,
+                                  souffle_gpu_system** out) {
+  if (!out) return fail(SOUFFLE_ERR_BAD_INPUT, "out is NULL");
+  *out = nullptr;
+  if (!params || n_systems <= 0) return fail(SOUFFLE_ERR_BAD_INPUT, "need at least one system");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(SOUFFLE_ERR_NO_DEVICE, "no CUDA device available");
+  std::unique_ptr<souffle_gpu_system> h(new souffle_gpu_system());
+  if (opts) h->opt = *opts;
+  if (h->opt.device < 0 || h->opt.device >= ndev) return fail(SOUFFLE_ERR_BAD_INPUT, "bad device ordinal");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  souffle_status s = derive_template(tpl, h->tpl);
+  if (s != SOUFFLE_OK) return s;
+  const int np = h->tpl.np;
+  h->n_sys = n_systems;
+  h->prm.assign(params, params + n_systems);
+  for (int k = 0; k < n_systems; k++) {
+    const souffle_params& p = params[k];
+    if (p.n_subunits <= 0 || !(p.box > 0) || p.center_local < 0 || p.center_local >= np ||
+        p.chain_length < 1 || p.chain_length >= kMaxChain || p.build_freq <= 0 || !(p.dt > 0))
+      return fail(SOUFFLE_ERR_BAD_INPUT, "system " + std::to_string(k) + ": parameter out of range");
+    if (p.ecut != params[0].ecut)
+      return fail(SOUFFLE_ERR_BAD_INPUT, "all systems must share ecut (the bead size in nm)");
+    if ((int64_t)h->S + p.n_subunits > (int64_t)1 << 30)
+      return fail(SOUFFLE_ERR_BAD_INPUT, "too many subunits");
+    h->S += p.n_subunits;
+  }
+  h->N = (int64_t)h->S * np;
+  if (h->N > ((int64_t)1 << 31) - 1) return fail(SOUFFLE_ERR_BAD_INPUT, "too many beads");
+  h->inter_cap = h->opt.inter_capacity > 0 ? h->opt.inter_capacity : 96;
+  h->cand_cap = h->opt.cand_capacity > 0 ? h->opt.cand_capacity : 128;
+  h->threads = 128;
+  h->subs_per_cta = std::max(1, 128 / np);
+
+  // per-system constants, cell grids, work items
+  int sub0 = 0, cell0 = 0;
+  std::vector<int> sub_sys(h->S), bead_sys(h->N);
+  for (int k = 0; k < n_systems; k++) {
+    const souffle_params& p = params[k];
+    SysParams q{};
+    q.box = p.box;
+    q.fx_to_len = p.box / (kTwo32 * kTwo32);
+    q.len_to_fx = (kTwo32 * kTwo32) / p.box;
+    q.unit32 = (float)(p.box / kTwo32);
+    q.ks = (float)p.ks;
+    q.kb = (float)p.kb;
+    q.ks_d = p.ks;
+    q.kb_d = p.kb;
+    q.kappa = (float)p.kappa;
+    q.ecut2 = (float)(p.ecut * p.ecut);
+    q.ecut_el2 = p.ecut_el != 0 ? (float)(p.ecut_el * p.ecut_el) : INFINITY;
+    q.elj_att = (float)p.elj_att;
+    q.nl2 = p.nlist_cutoff * p.nlist_cutoff;
+    q.nl2_f = (float)q.nl2;
+    q.pre2 = q.nl2 * 2.25;
+    q.bead0 = sub0 * np;
+    q.sub0 = sub0;
+    q.n_sub = p.n_subunits;
+    // cell edge >= sqrt(pre2) = 1.5 r (src/functions.cpp:91); at most 256 cells per side
+    int nc = (int)std::floor(p.box / std::sqrt(q.pre2));
+    nc = std::max(1, std::min(nc, 256));
+    q.ncell = nc;
+    q.cell0 = cell0;
+    q.quirks = (h->opt.compat_quirks >= 0) ? 1 : 0;
+    q.center_local = p.center_local;
+    q.dt = p.dt;
+    h->sp.push_back(q);
+    for (int i = 0; i < p.n_subunits; i++) sub_sys[sub0 + i] = k;
+    for (int i = 0; i < p.n_subunits * np; i++) bead_sys[(int64_t)sub0 * np + i] = k;
+    int first_slot = (int)h->work.size();
+    for (int b = 0; b < p.n_subunits; b += h->subs_per_cta) {
+      WorkItem w{k, sub0 + b, std::min(h->subs_per_cta, p.n_subunits - b), (int)h->work.size()};
+      h->work.push_back(w);
+    }
+    h->slots.push_back(make_int2(first_slot, (int)h->work.size() - first_slot));
+    sub0 += p.n_subunits;
+    cell0 += nc * nc * nc;
+  }
+  h->total_cells = cell0;
+  CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  s = upload(h.get());
+  if (s != SOUFFLE_OK) return s;
+
+  const int64_t N = h->N;
+  const TplLayout& L = h->L;
+  CUDA_TRY(h->d_sys.alloc(n_systems));
+  CUDA_TRY(cudaMemcpy(h->d_sys.p, h->sp.data(), sizeof(SysParams) * n_systems, cudaMemcpyHostToDevice));
+  CUDA_TRY(h->d_state.alloc(n_systems));
+  CUDA_TRY(cudaMemset(h->d_state.p, 0, sizeof(SysState) * n_systems));
+  CUDA_TRY(h->d_work.alloc(h->work.size()));
+  CUDA_TRY(cudaMemcpy(h->d_work.p, h->work.data(), sizeof(WorkItem) * h->work.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->d_slots.alloc(n_systems));
+  CUDA_TRY(cudaMemcpy(h->d_slots.p, h->slots.data(), sizeof(int2) * n_systems, cudaMemcpyHostToDevice));
+  CUDA_TRY(h->d_sub_sys.alloc(h->S));
+  CUDA_TRY(cudaMemcpy(h->d_sub_sys.p, sub_sys.data(), sizeof(int) * h->S, cudaMemcpyHostToDevice));
+  CUDA_TRY(h->d_bead_sys.alloc(N));
+  CUDA_TRY(cudaMemcpy(h->d_bead_sys.p, bead_sys.data(), sizeof(int) * N, cudaMemcpyHostToDevice));
+  CUDA_TRY(h->pos_fx.alloc(3 * N));
+  CUDA_TRY(h->pos32.alloc(N));
+  CUDA_TRY(h->vel.alloc(3 * N));
+  CUDA_TRY(h->force.alloc(3 * N));
+  CUDA_TRY(h->sbforce.alloc(6 * N));
+  CUDA_TRY(h->staging.alloc(6 * N));
+  CUDA_TRY(h->partial.alloc(4 * h->work.size()));
+  CUDA_TRY(h->intra_mask.alloc((size_t)h->S * np * L.words));
+  CUDA_TRY(h->inter_ids.alloc((size_t)h->inter_cap * N));
+  CUDA_TRY(h->inter_count.alloc(N));
+  CUDA_TRY(h->ref_len.alloc(N));
+  CUDA_TRY(h->cand.alloc((size_t)h->cand_cap * h->S));
+  CUDA_TRY(h->cand_count.alloc(h->S));
+  CUDA_TRY(h->cell_count.alloc(h->total_cells));
+  CUDA_TRY(h->cell_start.alloc(h->total_cells + 1));
+  CUDA_TRY(h->sub_rank.alloc(h->S));
+  CUDA_TRY(h->sub_cell.alloc(h->S));
+  CUDA_TRY(h->cell_subs.alloc(h->S));
+  CUDA_TRY(h->err.alloc(1));
+  CUDA_TRY(cudaMemset(h->err.p, 0, sizeof(unsigned int)));
+  CUDA_TRY(h->e_tot.alloc(8));
+  CUDA_TRY(cudaMemset(h->intra_mask.p, 0, sizeof(unsigned int) * (size_t)h->S * np * L.words));
+  CUDA_TRY(cudaMemset(h->inter_count.p, 0, sizeof(int) * N));
+  CUDA_TRY(cudaMemset(h->force.p, 0, sizeof(double) * 3 * N));
+
+  h->force_smem = sizeof(float4) * h->subs_per_cta * (L.ne + L.nf + 4 * L.nbend) +
+                  sizeof(int4) * h->subs_per_cta * np + sizeof(double) * 4 * 32 +
+                  sizeof(float) * (np + L.n_float) + sizeof(int) * L.n_int;
+  h->pair_smem = np * (3 * sizeof(long long) + sizeof(int4) + sizeof(double) + sizeof(int) + sizeof(float));
+  if (h->force_smem > 200 * 1024) return fail(SOUFFLE_ERR_BAD_INPUT, "template too large for shared memory");
+  CUDA_TRY(set_kernel_smem(h->force_smem, h->pair_smem));
+  *out = h.release();
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_destroy(souffle_gpu_system* h) {
+  delete h;
+  return SOUFFLE_OK;
+}
+
+int64_t souffle_gpu_num_beads(const souffle_gpu_system* h) { return h ? h->N : 0; }
+
+souffle_status souffle_gpu_set_state(souffle_gpu_system* h, const double* pos, const double* vel) {
+  if (!h || !pos) return fail(SOUFFLE_ERR_BAD_INPUT, "null argument");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  const int64_t N = h->N;
+  CUDA_TRY(cudaMemcpyAsync(h->staging.p, pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, h->stream));
+  if (vel)
+    CUDA_TRY(cudaMemcpyAsync(h->staging.p + 3 * N, vel, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, h->stream));
+  StateArgs a{};
+  a.sys = h->d_sys.p;
+  a.state = h->d_state.p;
+  a.bead_sys = h->d_bead_sys.p;
+  a.np = h->tpl.np;
+  a.n = (int)N;
+  a.pos_in = h->staging.p;
+  a.vel_in = vel ? h->staging.p + 3 * N : nullptr;
+  a.px = h->pos_fx.p;
+  a.py = h->pos_fx.p + N;
+  a.pz = h->pos_fx.p + 2 * N;
+  a.pos32 = h->pos32.p;
+  a.vx = h->vel.p;
+  a.vy = h->vel.p + N;
+  a.vz = h->vel.p + 2 * N;
+  // reset thermostat/COM bookkeeping
+  CUDA_TRY(cudaMemsetAsync(h->d_state.p, 0, sizeof(SysState) * h->n_sys, h->stream));
+  launch_state_in(a, (int)((N + 255) / 256), 256, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  h->have_state = true;
+  h->began = false;
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_get_state(souffle_gpu_system* h, double* pos, double* vel) {
+  if (!h) return fail(SOUFFLE_ERR_BAD_INPUT, "null handle");
+  if (!h->have_state) return fail(SOUFFLE_ERR_STATE, "no state set");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  const int64_t N = h->N;
+  StateArgs a{};
+  a.sys = h->d_sys.p;
+  a.state = h->d_state.p;
+  a.bead_sys = h->d_bead_sys.p;
+  a.np = h->tpl.np;
+  a.n = (int)N;
+  a.px = h->pos_fx.p;
+  a.py = h->pos_fx.p + N;
+  a.pz = h->pos_fx.p + 2 * N;
+  a.vx = h->vel.p;
+  a.vy = h->vel.p + N;
+  a.vz = h->vel.p + 2 * N;
+  a.pos_out = pos ? h->staging.p : nullptr;
+  a.vel_out = vel ? h->staging.p + 3 * N : nullptr;
+  launch_state_out(a, (int)((N + 255) / 256), 256, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  if (pos) CUDA_TRY(cudaMemcpyAsync(pos, h->staging.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+  if (vel)
+    CUDA_TRY(cudaMemcpyAsync(vel, h->staging.p + 3 * N, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return SOUFFLE_OK;
+}
+
+static souffle_status copy_force_out(souffle_gpu_system* h, const double* dev3, double* host) {
+  // device SoA [3][N] -> host xyz interleaved
+  const int64_t N = h->N;
+  std::vector<double> tmp(3 * N);
+  CUDA_TRY(cudaMemcpyAsync(tmp.data(), dev3, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  for (int64_t i = 0; i < N; i++) {
+    host[3 * i] = tmp[i];
+    host[3 * i + 1] = tmp[N + i];
+    host[3 * i + 2] = tmp[2 * N + i];
+  }
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_forces(souffle_gpu_system* h, int32_t rebuild, double* tforce, double* sforce,
+                                  double* bforce) {
+  if (!h) return fail(SOUFFLE_ERR_BAD_INPUT, "null handle");
+  if (!h->have_state) return fail(SOUFFLE_ERR_STATE, "no state set");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  if (rebuild) launch_rebuild(h);
+  const bool parts = sforce || bforce;
+  launch_forces(force_args(h, 0, parts), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  souffle_status s = check_err(h);
+  if (s != SOUFFLE_OK) return s;
+  if (tforce && (s = copy_force_out(h, h->force.p, tforce)) != SOUFFLE_OK) return s;
+  if (sforce && (s = copy_force_out(h, h->sbforce.p, sforce)) != SOUFFLE_OK) return s;
+  if (bforce && (s = copy_force_out(h, h->sbforce.p + 3 * h->N, bforce)) != SOUFFLE_OK) return s;
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_get_pairlist(souffle_gpu_system* h, int32_t cap, int32_t* counts, int32_t* ids) {
+  if (!h || cap < 0) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  const int np = h->tpl.np, words = h->L.words;
+  const int64_t N = h->N;
+  std::vector<unsigned int> mask((size_t)h->S * np * words);
+  std::vector<int> icnt(N), iids((size_t)h->inter_cap * N);
+  CUDA_TRY(cudaMemcpyAsync(mask.data(), h->intra_mask.p, mask.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(icnt.data(), h->inter_count.p, N * 4, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(iids.data(), h->inter_ids.p, iids.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  // merge the intra-subunit block into the ascending inter list: the reference order
+  for (int64_t g = 0; g < N; g++) {
+    const int sub = (int)(g / np), l = (int)(g % np);
+    const int lo = sub * np, hi = lo + np;
+    std::vector<int> out;
+    int k = 0;
+    const int n_in = icnt[g];
+    while (k < n_in && iids[(size_t)k * N + g] < lo) out.push_back(iids[(size_t)k++ * N + g]);
+    for (int jj = 0; jj < np; jj++)
+      if (mask[((size_t)sub * np + l) * words + (jj >> 5)] >> (jj & 31) & 1u) out.push_back(lo + jj);
+    while (k < n_in) {
+      int v = iids[(size_t)k++ * N + g];
+      (void)hi;
+      out.push_back(v);
+    }
+    if (counts) counts[g] = (int)out.size();
+    if (ids) {
+      for (int c = 0; c < cap; c++) ids[(size_t)g * cap + c] = c < (int)out.size() ? out[c] : -1;
+    }
+  }
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_pairlist_stats(souffle_gpu_system* h, int32_t system, souffle_pairlist_stats* out) {
+  if (!h || !out || system < 0 || system >= h->n_sys) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  const SysParams& P = h->sp[system];
+  const int n = P.n_sub * h->tpl.np;
+  std::vector<int> len(n), icnt(n);
+  CUDA_TRY(cudaMemcpyAsync(len.data(), h->ref_len.p + P.bead0, n * 4, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(icnt.data(), h->inter_count.p + P.bead0, n * 4, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  double sum = 0;
+  int mx = 0, mi = 0, over = 0;
+  for (int i = 0; i < n; i++) {
+    sum += len[i];
+    mx = std::max(mx, len[i]);
+    mi = std::max(mi, icnt[i]);
+    if (len[i] > h->prm[system].nlist_capacity) over++;
+  }
+  out->mean_length = sum / n;
+  out->max_length = mx;
+  out->max_inter = mi;
+  out->over_reference_capacity = over;
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_energies(souffle_gpu_system* h, int32_t system, souffle_energies* out, double* se,
+                                    double* be, double* ne, double* ce, double* ke) {
+  if (!h || system < 0 || system >= h->n_sys) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  if (!h->have_state) return fail(SOUFFLE_ERR_STATE, "no state set");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  const SysParams& P = h->sp[system];
+  const souffle_params& p = h->prm[system];
+  const int n = P.n_sub * h->tpl.np;
+  if (h->e_bead.n < (size_t)5 * n) CUDA_TRY(h->e_bead.alloc((size_t)5 * n));
+  EnergyArgs a{};
+  a.L = h->L;
+  a.tpl_i = h->tpl_i.p;
+  a.sys = h->d_sys.p;
+  a.state = h->d_state.p;
+  const int64_t N = h->N;
+  a.px = h->pos_fx.p;
+  a.py = h->pos_fx.p + N;
+  a.pz = h->pos_fx.p + 2 * N;
+  a.pos32 = h->pos32.p;
+  a.vx = h->vel.p;
+  a.vy = h->vel.p + N;
+  a.vz = h->vel.p + 2 * N;
+  a.len0 = h->len0_d.p;
+  a.mass = h->mass_d.p;
+  a.q = h->q_d.p;
+  a.sigma = h->sigma_d.p;
+  a.type = h->type_d.p;
+  a.lj_t = h->lj_d.p;
+  a.n_lj = h->tpl.n_lj;
+  a.ecut = p.ecut;
+  a.elj_att = p.elj_att;
+  a.lb = p.lb;
+  a.kappa = p.kappa;
+  a.ecut_el = p.ecut_el;
+  a.sigma_max = *std::max_element(h->tpl.sigma.begin(), h->tpl.sigma.end());
+  a.sysid = system;
+  a.n0 = P.bead0;
+  a.n = n;
+  a.se = h->e_bead.p;
+  a.be = h->e_bead.p + n;
+  a.ne = h->e_bead.p + 2 * (size_t)n;
+  a.ce = h->e_bead.p + 3 * (size_t)n;
+  a.ke = h->e_bead.p + 4 * (size_t)n;
+  a.totals = h->e_tot.p;
+  launch_energies(a, n, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  double tot[8];
+  SysState S;
+  CUDA_TRY(cudaMemcpyAsync(tot, h->e_tot.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(&S, h->d_state.p + system, sizeof(SysState), cudaMemcpyDeviceToHost, h->stream));
+  double* outs[5] = {se, be, ne, ce, ke};
+  const int order[5] = {0, 1, 2, 3, 4};
+  for (int k = 0; k < 5; k++)
+    if (outs[k])
+      CUDA_TRY(cudaMemcpyAsync(outs[k], h->e_bead.p + (size_t)order[k] * n, sizeof(double) * n,
+                               cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (out) {
+    out->kinetic = tot[0];
+    out->stretching = tot[1];
+    out->bending = tot[2];
+    out->lj = tot[3];
+    out->electrostatic = tot[4];
+    // THERMOSTAT::potential_energy / kinetic_energy (src/thermostat.h:43-52), kB = 1
+    double tpe = 0, tke = 0;
+    for (int j = 0; j < S.m; j++) {
+      tpe += S.dof[j] * 1.0 * S.t[j] * S.eta[j];
+      tke += 0.5 * S.q[j] * S.xi[j] * S.xi[j];
+    }
+    out->thermo_pe = tpe;
+    out->thermo_ke = tke;
+    out->temperature = tot[0] * 2 / (3.0 * n);
+    out->vcom_magnitude = S.vcom_mag;
+  }
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_kinetic_energy(souffle_gpu_system* h, int32_t system, double* ke) {
+  souffle_energies e;
+  if (!ke) return fail(SOUFFLE_ERR_BAD_INPUT, "null output");
+  souffle_status s = souffle_gpu_energies(h, system, &e, nullptr, nullptr, nullptr, nullptr, nullptr);
+  if (s == SOUFFLE_OK) *ke = e.kinetic;
+  return s;
+}
+
+souffle_status souffle_gpu_md_begin(souffle_gpu_system* h) {
+  if (!h) return fail(SOUFFLE_ERR_BAD_INPUT, "null handle");
+  if (!h->have_state) return fail(SOUFFLE_ERR_STATE, "no state set");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  // thermostat chain (src/md.cpp:187-196): [Q, T, 3N], (1, T, 1)..., dummy (0, T, 3N)
+  std::vector<SysState> st(h->n_sys);
+  for (int k = 0; k < h->n_sys; k++) {
+    const souffle_params& p = h->prm[k];
+    SysState& S = st[k];
+    std::memset(&S, 0, sizeof(S));
+    const double n3 = 3.0 * p.n_subunits * h->tpl.np;
+    S.n_beads = p.n_subunits * h->tpl.np;
+    if (p.chain_length == 1) {
+      S.m = 1;
+      S.q[0] = 0;
+      S.t[0] = p.temperature;
+      S.dof[0] = n3;
+    } else {
+      int m = 0;
+      S.q[m] = p.nhc_mass;
+      S.t[m] = p.temperature;
+      S.dof[m++] = n3;
+      while (m != p.chain_length - 1) {
+        S.q[m] = 1;
+        S.t[m] = p.temperature;
+        S.dof[m++] = 1;
+      }
+      S.q[m] = 0;
+      S.t[m] = p.temperature;
+      S.dof[m++] = n3;
+      S.m = m;
+    }
+  }
+  CUDA_TRY(cudaMemcpyAsync(h->d_state.p, st.data(), sizeof(SysState) * h->n_sys, cudaMemcpyHostToDevice, h->stream));
+  // initial forces with a rebuild (src/md.cpp:241) and particle_ke (src/md.cpp:258); the last
+  // CTA then applies the backward half of the first step
+  launch_rebuild(h);
+  launch_forces(force_args(h, 2, false), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  souffle_status s = check_err(h);
+  if (s != SOUFFLE_OK) return s;
+  h->began = true;
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_md_steps(souffle_gpu_system* h, int64_t first_step, int32_t n_steps) {
+  if (!h || n_steps < 0 || first_step < 0) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  if (!h->began) return fail(SOUFFLE_ERR_STATE, "md_begin has not been called");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  // All systems share the rebuild period of system 0 (a batch is rebuilt together).
+  const int B = h->prm[0].build_freq;
+  int64_t a = first_step;
+  const int64_t end = first_step + n_steps;
+  // graphs: key 2*len + rebuild-first; a whole rebuild window is one graph of B steps, any other
+  // step is a one-step graph with or without the rebuild
+  auto run_graph = [&](int len, bool rebuild_first) -> souffle_status {
+    const int key = 2 * len + (rebuild_first ? 1 : 0);
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+      cudaGraph_t g;
+      CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < len; k++) launch_step(h, k == 0 && rebuild_first);
+      CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
+      cudaGraphExec_t ge;
+      CUDA_TRY(cudaGraphInstantiate(&ge, g, 0));
+      cudaGraphDestroy(g);
+      it = h->graphs.emplace(key, ge).first;
+    }
+    CUDA_TRY(cudaGraphLaunch(it->second, h->stream));
+    return SOUFFLE_OK;
+  };
+  while (a < end) {
+    souffle_status s;
+    if (a % B == 0 && end - a >= B) {
+      s = run_graph(B, true);
+      a += B;
+    } else {
+      s = run_graph(1, a % B == 0);
+      a += 1;
+    }
+    if (s != SOUFFLE_OK) return s;
+  }
+  CUDA_TRY(cudaGetLastError());
+  return check_err(h);
+}
+
+void* souffle_gpu_stream(souffle_gpu_system* h) { return h ? (void*)h->stream : nullptr; }
+
+souffle_status souffle_gpu_md_profile(souffle_gpu_system* h, int64_t first_step, int32_t n_steps,
+                                      souffle_kernel_times* out) {
+  if (!h || !out || n_steps < 0 || first_step < 0) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  if (!h->began) return fail(SOUFFLE_ERR_STATE, "md_begin has not been called");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  const int B = h->prm[0].build_freq;
+  std::memset(out, 0, sizeof(*out));
+  cudaEvent_t ev[4];
+  for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
+  souffle_status st = SOUFFLE_OK;
+  for (int64_t a = first_step; a < first_step + n_steps && st == SOUFFLE_OK; a++) {
+    const bool rb = (a % B == 0);
+    cudaEventRecord(ev[0], h->stream);
+    launch_drift(drift_args(h), (int)h->work.size(), h->threads, h->stream);
+    cudaEventRecord(ev[1], h->stream);
+    if (rb) launch_rebuild(h);
+    cudaEventRecord(ev[2], h->stream);
+    launch_forces(force_args(h, 1, false), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+    cudaEventRecord(ev[3], h->stream);
+    if (cudaEventSynchronize(ev[3]) != cudaSuccess) {
+      st = fail(SOUFFLE_ERR_CUDA, "event synchronize failed");
+      break;
+    }
+    float t0, t1, t2;
+    cudaEventElapsedTime(&t0, ev[0], ev[1]);
+    cudaEventElapsedTime(&t1, ev[1], ev[2]);
+    cudaEventElapsedTime(&t2, ev[2], ev[3]);
+    out->drift_ms += t0;
+    out->forces_ms += t2;
+    if (rb) {
+      out->rebuild_ms += t1;
+      out->rebuilds++;
+    }
+    out->steps++;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (st != SOUFFLE_OK) return st;
+  CUDA_TRY(cudaGetLastError());
+  return check_err(h);
+}
+
+souffle_status souffle_gpu_md_scalars(souffle_gpu_system* h, int32_t system, double* ke, double* xi0,
+                                      double* vcom) {
+  if (!h || system < 0 || system >= h->n_sys) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  SysState S;
+  CUDA_TRY(cudaMemcpyAsync(&S, h->d_state.p + system, sizeof(S), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (ke) *ke = S.ke;
+  if (xi0) *xi0 = S.xi[0];
+  if (vcom) *vcom = S.vcom_mag;
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_synchronize(souffle_gpu_system* h) {
+  if (!h) return fail(SOUFFLE_ERR_BAD_INPUT, "null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return SOUFFLE_OK;
+}
+
+}  // extern "C"

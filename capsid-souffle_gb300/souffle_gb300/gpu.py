@@ -1,0 +1,246 @@
+"""ctypes binding of the C ABI in include/souffle_gpu.h.
+
+The library is ``capsid-souffle_gb300/_build/libsouffle_gb300.so`` (built by
+``capsid-souffle_gb300/build.py``).  There is no fallback: if the library or a
+GPU is missing, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .geometry import Template
+from .params import CliOptions, Derived
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "_build", "libsouffle_gb300.so")
+
+STATUS = {0: "OK", 1: "BAD_INPUT", 2: "CUDA", 3: "NL_OVERFLOW", 4: "NONFINITE", 5: "NO_DEVICE",
+          6: "STATE"}
+
+EXPORTED = [
+    "souffle_gpu_create", "souffle_gpu_destroy", "souffle_gpu_num_beads", "souffle_gpu_set_state",
+    "souffle_gpu_get_state", "souffle_gpu_forces", "souffle_gpu_get_pairlist",
+    "souffle_gpu_pairlist_stats", "souffle_gpu_energies", "souffle_gpu_kinetic_energy",
+    "souffle_gpu_md_begin", "souffle_gpu_md_steps", "souffle_gpu_md_scalars",
+    "souffle_gpu_synchronize", "souffle_gpu_last_error", "souffle_gpu_stream",
+    "souffle_gpu_md_profile",
+]
+
+
+class SouffleError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Template_(C.Structure):
+    _fields_ = [("np", C.c_int32), ("ne", C.c_int32), ("nf", C.c_int32), ("n_lj", C.c_int32),
+                ("bead_type", C.POINTER(C.c_int32)), ("bead_charge", C.POINTER(C.c_double)),
+                ("bead_sigma", C.POINTER(C.c_double)), ("bead_mass", C.POINTER(C.c_double)),
+                ("edge_beads", C.POINTER(C.c_int32)), ("edge_type", C.POINTER(C.c_int32)),
+                ("edge_len0", C.POINTER(C.c_double)), ("face_beads", C.POINTER(C.c_int32)),
+                ("lj_types", C.POINTER(C.c_int32))]
+
+
+class Params_(C.Structure):
+    _fields_ = [("n_subunits", C.c_int32), ("box", C.c_double), ("ks", C.c_double),
+                ("kb", C.c_double), ("elj_att", C.c_double), ("lb", C.c_double),
+                ("kappa", C.c_double), ("ecut", C.c_double), ("ecut_el", C.c_double),
+                ("nlist_cutoff", C.c_double), ("nlist_capacity", C.c_int32),
+                ("center_local", C.c_int32), ("dt", C.c_double), ("chain_length", C.c_int32),
+                ("nhc_mass", C.c_double), ("temperature", C.c_double), ("build_freq", C.c_int32)]
+
+
+class Options_(C.Structure):
+    _fields_ = [("inter_capacity", C.c_int32), ("cand_capacity", C.c_int32),
+                ("compat_quirks", C.c_int32), ("device", C.c_int32),
+                ("threads_per_cta", C.c_int32)]
+
+
+class Energies_(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ["kinetic", "stretching", "bending", "lj", "electrostatic",
+                                           "thermo_pe", "thermo_ke", "temperature",
+                                           "vcom_magnitude"]]
+
+
+class PairStats_(C.Structure):
+    _fields_ = [("mean_length", C.c_double), ("max_length", C.c_int32), ("max_inter", C.c_int32),
+                ("over_reference_capacity", C.c_int32)]
+
+
+class KernelTimes_(C.Structure):
+    _fields_ = [("drift_ms", C.c_double), ("rebuild_ms", C.c_double), ("forces_ms", C.c_double),
+                ("steps", C.c_int32), ("rebuilds", C.c_int32)]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with capsid-souffle_gb300/build.py")
+    lib = C.CDLL(LIB_PATH)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    lib.souffle_gpu_create.argtypes = [C.POINTER(Template_), C.POINTER(Params_), C.c_int32,
+                                       C.POINTER(Options_), C.POINTER(vp)]
+    lib.souffle_gpu_destroy.argtypes = [vp]
+    lib.souffle_gpu_num_beads.restype = C.c_int64
+    lib.souffle_gpu_num_beads.argtypes = [vp]
+    lib.souffle_gpu_set_state.argtypes = [vp, dp, dp]
+    lib.souffle_gpu_get_state.argtypes = [vp, dp, dp]
+    lib.souffle_gpu_forces.argtypes = [vp, C.c_int32, dp, dp, dp]
+    lib.souffle_gpu_get_pairlist.argtypes = [vp, C.c_int32, ip, ip]
+    lib.souffle_gpu_pairlist_stats.argtypes = [vp, C.c_int32, C.POINTER(PairStats_)]
+    lib.souffle_gpu_energies.argtypes = [vp, C.c_int32, C.POINTER(Energies_), dp, dp, dp, dp, dp]
+    lib.souffle_gpu_kinetic_energy.argtypes = [vp, C.c_int32, dp]
+    lib.souffle_gpu_md_begin.argtypes = [vp]
+    lib.souffle_gpu_md_steps.argtypes = [vp, C.c_int64, C.c_int32]
+    lib.souffle_gpu_md_scalars.argtypes = [vp, C.c_int32, dp, dp, dp]
+    lib.souffle_gpu_synchronize.argtypes = [vp]
+    lib.souffle_gpu_last_error.restype = C.c_char_p
+    lib.souffle_gpu_stream.restype = C.c_void_p
+    lib.souffle_gpu_stream.argtypes = [vp]
+    lib.souffle_gpu_md_profile.argtypes = [vp, C.c_int64, C.c_int32, C.POINTER(KernelTimes_)]
+    for name in EXPORTED:
+        if name not in ("souffle_gpu_last_error", "souffle_gpu_num_beads", "souffle_gpu_stream"):
+            getattr(lib, name).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _check(code: int) -> None:
+    if code != 0:
+        msg = load().souffle_gpu_last_error().decode(errors="replace")
+        raise SouffleError(code, msg)
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def system_params(opt: CliOptions, d: Derived, n_sub: int, center_local: int) -> Params_:
+    """Reduced-unit parameters of one system, as run_simulation derives them."""
+    return Params_(int(n_sub), d.box, opt.s, opt.b, opt.E, d.lb, d.kappa, d.ecut, d.ecut_el,
+                   d.nlist_cutoff, d.nlist_capacity, int(center_local), opt.t, int(opt.q), opt.Q,
+                   d.T_reduced, int(opt.B))
+
+
+class GpuSystem:
+    """A handle over one or more systems sharing one template."""
+
+    def __init__(self, t: Template, params: Sequence[Params_], inter_capacity: int = 0,
+                 cand_capacity: int = 0, quirks: bool = True, device: int = 0):
+        self.lib = load()
+        self.t = t
+        self._arrs = dict(
+            type=np.ascontiguousarray(t.types, dtype=np.int32),
+            q=np.ascontiguousarray(t.charge, dtype=np.float64),
+            sig=np.ascontiguousarray(t.diameter, dtype=np.float64),
+            m=np.ascontiguousarray(t.mass, dtype=np.float64),
+            eb=np.ascontiguousarray(t.edges, dtype=np.int32).reshape(-1),
+            et=np.ascontiguousarray(t.edge_type, dtype=np.int32),
+            l0=np.ascontiguousarray(t.edge_len0, dtype=np.float64),
+            fb=np.ascontiguousarray(t.faces, dtype=np.int32).reshape(-1),
+            lj=np.ascontiguousarray(np.array(t.lj_attract, dtype=np.int32).reshape(-1)),
+        )
+        a = self._arrs
+        tpl = Template_(t.n_beads, len(t.edges), len(t.faces), len(t.lj_attract), _ip(a["type"]),
+                        _dp(a["q"]), _dp(a["sig"]), _dp(a["m"]), _ip(a["eb"]), _ip(a["et"]),
+                        _dp(a["l0"]), _ip(a["fb"]),
+                        _ip(a["lj"]) if a["lj"].size else None)
+        self.params = list(params)
+        arr = (Params_ * len(self.params))(*self.params)
+        opts = Options_(inter_capacity, cand_capacity, 1 if quirks else -1, device, 0)
+        h = C.c_void_p()
+        _check(self.lib.souffle_gpu_create(C.byref(tpl), arr, len(self.params), C.byref(opts),
+                                           C.byref(h)))
+        self.h = h
+        self.n = int(self.lib.souffle_gpu_num_beads(self.h))
+        self.np = t.n_beads
+        self.sys_beads = [p.n_subunits * self.np for p in self.params]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.souffle_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, pos, vel=None):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        assert pos.size == 3 * self.n
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        _check(self.lib.souffle_gpu_set_state(self.h, _dp(pos), None if v is None else _dp(v)))
+
+    def get_state(self):
+        pos = np.empty((self.n, 3))
+        vel = np.empty((self.n, 3))
+        _check(self.lib.souffle_gpu_get_state(self.h, _dp(pos), _dp(vel)))
+        return pos, vel
+
+    def forces(self, rebuild: bool = True, parts: bool = False):
+        tf = np.empty((self.n, 3))
+        sf = np.empty((self.n, 3)) if parts else None
+        bf = np.empty((self.n, 3)) if parts else None
+        _check(self.lib.souffle_gpu_forces(self.h, int(rebuild), _dp(tf),
+                                           None if sf is None else _dp(sf),
+                                           None if bf is None else _dp(bf)))
+        return (tf, sf, bf) if parts else tf
+
+    def pairlist(self, cap: int):
+        counts = np.empty(self.n, dtype=np.int32)
+        ids = np.empty((self.n, cap), dtype=np.int32)
+        _check(self.lib.souffle_gpu_get_pairlist(self.h, cap, _ip(counts), _ip(ids)))
+        return counts, ids
+
+    def pairlist_stats(self, system: int = 0) -> dict:
+        s = PairStats_()
+        _check(self.lib.souffle_gpu_pairlist_stats(self.h, system, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in PairStats_._fields_}
+
+    def energies(self, system: int = 0, per_bead: bool = False):
+        e = Energies_()
+        n = self.sys_beads[system]
+        arrs = [np.empty(n) for _ in range(5)] if per_bead else [None] * 5
+        _check(self.lib.souffle_gpu_energies(self.h, system, C.byref(e),
+                                             *[None if x is None else _dp(x) for x in arrs]))
+        tot = {f: getattr(e, f) for f, _ in Energies_._fields_}
+        if per_bead:
+            return tot, dict(zip(["se", "be", "ne", "ce", "ke"], arrs))
+        return tot
+
+    def md_begin(self):
+        _check(self.lib.souffle_gpu_md_begin(self.h))
+
+    def md_steps(self, first_step: int, n_steps: int):
+        _check(self.lib.souffle_gpu_md_steps(self.h, int(first_step), int(n_steps)))
+
+    def md_scalars(self, system: int = 0):
+        ke, xi0, vc = C.c_double(), C.c_double(), C.c_double()
+        _check(self.lib.souffle_gpu_md_scalars(self.h, system, C.byref(ke), C.byref(xi0),
+                                               C.byref(vc)))
+        return ke.value, xi0.value, vc.value
+
+    def synchronize(self):
+        _check(self.lib.souffle_gpu_synchronize(self.h))
+
+    def stream(self) -> int:
+        """The handle's cudaStream_t as an integer."""
+        return int(self.lib.souffle_gpu_stream(self.h) or 0)
+
+    def md_profile(self, first_step: int, n_steps: int) -> dict:
+        k = KernelTimes_()
+        _check(self.lib.souffle_gpu_md_profile(self.h, int(first_step), int(n_steps), C.byref(k)))
+        return {f: getattr(k, f) for f, _ in KernelTimes_._fields_}

@@ -1,0 +1,96 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs the reference SOUFFLE sources, compiled unmodified by oracle/ref.mk into
+oracle/_ref/ (ref_dump: one forceCalculation with a pair-list rebuild plus the
+energy block; ref_run: run_simulation), on seeded synthetic states, and stores
+inputs and outputs as .npz.  Needs the reference tree (default /root/reference,
+or REF=...) only when regenerating; the tests read the committed fixtures.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "capsid-souffle_gb300"))
+sys.path.insert(0, HERE)
+
+from souffle_gb300 import geometry, state, workloads  # noqa: E402
+import refdump  # noqa: E402
+
+CASES = [
+    # name, template, subunits, concentration (uM), seed, min gap between subunit spheres
+    ("plain_small", "patch_n3", 20, 800.0, 12345, 1.0),
+    ("bilayer_dense", "bilayer_n5", 30, 6000.0, 777, -1.5),
+    ("patch_crowded", "patch_n3", 60, 20000.0, 4242, -1.0),
+]
+MD_STEPS = 20
+
+
+def cli(name, S, C):
+    o = workloads.base_options()
+    return ["-f", name, "-S", str(S), "-C", repr(C), "-c", repr(o.c), "-s", repr(o.s), "-b",
+            repr(o.b), "-E", repr(o.E), "-e", repr(o.e), "-L", repr(o.L)]
+
+
+def main():
+    ref = os.environ.get("REF", "/root/reference")
+    subprocess.run(["make", "-f", os.path.join(REPO, "oracle", "ref.mk"), f"REF={ref}", "-j8"],
+                   check=True, stdout=subprocess.DEVNULL)
+    for name, tname, S, C, seed, gap in CASES:
+        t = geometry.template_by_name(tname)
+        L = state.box_length(S, C)
+        st = state.random_state(t, S, L, seed=seed, min_gap=gap)
+        with tempfile.TemporaryDirectory() as wd:
+            os.makedirs(f"{wd}/infiles")
+            os.makedirs(f"{wd}/outfiles")
+            geometry.write_infile(t, f"{wd}/infiles/{tname}")
+            state.write_restart(st, f"{wd}/outfiles")
+            # read back exactly what the reference reads
+            t2, _, _, _ = geometry.read_infile(f"{wd}/infiles/{tname}")
+            _, vel, pos = state.read_restart(f"{wd}/outfiles/restart_0.out")
+            d = refdump.run_dump(wd, cli(tname, S, C))
+            n = S * t.n_beads
+            cap = int(d["params"]["nlist_capacity"])
+            counts = np.array([len(x) for x in d["nlist"]], dtype=np.int32)
+            ids = np.full((n, max(1, counts.max())), -1, dtype=np.int32)
+            for i, lst in enumerate(d["nlist"]):
+                ids[i, :len(lst)] = lst
+            # MD: run_simulation for MD_STEPS steps from the same state
+            md = f"{wd}/md"
+            os.makedirs(f"{md}/outfiles")
+            shutil.copytree(f"{wd}/infiles", f"{md}/infiles")
+            for f in ("restart_0.out", "rb_0.out"):
+                shutil.copy(f"{wd}/outfiles/{f}", f"{md}/outfiles/{f}")
+            o = workloads.base_options()
+            args = cli(tname, S, C) + ["-D", "m", "-B", str(o.B), "-t", repr(o.t), "-q", str(int(o.q)),
+                                       "-Q", repr(o.Q), "-K", repr(o.K), "-T", str(MD_STEPS),
+                                       "-W", "1", "-M", "1000000", "-w", str(MD_STEPS)]
+            subprocess.run([refdump.REF_RUN] + args, cwd=md, check=True, capture_output=True)
+            _, vmd, pmd = state.read_restart(f"{md}/outfiles/restart_{MD_STEPS}.out")
+            rows = np.loadtxt(f"{md}/outfiles/energy.out", skiprows=1, usecols=range(11))
+            np.savez_compressed(
+                os.path.join(HERE, f"{name}.npz"),
+                template=np.array(tname), n_sub=S, conc=C, seed=seed, gap=gap,
+                pos=pos, vel=vel, box=d["params"]["box"], center=int(d["params"]["center_bead"]),
+                kappa=d["params"]["kappa"], ecut_el=d["params"]["ecut_el"],
+                nlist_cutoff=d["params"]["nlist_cutoff"], nlist_capacity=cap,
+                ld_mant_dig=int(d["params"]["long_double_mant_dig"]),
+                tforce=d["tforce"], sforce=d["sforce"], bforce=d["bforce"],
+                nl_counts=counts, nl_ids=ids,
+                se=d["se"], ke=d["ke"], be=d["be"], ne=d["ne"], ce=d["ce"], ke_total=d["ke_total"],
+                md_steps=MD_STEPS, md_pos=pmd, md_vel=vmd, md_energy_rows=rows,
+            )
+            print(name, n, "beads; mean list", counts.mean(), "max", counts.max(), "cap", cap)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+"""GPU path (through the C ABI) against the reference's fixtures and the oracle.
+
+Tolerances: forces are FP32 with 64-bit fixed-point accumulation, so the per-bead
+force RMS relative error against the FP64/long-double reference must be <= 1e-5;
+pair sets are integer results and must be identical; energies are FP64 sums of
+exact-difference terms (relative 1e-9 of the total scale).
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, golden_workload, load_golden, rms_rel
+
+pytestmark = pytest.mark.gpu
+FORCE_RMS_TOL = 1e-5
+
+
+def _gpu(g, **kw):
+    from souffle_gb300 import gpu
+    t, opt, d = golden_workload(g)
+    p = gpu.system_params(opt, d, int(g["n_sub"]), int(g["center"]))
+    s = gpu.GpuSystem(t, [p], **kw)
+    s.set_state(g["pos"], g["vel"])
+    return s, t, opt, d
+
+
+def _ref_sets(g):
+    c, ids = g["nl_counts"], g["nl_ids"]
+    return [set(ids[i, :c[i]].tolist()) for i in range(len(c))]
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_forces_match_reference(name):
+    g = load_golden(name)
+    s, t, opt, d = _gpu(g)
+    tf, sf, bf = s.forces(rebuild=True, parts=True)
+    assert rms_rel(tf, g["tforce"]) <= FORCE_RMS_TOL, rms_rel(tf, g["tforce"])
+    assert rms_rel(bf, g["bforce"]) <= FORCE_RMS_TOL
+    # stretching forces are tiny at rest length; compare against the total force scale
+    assert np.sqrt(((sf - g["sforce"]) ** 2).sum() / (g["tforce"] ** 2).sum()) <= FORCE_RMS_TOL
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_pairlist_identical_to_reference(name):
+    g = load_golden(name)
+    s, t, opt, d = _gpu(g)
+    s.forces(rebuild=True)
+    cap = int(g["nlist_capacity"])
+    counts, ids = s.pairlist(cap)
+    assert np.array_equal(counts, g["nl_counts"])
+    w = g["nl_ids"].shape[1]
+    assert np.array_equal(ids[:, :w], g["nl_ids"])   # same entries in the same (ascending) order
+    st = s.pairlist_stats()
+    assert st["mean_length"] == pytest.approx(g["nl_counts"].mean())
+    assert st["max_length"] == g["nl_counts"].max()
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_energies_match_reference(name):
+    g = load_golden(name)
+    s, t, opt, d = _gpu(g)
+    tot, pb = s.energies(per_bead=True)
+    scale = max(1.0, sum(abs(g[k]).sum() for k in ("se", "be", "ne", "ce", "ke")))
+    for k in ("se", "be", "ne", "ce", "ke"):
+        np.testing.assert_allclose(pb[k], g[k], rtol=1e-7, atol=1e-9 * scale / len(g[k]))
+    assert tot["kinetic"] == pytest.approx(g["ke"].sum(), rel=1e-12)
+    assert tot["lj"] == pytest.approx(g["ne"].sum(), rel=1e-9, abs=1e-9)
+    assert tot["electrostatic"] == pytest.approx(g["ce"].sum(), rel=1e-9, abs=1e-9)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_md_steps_match_reference_run(name):
+    g = load_golden(name)
+    s, t, opt, d = _gpu(g)
+    s.md_begin()
+    n = int(g["md_steps"]) + 1        # loop runs T+1 iterations (src/md.cpp:387)
+    s.md_steps(0, n)
+    pos, vel = s.get_state()
+    L = float(g["box"])
+    dp = pos - g["md_pos"]
+    dp -= L * np.round(dp / L)
+    assert np.abs(dp).max() < 1e-6
+    assert np.abs(vel - g["md_vel"]).max() < 1e-5 * max(1.0, np.abs(g["md_vel"]).max())
+    # temperature column of energy.out (6 significant digits in the reference file)
+    tot = s.energies()
+    assert tot["temperature"] == pytest.approx(g["md_energy_rows"][-1, 8], rel=2e-5)
+
+
+def test_md_long_run_tracks_oracle():
+    """100 steps at 2000-bead scale: KE and thermostat trajectories against the oracle."""
+    import pyoracle
+    g = load_golden("bilayer_dense")
+    s, t, opt, d = _gpu(g)
+    o = pyoracle.Oracle(t, int(g["n_sub"]), d, opt.s, opt.b, opt.E, int(g["center"]))
+    o.set_state(g["pos"], g["vel"])
+    o.forces(True)
+    ke_o = o.kinetic_energy()
+    o.nhc_init(int(opt.q), opt.Q, opt.K)
+    s.md_begin()
+    for a in range(100):
+        ke_o, vc_o, _ = o.md_step(a, opt.t, int(opt.B), ke_o)
+        s.md_steps(a, 1)
+        ke_g, xi_g, vc_g = s.md_scalars()
+        assert ke_g == pytest.approx(ke_o, rel=1e-6), a
+    po, vo = o.get_state()
+    pg, vg = s.get_state()
+    L = float(g["box"])
+    dp = pg - po
+    dp -= L * np.round(dp / L)
+    assert np.abs(dp).max() < 1e-4
+
+
+def test_runs_are_bitwise_deterministic():
+    g = load_golden("patch_crowded")
+    out = []
+    for _ in range(2):
+        s, *_ = _gpu(g)
+        s.md_begin()
+        s.md_steps(0, 25)
+        out.append(s.get_state())
+        s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_graph_windows_equal_single_steps():
+    g = load_golden("plain_small")
+    s1, *_ = _gpu(g)
+    s1.md_begin()
+    s1.md_steps(0, 30)           # three 10-step graph windows
+    s2, *_ = _gpu(g)
+    s2.md_begin()
+    for a in range(30):
+        s2.md_steps(a, 1)        # direct launches
+    p1, v1 = s1.get_state()
+    p2, v2 = s2.get_state()
+    assert np.array_equal(p1, p2) and np.array_equal(v1, v2)
+
+
+def test_batched_systems_equal_separate_runs():
+    """Replicas in one handle give bitwise the same trajectories as separate handles."""
+    from souffle_gb300 import gpu, workloads
+    reps = workloads.replicas(3, seed=11, sub_range=(20, 40))
+    params = [gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local) for w in reps]
+    batch = gpu.GpuSystem(reps[0].template, params)
+    batch.set_state(np.concatenate([w.state.pos for w in reps]), np.concatenate([w.state.vel for w in reps]))
+    batch.md_begin()
+    batch.md_steps(0, 20)
+    pb, vb = batch.get_state()
+    off = 0
+    for w, p in zip(reps, params):
+        one = gpu.GpuSystem(w.template, [p])
+        one.set_state(w.state.pos, w.state.vel)
+        one.md_begin()
+        one.md_steps(0, 20)
+        po, vo = one.get_state()
+        n = po.shape[0]
+        assert np.array_equal(pb[off:off + n], po)
+        assert np.array_equal(vb[off:off + n], vo)
+        off += n
+
+
+def test_inter_capacity_overflow_is_reported():
+    from souffle_gb300 import gpu
+    g = load_golden("bilayer_dense")
+    s, *_ = _gpu(g, inter_capacity=4)
+    with pytest.raises(gpu.SouffleError) as e:
+        s.forces(rebuild=True)
+    assert e.value.code == 3
+
+
+def test_bad_template_is_rejected():
+    from souffle_gb300 import gpu, geometry
+    g = load_golden("plain_small")
+    t, opt, d = golden_workload(g)
+    t.faces = t.faces[:2]
+    with pytest.raises(gpu.SouffleError) as e:
+        gpu.GpuSystem(t, [gpu.system_params(opt, d, 20, 5)])
+    assert e.value.code == 1

@@ -1,0 +1,102 @@
+"""Host-side logic and the C-ABI library, without GPU compute."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO, load_golden, golden_workload
+
+
+def _header_symbols():
+    text = open(os.path.join(REPO, "include", "souffle_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(souffle_gpu_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    from souffle_gb300 import gpu
+    lib = gpu.load()
+    syms = _header_symbols()
+    assert len(syms) >= 14
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(gpu.EXPORTED) == syms
+
+
+def test_create_rejects_bad_arguments_without_crashing():
+    from souffle_gb300 import gpu
+    lib = gpu.load()
+    h = ctypes.c_void_p()
+    rc = lib.souffle_gpu_create(None, None, 0, None, ctypes.byref(h))
+    assert rc in (1, 5)  # BAD_INPUT, or NO_DEVICE on a host without a GPU
+    assert not h.value
+    assert lib.souffle_gpu_create(None, None, 1, None, None) == 1
+    assert lib.souffle_gpu_last_error()
+
+
+def test_infile_round_trip(tmp_path):
+    from souffle_gb300 import geometry
+    for t in (geometry.patch_n3(), geometry.bilayer_n5()):
+        p = tmp_path / t.name
+        geometry.write_infile(t, str(p))
+        t2, bl, m, s = geometry.read_infile(str(p))
+        assert np.array_equal(t2.pos, t.pos)
+        assert np.array_equal(t2.edges, t.edges)
+        assert np.array_equal(t2.faces, t.faces)
+        assert np.array_equal(t2.edge_len0, t.edge_len0)
+        assert t2.lj_attract == t.lj_attract
+        assert s == 1e-9
+
+
+def test_template_shapes():
+    from souffle_gb300 import geometry
+    a = geometry.patch_n3()
+    assert (a.n_beads, len(a.edges), len(a.faces), int((a.edge_type != 0).sum())) == (10, 18, 9, 9)
+    b = geometry.bilayer_n5()
+    assert (b.n_beads, len(b.faces), int((b.edge_type != 0).sum())) == (42, 50, 60)
+    assert len(b.edges) == 2 * 45 + 21 + 45
+
+
+def test_restart_round_trip_is_exact(tmp_path):
+    from souffle_gb300 import geometry, state
+    t = geometry.patch_n3()
+    s = state.random_state(t, 20, state.box_length(20, 800), seed=3)
+    state.write_restart(s, str(tmp_path))
+    step, vel, pos = state.read_restart(str(tmp_path / "restart_0.out"))
+    assert step == 0
+    assert np.array_equal(pos, s.pos)
+    assert np.array_equal(vel, s.vel)
+    assert (tmp_path / "rb_0.out").exists()
+    assert np.abs(pos).max() <= s.box / 2
+
+
+def test_random_state_has_zero_momentum_and_no_overlap():
+    from souffle_gb300 import geometry, state
+    t = geometry.bilayer_n5()
+    L = state.box_length(200, 800)
+    s = state.random_state(t, 200, L, seed=9)
+    assert np.abs(s.vel.mean(axis=0)).max() < 1e-12
+    com = s.pos.reshape(200, 42, 3)
+    # bead sets of different subunits are separated by at least ~1 sigma
+    from scipy.spatial import cKDTree
+    tree = cKDTree(s.pos + L / 2, boxsize=L * (1 + 1e-12))
+    pairs = tree.query_pairs(0.9)
+    sub = np.arange(s.pos.shape[0]) // 42
+    assert all(sub[i] == sub[j] for i, j in pairs)
+
+
+def test_salt_for_debye_length_inverts_kappa():
+    from souffle_gb300 import state
+    for lam in (0.5, 1.0, 2.0):
+        c = state.salt_for_debye_length(lam)
+        assert abs(1 / state.debye_kappa(c) - lam) < 1e-12
+
+
+def test_replica_draws_are_seeded_and_in_range():
+    from souffle_gb300 import workloads
+    a = workloads.replicas(4, seed=5)
+    b = workloads.replicas(4, seed=5)
+    for x, y in zip(a, b):
+        assert x.opt.S == y.opt.S and x.opt.E == y.opt.E and np.array_equal(x.state.pos, y.state.pos)
+        assert 20 <= x.opt.S <= 500 and 1.5 <= x.opt.E <= 3.0 and 200 <= x.opt.C <= 1600

@@ -118,6 +118,8 @@ def main():
     ap.add_argument("--subunits", type=int, default=2000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="md_begin, then --steps MD steps as direct launches (no graphs); for ncu")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -160,6 +162,9 @@ def main():
     s = gpu.GpuSystem(w.template, [p])
     s.set_state(w.state.pos, w.state.vel)
     s.md_begin()
+    if args.profile:
+        print(json.dumps(s.md_profile(0, args.steps)))
+        return
     stats = s.pairlist_stats()
     n_bar = stats["mean_length"]
     ext = torch.cuda.ExternalStream(s.stream())

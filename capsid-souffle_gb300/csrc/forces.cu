@@ -88,12 +88,19 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a) {
   float4* s_bend = s_face + a.max_sub * nf;                         // [max_sub * nb * 4]
   int4* s_pos = reinterpret_cast<int4*>(s_bend + a.max_sub * nb * 4);  // [max_sub * np]
   double* s_red = reinterpret_cast<double*>(s_pos + a.max_sub * np);   // [4 * 32]
-  float* s_w = reinterpret_cast<float*>(s_red + 4 * 32);               // [np]
-  float* s_tf = s_w + np;                                              // [n_float]
-  int* s_ti = reinterpret_cast<int*>(s_tf + L.n_float);                // [n_int]
+  float* s_tf = reinterpret_cast<float*>(s_red + 4 * 32);              // [n_float], n_float % 4 == 0
+  int* s_ti = reinterpret_cast<int*>(s_tf + L.n_float);                // [n_int], n_int % 4 == 0
+  float* s_w = reinterpret_cast<float*>(s_ti + L.n_int);               // [np]
 
-  for (int t = threadIdx.x; t < L.n_int; t += blockDim.x) s_ti[t] = a.tpl_i[t];
-  for (int t = threadIdx.x; t < L.n_float; t += blockDim.x) s_tf[t] = a.tpl_f[t];
+  // template and tile staged with 16-byte loads (all pieces 16-byte aligned, sizes padded)
+  {
+    const int4* gi = reinterpret_cast<const int4*>(a.tpl_i);
+    int4* si = reinterpret_cast<int4*>(s_ti);
+    for (int t = threadIdx.x; t < (L.n_int >> 2); t += blockDim.x) si[t] = __ldg(gi + t);
+    const float4* gf = reinterpret_cast<const float4*>(a.tpl_f);
+    float4* sf = reinterpret_cast<float4*>(s_tf);
+    for (int t = threadIdx.x; t < (L.n_float >> 2); t += blockDim.x) sf[t] = __ldg(gf + t);
+  }
   for (int t = threadIdx.x; t < np; t += blockDim.x) s_w[t] = a.dh_w[w.sys * np + t];
   for (int t = threadIdx.x; t < nbead; t += blockDim.x) s_pos[t] = a.pos32[bead0 + t];
   __syncthreads();
@@ -319,31 +326,54 @@ __global__ void __launch_bounds__(128) k_forces(ForceArgs a) {
       y += s_red[q * 4 + 2];
       z += s_red[q * 4 + 3];
     }
-    double* dst = a.partial + (size_t)w.slot * 4;
-    dst[0] = k;
-    dst[1] = x;
-    dst[2] = y;
-    dst[3] = z;
+    double4* dst = reinterpret_cast<double4*>(a.partial) + w.slot;
+    *dst = make_double4(k, x, y, z);
     __threadfence();
     const int2 sl = a.sys_slots[w.sys];
     unsigned int prev = atomicAdd(&a.state[w.sys].done, 1u);
     last = (prev == (unsigned int)sl.y - 1);
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
 
-  // last CTA of this system: totals in slot order, then the thermostat and COM updates
+  // Last CTA of this system: all its threads sum the slots (thread t takes slots t, t+blockDim,
+  // ... in order, then the fixed shuffle tree and warps in order), so the totals are the same
+  // on every run; then thread 0 applies the thermostat and COM updates.
   __threadfence();
-  SysState& S = a.state[w.sys];
   const int2 sl = a.sys_slots[w.sys];
-  double k = 0, x = 0, y = 0, z = 0;
-  for (int q = 0; q < sl.y; q++) {
-    const volatile double* src = a.partial + (size_t)(sl.x + q) * 4;
-    k += src[0];
-    x += src[1];
-    y += src[2];
-    z += src[3];
+  ke_acc = px_acc = py_acc = pz_acc = 0.0;
+  for (int q = threadIdx.x; q < sl.y; q += blockDim.x) {
+    const double2* src = reinterpret_cast<const double2*>(a.partial) + 2 * (size_t)(sl.x + q);
+    const double2 v0 = __ldcg(src), v1 = __ldcg(src + 1);  // L2 (coherent), not L1
+    ke_acc += v0.x;
+    px_acc += v0.y;
+    py_acc += v1.x;
+    pz_acc += v1.y;
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ke_acc += __shfl_xor_sync(0xffffffffu, ke_acc, o);
+    px_acc += __shfl_xor_sync(0xffffffffu, px_acc, o);
+    py_acc += __shfl_xor_sync(0xffffffffu, py_acc, o);
+    pz_acc += __shfl_xor_sync(0xffffffffu, pz_acc, o);
+  }
+  __syncthreads();
+  if (lane == 0) {
+    s_red[wid * 4 + 0] = ke_acc;
+    s_red[wid * 4 + 1] = px_acc;
+    s_red[wid * 4 + 2] = py_acc;
+    s_red[wid * 4 + 3] = pz_acc;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double k = 0, x = 0, y = 0, z = 0;
+  for (int q = 0; q < nw; q++) {
+    k += s_red[q * 4];
+    x += s_red[q * 4 + 1];
+    y += s_red[q * 4 + 2];
+    z += s_red[q * 4 + 3];
+  }
+  SysState& S = a.state[w.sys];
   S.done = 0;
   S.ke = k;
   if (!isfinite(k)) atomicOr(a.err, kErrNonFinite);

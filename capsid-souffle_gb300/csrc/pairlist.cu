@@ -79,66 +79,69 @@ __global__ void k_cells_scatter(CellArgs a) {
 }
 
 
-// One thread per subunit: centre-distance test over the 27-cell stencil (src/functions.cpp:80-91).
-__global__ void k_candidates(CandArgs a) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.c.n_sub_total) return;
-  const int sysid = a.c.sub_sys[i];
-  const SysParams& p = a.c.sys[sysid];
+// One warp per subunit i: lane k scans stencil cell k (27 cells; with fewer than 3 cells per side
+// every cell of the system is a neighbour and is scanned once), testing centre distances
+// (src/functions.cpp:80-91) exactly in double.  Hits are compacted with a warp scan into shared
+// memory and put in ascending order by rank.  blockDim must be 128 (4 warps).
+__global__ void __launch_bounds__(128) k_candidates(CandArgs a) {
+  extern __shared__ int s_cand[];  // [4 warps][cap]
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= a.c.n_sub_total) return;  // uniform per warp
+  int* buf = s_cand + wib * a.cap;
+  const SysParams& p = a.c.sys[a.c.sub_sys[i]];
   const int np = a.c.np, cl = p.center_local;
   const int ci = i * np + cl;
   const long long xi = a.c.px[ci], yi = a.c.py[ci], zi = a.c.pz[ci];
   const int n = p.ncell;
-  const int cx = cell_coord(xi, n), cy = cell_coord(yi, n), cz = cell_coord(zi, n);
-  int* out = a.cand + (size_t)i * a.cap;
-  int cnt = 0;
-  // iterate over distinct neighbouring cells; with fewer than 3 cells per side every cell is a
-  // neighbour, so loop over all of them once
   const int span = (n < 3) ? n : 3;
-  for (int dx = 0; dx < span; dx++) {
-    int gx = (n < 3) ? dx : (cx + dx - 1 + n) % n;
-    for (int dy = 0; dy < span; dy++) {
-      int gy = (n < 3) ? dy : (cy + dy - 1 + n) % n;
-      for (int dz = 0; dz < span; dz++) {
-        int gz = (n < 3) ? dz : (cz + dz - 1 + n) % n;
-        int cell = p.cell0 + (gx * n + gy) * n + gz;
-        int s0 = a.c.cell_start[cell], s1 = a.c.cell_start[cell + 1];
-        for (int k = s0; k < s1; k++) {
-          int j = a.c.cell_subs[k];
-          bool take;
-          if (j == i) {
-            take = true;  // r2 = 0 for i == j (src/functions.cpp:90)
-          } else {
-            int cj = j * np + cl;
-            double ddx = fixed_diff(xi, a.c.px[cj], p.fx_to_len);
-            double ddy = fixed_diff(yi, a.c.py[cj], p.fx_to_len);
-            double ddz = fixed_diff(zi, a.c.pz[cj], p.fx_to_len);
-            double r2 = ddx * ddx + ddy * ddy + ddz * ddz;
-            take = r2 < p.pre2;
-          }
-          if (take) {
-            if (cnt < a.cap) out[cnt] = j;
-            cnt++;
-          }
-        }
-      }
-    }
+  const int ncells = span * span * span;
+  int s0 = 0, s1 = 0;
+  if (lane < ncells) {
+    const int dx = lane / (span * span), dy = (lane / span) % span, dz = lane % span;
+    const int cx = cell_coord(xi, n), cy = cell_coord(yi, n), cz = cell_coord(zi, n);
+    const int gx = (n < 3) ? dx : (cx + dx - 1 + n) % n;
+    const int gy = (n < 3) ? dy : (cy + dy - 1 + n) % n;
+    const int gz = (n < 3) ? dz : (cz + dz - 1 + n) % n;
+    const int cell = p.cell0 + (gx * n + gy) * n + gz;
+    s0 = a.c.cell_start[cell];
+    s1 = a.c.cell_start[cell + 1];
   }
-  if (cnt > a.cap) {
-    atomicOr(a.err, kErrCandOverflow);
-    cnt = a.cap;
+  auto take = [&](int j) {
+    if (j == i) return true;  // r2 = 0 for i == j (src/functions.cpp:90)
+    const int cj = j * np + cl;
+    const double ddx = fixed_diff(xi, a.c.px[cj], p.fx_to_len);
+    const double ddy = fixed_diff(yi, a.c.py[cj], p.fx_to_len);
+    const double ddz = fixed_diff(zi, a.c.pz[cj], p.fx_to_len);
+    return (ddx * ddx + ddy * ddy + ddz * ddz) < p.pre2;
+  };
+  int nh = 0;  // pass 1: count this lane's hits
+  for (int k = s0; k < s1; k++) nh += take(a.c.cell_subs[k]) ? 1 : 0;
+  // warp exclusive scan of hit counts
+  int x = nh;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  // insertion sort: candidate lists are short (a few to a few dozen)
-  for (int x = 1; x < cnt; x++) {
-    int v = out[x];
-    int y = x - 1;
-    while (y >= 0 && out[y] > v) {
-      out[y + 1] = out[y];
-      y--;
-    }
-    out[y + 1] = v;
+  const int total = __shfl_sync(0xffffffffu, x, 31);
+  int off = x - nh;  // pass 2: write at the lane's offset
+  for (int k = s0; k < s1 && off < a.cap; k++) {
+    const int j = a.c.cell_subs[k];
+    if (take(j)) buf[off++] = j;
   }
-  a.cand_count[i] = cnt;
+  __syncwarp();
+  const int cnt = total < a.cap ? total : a.cap;
+  if (lane == 0 && total > a.cap) atomicOr(a.err, kErrCandOverflow);
+  // rank sort (ids are distinct)
+  int* out = a.cand + (size_t)i * a.cap;
+  for (int k = lane; k < cnt; k += 32) {
+    const int v = buf[k];
+    int r = 0;
+    for (int m = 0; m < cnt; m++) r += (buf[m] < v);
+    out[r] = v;
+  }
+  if (lane == 0) a.cand_count[i] = cnt;
 }
 
 
@@ -320,7 +323,11 @@ void launch_cells_scatter(const CellArgs& a, int grid, int block, cudaStream_t s
   k_cells_scatter<<<grid, block, 0, s>>>(a);
 }
 void launch_candidates(const CandArgs& a, int grid, int block, cudaStream_t s) {
-  k_candidates<<<grid, block, 0, s>>>(a);
+  (void)grid;
+  (void)block;
+  const int warps_per_block = 4;
+  const int g = (a.c.n_sub_total + warps_per_block - 1) / warps_per_block;
+  k_candidates<<<g, 32 * warps_per_block, sizeof(int) * warps_per_block * a.cap, s>>>(a);
 }
 void launch_pairs(const PairArgs& a, int n_sub, size_t smem, cudaStream_t s) {
   k_pairs<<<n_sub, 128, smem, s>>>(a);

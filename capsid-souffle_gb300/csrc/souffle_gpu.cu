@@ -498,7 +498,11 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   }
   h->N = (int64_t)h->S * np;
   if (h->N > ((int64_t)1 << 31) - 1) return fail(SOUFFLE_ERR_BAD_INPUT, "too many beads");
-  h->inter_cap = h->opt.inter_capacity > 0 ? h->opt.inter_capacity : 96;
+  // default inter-subunit capacity: the reference's whole-list capacity (src/md.cpp:231-232),
+  // which bounds the inter part of any list the reference can hold
+  int ref_cap = 64;
+  for (int k = 0; k < n_systems; k++) ref_cap = std::max<int>(ref_cap, params[k].nlist_capacity);
+  h->inter_cap = h->opt.inter_capacity > 0 ? h->opt.inter_capacity : ref_cap;
   h->cand_cap = h->opt.cand_capacity > 0 ? h->opt.cand_capacity : 128;
   h->threads = 128;
   h->subs_per_cta = std::max(1, 128 / np);
@@ -686,11 +690,25 @@ souffle_status souffle_gpu_forces(souffle_gpu_system* h, int32_t rebuild, double
   if (!h) return fail(SOUFFLE_ERR_BAD_INPUT, "null handle");
   if (!h->have_state) return fail(SOUFFLE_ERR_STATE, "no state set");
   CUDA_TRY(cudaSetDevice(h->opt.device));
-  if (rebuild) launch_rebuild(h);
   const bool parts = sforce || bforce;
-  launch_forces(force_args(h, 0, parts), (int)h->work.size(), h->threads, h->force_smem, h->stream);
-  CUDA_TRY(cudaGetLastError());
-  souffle_status s = check_err(h);
+  souffle_status s = SOUFFLE_OK;
+  for (int attempt = 0; attempt < 4; attempt++) {
+    if (rebuild) launch_rebuild(h);
+    launch_forces(force_args(h, 0, parts), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+    CUDA_TRY(cudaGetLastError());
+    s = check_err(h);
+    // a forces-only call changes no state, so an overflowing list is rebuilt with twice the room
+    if (s != SOUFFLE_ERR_NL_OVERFLOW || !rebuild) break;
+    if (g_last_error.find("candidate") != std::string::npos) {
+      h->cand_cap *= 2;
+      CUDA_TRY(h->cand.alloc((size_t)h->cand_cap * h->S));
+    } else {
+      h->inter_cap *= 2;
+      CUDA_TRY(h->inter_ids.alloc((size_t)h->inter_cap * h->N));
+    }
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
+    h->graphs.clear();
+  }
   if (s != SOUFFLE_OK) return s;
   if (tforce && (s = copy_force_out(h, h->force.p, tforce)) != SOUFFLE_OK) return s;
   if (sforce && (s = copy_force_out(h, h->sbforce.p, sforce)) != SOUFFLE_OK) return s;

@@ -1,0 +1,456 @@
+// souffle_gb300: the SOUFFLE molecular-dynamics driver on the GB300 path.
+//
+// Same command line (letters and defaults of src/md.cpp:53-90), same inputs (infiles/<-f>,
+// auto-restart from the newest outfiles/restart_*.out, src/initialize.cpp:166-214) and the same
+// outfiles in the working directory:
+//   outfiles/energy.out          header src/initialize.cpp:12-19, rows src/md.cpp:339-353,616-623
+//   outfiles/ovito.lammpstrj     LAMMPS text dump, src/md.cpp:647-678
+//   outfiles/restart_<a>.out     src/md.cpp:526-546 (12 significant digits)
+//   outfiles/model.parameters.out  src/md.cpp:111-180,233-235
+// The MD loop (src/md.cpp:387-688, molecular-dynamics branch) runs on the GPU through the C ABI
+// in include/souffle_gpu.h; the host only steps between output points.  Brownian dynamics
+// (-D b) and encapsulation (-p) are not part of the GPU path and are rejected.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <dirent.h>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <random>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "souffle_gpu.h"
+
+using namespace std;
+
+namespace {
+
+struct Options {
+  char D = 'm';
+  string f = "41part_c";
+  double C = 200, c = 500, S = 64, s = 50, b = 20, T = 2500, t = 0.004, r = 1, d = 100, q = 5, Q = 10;
+  double K = 298, e = 12;
+  bool R = true, X = false, V = true;
+  double E = 2;
+  int B = 20;
+  double L = 7.5;
+  int M = 1000, W = 1000, w = 1000000, N = 4;
+  bool p = false;
+  double a = 3.0, G = -78.0;
+  int m = 1;
+  double H = 3.5;
+};
+
+bool parse_bool(const string& v) {
+  if (v == "1" || v == "true" || v == "yes" || v == "on") return true;
+  if (v == "0" || v == "false" || v == "no" || v == "off") return false;
+  fprintf(stderr, "bad boolean value: %s\n", v.c_str());
+  exit(2);
+}
+
+void usage() {
+  printf("Usage:\nsouffle_gb300 <options>  (letters as the reference driver)\n"
+         "  -D b|m  -f infile  -C uM  -c mM  -S subunits  -s ks  -b kb  -T steps  -t dt\n"
+         "  -q chain  -Q mass  -K kelvin  -e ecut_c  -R bool  -E eps  -B rebuild  -L skin\n"
+         "  -M movie  -W energy  -w restart  (-r -d -X -V -N -p -a -G -m -H accepted)\n");
+}
+
+// Short options "-X value" or "-Xvalue" (src/md.cpp:53-90).
+Options parse(int argc, char** argv) {
+  Options o;
+  for (int i = 1; i < argc; i++) {
+    string tok = argv[i];
+    if (tok == "-h" || tok == "--help") {
+      usage();
+      exit(0);
+    }
+    if (tok.size() < 2 || tok[0] != '-') {
+      fprintf(stderr, "unexpected argument %s\n", tok.c_str());
+      exit(2);
+    }
+    char k = tok[1];
+    string v;
+    if (tok.size() > 2)
+      v = tok.substr(2);
+    else if (i + 1 < argc)
+      v = argv[++i];
+    else {
+      fprintf(stderr, "option %s needs a value\n", tok.c_str());
+      exit(2);
+    }
+    switch (k) {
+      case 'D': o.D = v[0]; break;
+      case 'f': o.f = v; break;
+      case 'C': o.C = atof(v.c_str()); break;
+      case 'c': o.c = atof(v.c_str()); break;
+      case 'S': o.S = atof(v.c_str()); break;
+      case 's': o.s = atof(v.c_str()); break;
+      case 'b': o.b = atof(v.c_str()); break;
+      case 'T': o.T = atof(v.c_str()); break;
+      case 't': o.t = atof(v.c_str()); break;
+      case 'r': o.r = atof(v.c_str()); break;
+      case 'd': o.d = atof(v.c_str()); break;
+      case 'q': o.q = atof(v.c_str()); break;
+      case 'Q': o.Q = atof(v.c_str()); break;
+      case 'K': o.K = atof(v.c_str()); break;
+      case 'e': o.e = atof(v.c_str()); break;
+      case 'R': o.R = parse_bool(v); break;
+      case 'X': o.X = parse_bool(v); break;
+      case 'V': o.V = parse_bool(v); break;
+      case 'E': o.E = atof(v.c_str()); break;
+      case 'B': o.B = atoi(v.c_str()); break;
+      case 'L': o.L = atof(v.c_str()); break;
+      case 'M': o.M = atoi(v.c_str()); break;
+      case 'W': o.W = atoi(v.c_str()); break;
+      case 'w': o.w = atoi(v.c_str()); break;
+      case 'N': o.N = atoi(v.c_str()); break;
+      case 'p': o.p = parse_bool(v); break;
+      case 'a': o.a = atof(v.c_str()); break;
+      case 'G': o.G = atof(v.c_str()); break;
+      case 'm': o.m = atoi(v.c_str()); break;
+      case 'H': o.H = atof(v.c_str()); break;
+      default:
+        fprintf(stderr, "unrecognised option -%c\n", k);
+        exit(2);
+    }
+  }
+  return o;
+}
+
+struct Infile {
+  double bondlength = 0, mass_si = 0, sigma_si = 0;
+  int np = 0, ne = 0, nf = 0, na = 0;
+  vector<double> x, y, z, q, sigma, mass, len0;
+  vector<int> type, eb, et, fb, lj;
+};
+
+// Token-counted infile layout of src/initialize.cpp:47-128.
+bool read_infile(const string& path, Infile& in) {
+  ifstream f(path.c_str());
+  if (!f) return false;
+  string d;
+  f >> d >> d >> in.bondlength >> d >> d >> in.mass_si >> d >> d >> in.sigma_si;
+  f >> d >> d >> d >> d >> d >> in.np;
+  for (int k = 0; k < 8; k++) f >> d;
+  for (int i = 0; i < in.np; i++) {
+    double name, x, y, z, type, ch, rad, m;
+    f >> name >> x >> y >> z >> type >> ch >> rad >> m;
+    in.x.push_back(x);
+    in.y.push_back(y);
+    in.z.push_back(z);
+    in.type.push_back((int)type);
+    in.q.push_back(ch);
+    in.sigma.push_back(rad);
+    in.mass.push_back(m);
+  }
+  f >> d >> d >> d >> d >> d >> in.ne;
+  for (int k = 0; k < 5; k++) f >> d;
+  for (int i = 0; i < in.ne; i++) {
+    double name, e1, e2, type, len;
+    f >> name >> e1 >> e2 >> type >> len;
+    in.eb.push_back((int)e1);
+    in.eb.push_back((int)e2);
+    in.et.push_back((int)type);
+    in.len0.push_back(len);
+  }
+  f >> d >> d >> d >> d >> d >> in.nf;
+  for (int k = 0; k < 6; k++) f >> d;
+  for (int i = 0; i < in.nf; i++) {
+    double name, t1, t2, t3, type, normal;
+    f >> name >> t1 >> t2 >> t3 >> type >> normal;
+    in.fb.push_back((int)t1);
+    in.fb.push_back((int)t2);
+    in.fb.push_back((int)t3);
+  }
+  f >> d >> d >> d >> d >> d >> d >> in.na;
+  for (int k = 0; k < 5; k++) f >> d;
+  for (int i = 0; i < in.na; i++) {
+    double name, t1, t2, eps, sig;
+    f >> name >> t1 >> t2 >> eps >> sig;
+    in.lj.push_back((int)t1);
+    in.lj.push_back((int)t2);
+  }
+  return !f.fail();
+}
+
+// Newest restart file: names containing "restart", shortest-then-lexicographic order
+// (src/functions.cpp:262-311, src/initialize.cpp:166-191).
+string newest_restart(const string& dir) {
+  vector<string> names;
+  if (DIR* dp = opendir(dir.c_str())) {
+    while (dirent* e = readdir(dp)) {
+      string n = e->d_name;
+      if (n.find("restart") != string::npos) names.push_back(n);
+    }
+    closedir(dp);
+  }
+  if (names.empty()) return "";
+  sort(names.begin(), names.end(), [](const string& a, const string& b) {
+    if (a.size() != b.size()) return a.size() < b.size();
+    return a < b;
+  });
+  return names.back();
+}
+
+void check(souffle_status s, const char* what) {
+  if (s != SOUFFLE_OK) {
+    fprintf(stderr, "souffle_gb300: %s failed (%d): %s\n", what, (int)s, souffle_gpu_last_error());
+    exit(1);
+  }
+}
+
+void progress(double frac) {  // the bar of src/functions.cpp:24-30
+  static const char* bar = "||||||||||||||||||||||||||||||||||||||||||||||||||||||||||||";
+  int val = (int)(frac * 100), lpad = (int)(frac * 60), rpad = 60 - lpad;
+  printf("\r%3d%% |%.*s%*s|", val, lpad, bar, rpad, "");
+  fflush(stdout);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  Options o = parse(argc, argv);
+  if (o.D != 'm') {
+    fprintf(stderr, "souffle_gb300: only molecular dynamics (-D m) runs on the GPU path\n");
+    return 1;
+  }
+  if (o.p) {
+    fprintf(stderr, "souffle_gb300: encapsulation (-p true) is not part of the GPU path\n");
+    return 1;
+  }
+  ofstream traj("outfiles/energy.out", ios_base::app);
+  ofstream ofile("outfiles/ovito.lammpstrj", ios_base::app);
+  ofstream sysdata("outfiles/model.parameters.out", ios::out);
+  if (!traj || !ofile || !sysdata) {
+    cerr << "ERR: outfiles/ directory missing or not writable" << endl;
+    return 1;
+  }
+  traj << "time" << setw(15) << "kinetic" << setw(15) << "stretching" << setw(15) << "bending" << setw(15)
+       << "LJ" << setw(15) << "electrostatics" << setw(15) << "total" << setw(15) << "potential" << setw(15)
+       << "temperature" << setw(20) << "thermo_potential" << setw(15) << "thermo_kinetic" << setw(15)
+       << "system_velocity_magnitude" << endl;
+  sysdata << "Running molecular dynamics with Nose Hoover thermostat." << endl;
+
+  Infile in;
+  if (!read_infile("infiles/" + o.f, in)) {
+    cerr << "ERR: FILE " << o.f << " NOT OPENED. Check directory and/or filename.";
+    return 1;
+  }
+  const int S = (int)o.S, np = in.np;
+  const long N = (long)S * np;
+  const double Avagadro = 6.022e23, Boltzmann = 1.3806e-23, Pi = 3.14159;
+
+  // state: restart file or cubic lattice (src/initialize.cpp:199-231)
+  vector<double> pos(3 * N), vel(3 * N, 0.0);
+  double box_x = pow((o.S * 1000 / (o.C * pow(in.sigma_si, 3) * Avagadro)), 1.0 / 3.0);
+  int loopStart = 0;
+  string rname = o.R ? newest_restart("outfiles/") : "";
+  bool restart = !rname.empty();
+  if (restart) {
+    cout << "Restarting from: " << rname << endl;
+    ifstream rf(("outfiles/" + rname).c_str());
+    if (!rf) {
+      cerr << "ERR: RESTART FILE outfiles/restart.out NOT OPENED. Check directory and/or filename.";
+      return 1;
+    }
+    string d;
+    rf >> d >> d >> d >> d >> loopStart;
+    for (long i = 0; i < N; i++) {
+      rf >> d >> vel[3 * i] >> vel[3 * i + 1] >> vel[3 * i + 2] >> pos[3 * i] >> pos[3 * i + 1] >> pos[3 * i + 2];
+      if (!rf) {
+        cerr << "ERR: restart file " << rname << " has fewer than " << N << " beads" << endl;
+        return 1;
+      }
+    }
+  } else {
+    cout << "No restart files found! Starting simulation from scratch." << endl;
+    const unsigned nf = (unsigned)ceil(pow(double(S), 1.0 / 3.0));
+    long k0 = 0;
+    for (unsigned i = 0; i < nf; i++)
+      for (unsigned j = 0; j < nf; j++)
+        for (unsigned k = 0; k < nf; k++, k0++) {
+          if (k0 >= S) continue;
+          for (int l = 0; l < np; l++) {
+            long g = k0 * np + l;
+            pos[3 * g] = (double)i * box_x * (1 / (double)nf) + in.x[l];
+            pos[3 * g + 1] = (double)j * box_x * (1 / (double)nf) + in.y[l];
+            pos[3 * g + 2] = (double)k * box_x * (1 / (double)nf) + in.z[l];
+          }
+        }
+  }
+  // centre bead of subunit 0 (src/initialize.cpp:266-288)
+  int center = 0;
+  {
+    double c[3] = {0, 0, 0};
+    for (int l = 0; l < np; l++)
+      for (int d = 0; d < 3; d++) c[d] += pos[3 * l + d];
+    for (int d = 0; d < 3; d++) c[d] /= np;
+    double best = 1000;
+    for (int l = 0; l < np; l++) {
+      double r2 = 0;
+      for (int d = 0; d < 3; d++) {
+        double r = pos[3 * l + d] - c[d];
+        if (r > box_x / 2) r -= box_x;
+        else if (r < -box_x / 2) r += box_x;
+        r2 += r * r;
+      }
+      if (r2 < best) {
+        best = r2;
+        center = l;
+      }
+    }
+  }
+
+  // units (src/md.cpp:135-173)
+  const double SIenergy = o.K * Boltzmann;
+  const double SItime = sqrt(in.sigma_si * in.sigma_si * in.mass_si / SIenergy);
+  const double totaltime = o.T * o.t;
+  const double Tred = o.K / double(298);
+  const double UnitEnergy = SIenergy * SItime * SItime / (in.mass_si * in.sigma_si * (1e-9));
+  sysdata << "Simulation will run for " << totaltime * SItime / (1e-9) << " nanoseconds with a "
+          << o.t * SItime / (1e-12) << " picosecond timestep." << endl;
+  sysdata << "Capsomere concentration: " << o.C << " micromolar" << endl;
+  sysdata << "Salt concentration: " << o.c << " millimolar" << endl;
+  sysdata << "Stretching constant: " << o.s << " KbT" << "( " << (o.s * in.mass_si / (SItime * SItime)) << " N/m)" << endl;
+  sysdata << "Bending constant: " << o.b << " KbT" << "( "
+          << (o.b * in.mass_si * in.sigma_si * in.sigma_si / (SItime * SItime)) << " J)" << endl;
+  sysdata << "Bondlength between beads is " << in.bondlength << " LJ reduced units, which is "
+          << in.bondlength * in.sigma_si / (1e-9) << " nanometers." << endl;
+  sysdata << "Mass of a bead is " << in.mass_si << " kg." << endl;
+  sysdata << "Diameter of a bead is " << in.sigma_si / (1e-9) << " nanometers." << endl;
+  sysdata << "Total number of subunits is " << o.S << endl;
+  sysdata << "Temperature is " << o.K << " K" << " Which is " << Tred << " in reduced units" << endl;
+  sysdata << "Attractive LJ paramerter is " << o.E << " Which is "
+          << o.E * (SIenergy * Avagadro / (1000 * UnitEnergy)) << " kJ/mol." << endl;
+  const double ecut = 2.5 * (in.sigma_si / 1e-9);
+  const double lb = (0.701e-9) / in.sigma_si;
+  const double ni = o.c * Avagadro * in.sigma_si * in.sigma_si * in.sigma_si;
+  const double kappa = sqrt(8 * Pi * ni * lb * 1 * 1);
+  const double screen = 1 / kappa;
+  const double ecut_el = screen * o.e;
+  const double NListCutoff = (ecut_el > ecut) ? ecut_el + o.L : ecut + o.L;
+  sysdata << "Box length is " << box_x * in.sigma_si / (1e-9) << " nanometers." << endl;
+  sysdata << "Screening length is " << screen << " nanometers." << endl;
+  sysdata << "electrostatic cutoff is " << ecut_el * in.sigma_si / (1e-9) << " nanometers." << endl;
+  sysdata << "Neighborlist cutoff is " << NListCutoff * in.sigma_si / (1e-9) << " nanometers." << endl;
+  unsigned cap = (unsigned)ceil((NListCutoff + 0.5) * (NListCutoff + 0.5) * (NListCutoff + 0.5));
+  if (cap > (unsigned)N) cap = (unsigned)N;
+  sysdata << "Neighborlist has a maximum of " << cap << " neighbors per bead." << endl;
+
+  if (!restart) {
+    // rigid per-subunit velocities uniform in [-0.5, 0.5)^3, zero net momentum, scaled to T
+    // (the structure of src/initialize.cpp:471-564, drawn from a fixed-seed std::mt19937)
+    std::mt19937 eng(5489u);
+    std::uniform_real_distribution<double> u(-0.5, 0.5);
+    for (int i = 0; i < S; i++) {
+      double vx = u(eng), vy = u(eng), vz = u(eng);
+      for (int l = 0; l < np; l++) {
+        long g = (long)i * np + l;
+        vel[3 * g] = vx;
+        vel[3 * g + 1] = vy;
+        vel[3 * g + 2] = vz;
+      }
+    }
+    double avg[3] = {0, 0, 0};
+    for (long g = 0; g < N; g++)
+      for (int d = 0; d < 3; d++) avg[d] += vel[3 * g + d];
+    double ke = 0;
+    for (long g = 0; g < N; g++) {
+      double v2 = 0;
+      for (int d = 0; d < 3; d++) {
+        vel[3 * g + d] -= avg[d] / N;
+        v2 += vel[3 * g + d] * vel[3 * g + d];
+      }
+      ke += 0.5 * in.mass[g % np] * v2;
+    }
+    const double sf = sqrt(Tred / (ke / (1.5 * N)));
+    for (auto& v : vel) v *= sf;
+  }
+
+  souffle_template t{np, in.ne, in.nf, in.na, in.type.data(), in.q.data(), in.sigma.data(), in.mass.data(),
+                     in.eb.data(), in.et.data(), in.len0.data(), in.fb.data(), in.lj.empty() ? nullptr : in.lj.data()};
+  souffle_params p{};
+  p.n_subunits = S;
+  p.box = box_x;
+  p.ks = o.s;
+  p.kb = o.b;
+  p.elj_att = o.E;
+  p.lb = lb;
+  p.kappa = kappa;
+  p.ecut = ecut;
+  p.ecut_el = ecut_el;
+  p.nlist_cutoff = NListCutoff;
+  p.nlist_capacity = (int)cap;
+  p.center_local = center;
+  p.dt = o.t;
+  p.chain_length = (int)o.q;
+  p.nhc_mass = o.Q;
+  p.temperature = Tred;
+  p.build_freq = o.B;
+  souffle_gpu_system* h = nullptr;
+  check(souffle_gpu_create(&t, &p, 1, nullptr, &h), "souffle_gpu_create");
+  // the reference wraps lattice positions only when they move; the fixed-point state wraps now
+  check(souffle_gpu_set_state(h, pos.data(), vel.data()), "souffle_gpu_set_state");
+  check(souffle_gpu_md_begin(h), "souffle_gpu_md_begin");
+
+  vector<double> be(N);
+  auto energy_row = [&](long a, bool with_vcom) {
+    souffle_energies e;
+    check(souffle_gpu_energies(h, 0, &e, nullptr, be.data(), nullptr, nullptr, nullptr), "souffle_gpu_energies");
+    const double tot = e.stretching + e.kinetic + e.lj + e.bending + e.electrostatic + e.thermo_pe + e.thermo_ke;
+    traj << a << setw(15) << e.kinetic / N << setw(15) << e.stretching / N << setw(15) << e.bending / N
+         << setw(15) << e.lj / N << setw(15) << e.electrostatic / N << setw(15) << tot / N << setw(15)
+         << (e.bending + e.stretching + e.lj + e.electrostatic) / N << setw(15) << e.kinetic * 2 / (3 * N)
+         << setw(15) << e.thermo_pe / N << setw(15) << e.thermo_ke / N;
+    if (with_vcom) traj << setw(15) << e.vcom_magnitude;
+    traj << endl;
+  };
+  energy_row(0, false);  // row 0 before the loop (src/md.cpp:339-346)
+
+  ofstream rs;  // one stream object for every restart file, as src/md.cpp:104
+  const double loop_end = (totaltime / o.t) + 1;  // src/md.cpp:387
+  long a = loopStart;
+  double pre = -1;
+  while (a < loop_end) {
+    // advance to the next step that writes anything (inclusive)
+    long next = a;
+    while (next + 1 < loop_end && !(next % o.w == 0 || next % o.W == 0 || next % o.M == 0)) next++;
+    check(souffle_gpu_md_steps(h, a, (int)(next - a + 1)), "souffle_gpu_md_steps");
+    a = next;
+    if (a % o.w == 0 || a % o.M == 0) check(souffle_gpu_get_state(h, pos.data(), vel.data()), "souffle_gpu_get_state");
+    if (a % o.w == 0) {
+      rs.open(("outfiles/restart_" + to_string(a) + ".out").c_str(), ios::out);
+      rs << "Velocities & Positions for " << a << endl;
+      for (long i = 0; i < N; i++)
+        rs << i << "  " << vel[3 * i] << setw(25) << setprecision(12) << vel[3 * i + 1] << setw(25)
+           << setprecision(12) << vel[3 * i + 2] << setw(25) << setprecision(12) << pos[3 * i] << setw(25)
+           << setprecision(12) << pos[3 * i + 1] << setw(25) << setprecision(12) << pos[3 * i + 2] << setw(25)
+           << setprecision(12) << endl;
+      rs.close();
+    }
+    if (a % o.W == 0) energy_row(a, true);
+    if (a % o.M == 0) {
+      ofile << "ITEM: TIMESTEP" << endl << a << endl << "ITEM: NUMBER OF ATOMS" << endl << N << endl
+            << "ITEM: BOX BOUNDS" << endl << -box_x / 2 << setw(15) << box_x / 2 << endl << -box_x / 2
+            << setw(15) << box_x / 2 << endl << -box_x / 2 << setw(15) << box_x / 2 << endl
+            << "ITEM: ATOMS index type x y z b charge" << endl;
+      for (long g = 0; g < N; g++)
+        ofile << g + 1 << setw(15) << in.type[g % np] << setw(15) << pos[3 * g] << setw(15) << pos[3 * g + 1]
+              << setw(15) << pos[3 * g + 2] << setw(15) << be[g] << setw(15) << in.q[g % np] << endl;
+    }
+    double pct = roundf(a / (totaltime / o.t) * 100 * 10) / 10;
+    if (pct != pre) {
+      progress(pct / 100);
+      pre = pct;
+    }
+    a++;
+  }
+  printf("\n");
+  souffle_gpu_destroy(h);
+  return 0;
+}

@@ -77,6 +77,8 @@ def main():
             subprocess.run([refdump.REF_RUN] + args, cwd=md, check=True, capture_output=True)
             _, vmd, pmd = state.read_restart(f"{md}/outfiles/restart_{MD_STEPS}.out")
             rows = np.loadtxt(f"{md}/outfiles/energy.out", skiprows=1, usecols=range(11))
+            energy_text = open(f"{md}/outfiles/energy.out").read()
+            restart_text = open(f"{md}/outfiles/restart_{MD_STEPS}.out").read()
             np.savez_compressed(
                 os.path.join(HERE, f"{name}.npz"),
                 template=np.array(tname), n_sub=S, conc=C, seed=seed, gap=gap,
@@ -88,6 +90,8 @@ def main():
                 nl_counts=counts, nl_ids=ids,
                 se=d["se"], ke=d["ke"], be=d["be"], ne=d["ne"], ce=d["ce"], ke_total=d["ke_total"],
                 md_steps=MD_STEPS, md_pos=pmd, md_vel=vmd, md_energy_rows=rows,
+                md_energy_text=np.array(energy_text), md_restart_text=np.array(restart_text),
+                md_args=np.array(args),
             )
             print(name, n, "beads; mean list", counts.mean(), "max", counts.max(), "cap", cap)
 

@@ -64,12 +64,13 @@ struct ForceArgs {
   const int* inter_count;
   const float* dh_w;         // [n_sys * np] q * exp(kappa sigma/2)/(1 + kappa sigma/2) * sqrt(lb)
   const PairTable* pt;
-  const double* inv_mass;    // [np]
-  double* fx; double* fy; double* fz;
-  double* vx; double* vy; double* vz;
-  double* sfx; double* sfy; double* sfz;   // optional stretching force out
-  double* bfx; double* bfy; double* bfz;   // optional bending force out
-  double* partial;           // [slots * 4]
+  const double* inv_mass_d;  // [np] (thermostat thread only)
+  long long* kick_c;         // [n_sys * np] dt sqrt(expfac) / (2 m) * 2^62, written by the last CTA
+  long long* fx; long long* fy; long long* fz;   // force, 2^-32 units
+  long long* vx; long long* vy; long long* vz;   // velocity, 2^-32 units
+  float* sfx; float* sfy; float* sfz;   // optional stretching force out
+  float* bfx; float* bfy; float* bfz;   // optional bending force out
+  long long* partial;        // [slots * 4] KE (2^-32), momentum (2^-32)
   unsigned int* err;
   int n_beads_total;
   int max_sub;               // subunits per CTA (shared-memory sizing)
@@ -80,10 +81,10 @@ struct DriftArgs {
   const SysParams* sys;
   const SysState* state;
   const WorkItem* work;
-  const double* inv_mass;
+  const long long* kick_c;
   int np;
-  const double* fx; const double* fy; const double* fz;
-  double* vx; double* vy; double* vz;
+  const long long* fx; const long long* fy; const long long* fz;
+  long long* vx; long long* vy; long long* vz;
   long long* px; long long* py; long long* pz;
   int4* pos32;
 };
@@ -97,9 +98,11 @@ struct StateArgs {
   const double* vel_in;
   long long* px; long long* py; long long* pz;
   int4* pos32;
-  double* vx; double* vy; double* vz;
+  long long* vx; long long* vy; long long* vz;
   double* pos_out;       // [N*3]
   double* vel_out;
+  double* force_out;     // [N*3] optional
+  const long long* fx_in; const long long* fy_in; const long long* fz_in;
 };
 
 struct EnergyArgs {
@@ -109,7 +112,7 @@ struct EnergyArgs {
   const SysState* state;
   const long long* px; const long long* py; const long long* pz;
   const int4* pos32;
-  const double* vx; const double* vy; const double* vz;
+  const long long* vx; const long long* vy; const long long* vz;   // 2^-32 units
   const double* len0;      // [ne]
   const double* mass;      // [np]
   const double* q;         // [np]

@@ -43,6 +43,7 @@ struct TplLayout {
   int o_len0;         // [ne]
   int o_q;            // [np]
   int o_sigma;        // [np]
+  int o_mass;         // [np]
   int n_float;
   int nspecies;
   int lj_att_bits[kMaxSpecies];  // bit js of row is: (species is -> js) attractive
@@ -69,6 +70,7 @@ struct SysParams {
   int center_local;         // template-local centre bead (src/initialize.cpp:266-288)
   double dt;
   double ks_d, kb_d;        // double copies for the FP64 energy pass
+  long long drift_fx;       // dt 2^32 / L in 2^-40 units: x_fixed += v_fixed * drift_fx >> 40
 };
 
 // Thermostat chain and step scalars of one system, updated on the device.
@@ -84,7 +86,8 @@ struct SysState {
   double xi_b[kMaxChain], eta_b[kMaxChain];
   double ke;             // particle_ke carried between steps (src/md.cpp:456)
   double expfac;         // exp(-dt xi0 / 2) for the next step (src/md.cpp:406)
-  double vcom[3];        // mean velocity still to subtract from vel (0 once applied)
+  long long delta_fx;    // (1 - expfac) * 2^62 for the integer kicks
+  long long vcom_fx[3];  // mean velocity (2^-32 units) still to subtract from vel (0 once applied)
   double vcom_mag;       // |mean velocity| removed at the last step (src/md.cpp:623)
   unsigned int done;     // arrival counter for the last-block reduction
   unsigned int steps;    // MD steps completed since md_begin
@@ -137,6 +140,37 @@ __host__ __device__ inline double fixed_diff(long long a, long long b, double fx
 
 __device__ inline float hi_diff(int a, int b, float unit) {
   return (float)(int)((unsigned int)a - (unsigned int)b) * unit;
+}
+
+// ---- 64-bit fixed point without FP64 instructions -------------------------------------------
+// GB300 runs FP64 at a small fraction of its FP32 rate, so per-bead integration is done in
+// integers: velocities and forces are int64 in units of 2^-32, positions int64 in units of
+// L/2^64, and every product is an exact 64x64->128 multiply rounded to nearest.
+
+// round(a * b / 2^s) for 0 < s < 64, exact (128-bit product, ties away from zero is not needed:
+// adding 2^(s-1) rounds half up).
+__device__ __forceinline__ long long mul_shr(long long a, long long b, int s) {
+  unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
+  long long hi = __mul64hi(a, b);
+  const unsigned long long half = 1ull << (s - 1);
+  const unsigned long long lo2 = lo + half;
+  hi += (lo2 < lo) ? 1 : 0;
+  return (long long)(((unsigned long long)hi << (64 - s)) | (lo2 >> s));
+}
+
+// round(v * 2^32) as int64 for |v| < 2^31, using only 32-bit conversions.
+__device__ __forceinline__ long long f32_to_fx32(float v) {
+  const float hi = floorf(v);
+  const float frac = (v - hi) * 4294967296.0f;  // in [0, 2^32]
+  const unsigned long long lo = (unsigned long long)__float2uint_rn(frac);
+  return (long long)(((unsigned long long)(long long)__float2int_rz(hi) << 32) + lo);
+}
+
+// int64 in units of 2^-32 to float, using only 32-bit conversions.
+__device__ __forceinline__ float fx32_to_f32(long long x) {
+  const int hi = (int)(x >> 32);
+  const unsigned int lo = (unsigned int)x;
+  return fmaf((float)lo, 2.3283064365386963e-10f, (float)hi);
 }
 
 }  // namespace souffle

@@ -202,7 +202,9 @@ struct souffle_gpu_system {
   DevBuf<int> d_sub_sys, d_bead_sys;
   DevBuf<long long> pos_fx;
   DevBuf<int4> pos32;
-  DevBuf<double> vel, force, sbforce, partial, staging;
+  DevBuf<long long> vel, force, partial, kick_c;   // 2^-32 fixed point
+  DevBuf<float> sbforce;
+  DevBuf<double> staging;
   DevBuf<unsigned int> intra_mask;
   DevBuf<int> inter_ids, inter_count, ref_len;
   DevBuf<int> cand, cand_count;
@@ -259,6 +261,8 @@ souffle_status upload(souffle_gpu_system* h) {
   for (double v : T.q) tf.push_back((float)v);
   L.o_sigma = (int)tf.size();
   for (double v : T.sigma) tf.push_back((float)v);
+  L.o_mass = (int)tf.size();
+  for (double v : T.mass) tf.push_back((float)v);
   while (tf.size() % 4) tf.push_back(0.f);
   L.n_float = (int)tf.size();
   L.nspecies = T.nspecies;
@@ -410,7 +414,8 @@ ForceArgs force_args(souffle_gpu_system* h, int mode, bool want_parts) {
   a.inter_count = h->inter_count.p;
   a.dh_w = h->dh_w.p;
   a.pt = h->pt.p;
-  a.inv_mass = h->inv_mass.p;
+  a.inv_mass_d = h->inv_mass.p;
+  a.kick_c = h->kick_c.p;
   const int64_t N = h->N;
   a.fx = h->force.p;
   a.fy = h->force.p + N;
@@ -440,7 +445,7 @@ DriftArgs drift_args(souffle_gpu_system* h) {
   a.sys = h->d_sys.p;
   a.state = h->d_state.p;
   a.work = h->d_work.p;
-  a.inv_mass = h->inv_mass.p;
+  a.kick_c = h->kick_c.p;
   a.np = h->tpl.np;
   a.fx = h->force.p;
   a.fy = h->force.p + N;
@@ -504,8 +509,8 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   for (int k = 0; k < n_systems; k++) ref_cap = std::max<int>(ref_cap, params[k].nlist_capacity);
   h->inter_cap = h->opt.inter_capacity > 0 ? h->opt.inter_capacity : ref_cap;
   h->cand_cap = h->opt.cand_capacity > 0 ? h->opt.cand_capacity : 128;
-  h->threads = 128;
-  h->subs_per_cta = std::max(1, 128 / np);
+  h->threads = 256;                        // two threads per bead in k_forces
+  h->subs_per_cta = std::max(1, 128 / np);  // up to 128 beads per CTA
 
   // per-system constants, cell grids, work items
   int sub0 = 0, cell0 = 0;
@@ -539,6 +544,14 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
     q.quirks = (h->opt.compat_quirks >= 0) ? 1 : 0;
     q.center_local = p.center_local;
     q.dt = p.dt;
+    // x_fixed advances by v dt 2^64 / L = v_fixed dt 2^32 / L: the multiplier in 2^-40 units
+    const double dx = p.dt * kTwo32 / p.box;
+    if (!(dx < 8388608.0))
+      return fail(SOUFFLE_ERR_BAD_INPUT, "time step too large for the box (dt 2^32 / L >= 2^23)");
+    q.drift_fx = (long long)std::llrint(dx * 1099511627776.0);
+    for (int i = 0; i < np; i++)
+      if (!(0.5 * p.dt * 1.5 / tpl->bead_mass[i] < 2.0))
+        return fail(SOUFFLE_ERR_BAD_INPUT, "dt / (2 m) too large for the fixed-point kick");
     h->sp.push_back(q);
     for (int i = 0; i < p.n_subunits; i++) sub_sys[sub0 + i] = k;
     for (int i = 0; i < p.n_subunits * np; i++) bead_sys[(int64_t)sub0 * np + i] = k;
@@ -575,8 +588,10 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(h->vel.alloc(3 * N));
   CUDA_TRY(h->force.alloc(3 * N));
   CUDA_TRY(h->sbforce.alloc(6 * N));
-  CUDA_TRY(h->staging.alloc(6 * N));
+  CUDA_TRY(h->staging.alloc(9 * N));
   CUDA_TRY(h->partial.alloc(4 * h->work.size()));
+  CUDA_TRY(h->kick_c.alloc((size_t)n_systems * np));
+  CUDA_TRY(cudaMemset(h->kick_c.p, 0, sizeof(long long) * n_systems * np));
   CUDA_TRY(h->intra_mask.alloc((size_t)h->S * np * L.words));
   CUDA_TRY(h->inter_ids.alloc((size_t)h->inter_cap * N));
   CUDA_TRY(h->inter_count.alloc(N));
@@ -593,7 +608,7 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(h->e_tot.alloc(8));
   CUDA_TRY(cudaMemset(h->intra_mask.p, 0, sizeof(unsigned int) * (size_t)h->S * np * L.words));
   CUDA_TRY(cudaMemset(h->inter_count.p, 0, sizeof(int) * N));
-  CUDA_TRY(cudaMemset(h->force.p, 0, sizeof(double) * 3 * N));
+  CUDA_TRY(cudaMemset(h->force.p, 0, sizeof(long long) * 3 * N));
 
   h->force_smem = sizeof(float4) * h->subs_per_cta * (L.ne + L.nf + 4 * L.nbend) +
                   sizeof(int4) * h->subs_per_cta * np + sizeof(double) * 4 * 32 +
@@ -671,17 +686,37 @@ souffle_status souffle_gpu_get_state(souffle_gpu_system* h, double* pos, double*
   return SOUFFLE_OK;
 }
 
-static souffle_status copy_force_out(souffle_gpu_system* h, const double* dev3, double* host) {
-  // device SoA [3][N] -> host xyz interleaved
+static souffle_status copy_force_out(souffle_gpu_system* h, const float* dev3, double* host) {
+  // device float SoA [3][N] -> host double xyz interleaved
   const int64_t N = h->N;
-  std::vector<double> tmp(3 * N);
-  CUDA_TRY(cudaMemcpyAsync(tmp.data(), dev3, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+  std::vector<float> tmp(3 * N);
+  CUDA_TRY(cudaMemcpyAsync(tmp.data(), dev3, sizeof(float) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   for (int64_t i = 0; i < N; i++) {
     host[3 * i] = tmp[i];
     host[3 * i + 1] = tmp[N + i];
     host[3 * i + 2] = tmp[2 * N + i];
   }
+  return SOUFFLE_OK;
+}
+
+// Total force (int64, 2^-32 units) to host doubles, xyz interleaved.
+static souffle_status copy_total_force_out(souffle_gpu_system* h, double* host) {
+  const int64_t N = h->N;
+  StateArgs a{};
+  a.sys = h->d_sys.p;
+  a.state = h->d_state.p;
+  a.bead_sys = h->d_bead_sys.p;
+  a.np = h->tpl.np;
+  a.n = (int)N;
+  a.force_out = h->staging.p + 6 * N;
+  a.fx_in = h->force.p;
+  a.fy_in = h->force.p + N;
+  a.fz_in = h->force.p + 2 * N;
+  launch_state_out(a, (int)((N + 255) / 256), 256, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(host, a.force_out, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
   return SOUFFLE_OK;
 }
 
@@ -710,7 +745,7 @@ souffle_status souffle_gpu_forces(souffle_gpu_system* h, int32_t rebuild, double
     h->graphs.clear();
   }
   if (s != SOUFFLE_OK) return s;
-  if (tforce && (s = copy_force_out(h, h->force.p, tforce)) != SOUFFLE_OK) return s;
+  if (tforce && (s = copy_total_force_out(h, tforce)) != SOUFFLE_OK) return s;
   if (sforce && (s = copy_force_out(h, h->sbforce.p, sforce)) != SOUFFLE_OK) return s;
   if (bforce && (s = copy_force_out(h, h->sbforce.p + 3 * h->N, bforce)) != SOUFFLE_OK) return s;
   return SOUFFLE_OK;

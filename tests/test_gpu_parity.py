@@ -67,7 +67,9 @@ def test_energies_match_reference(name):
     assert tot["electrostatic"] == pytest.approx(g["ce"].sum(), rel=1e-9, abs=1e-9)
 
 
-@pytest.mark.parametrize("name", GOLDEN_CASES)
+# patch_crowded starts from overlapping subunits and blows up within 20 steps in the reference
+# itself (|v| ~ 1e9), so it pins forces, lists and energies but not a trajectory.
+@pytest.mark.parametrize("name", ["plain_small", "bilayer_dense"])
 def test_md_steps_match_reference_run(name):
     g = load_golden(name)
     s, t, opt, d = _gpu(g)

@@ -74,7 +74,7 @@ __global__ void k_energy_bonded(EnergyArgs a) {
     double c = (A0[0] * A1[0] + A0[1] * A1[1] + A0[2] * A1[2]) / (a0 * a1);
     be += P.kb_d * 0.25 * (1.0 - fabs(c));
   }
-  const double inv = 1.0 / kTwo32;
+  const double inv = 1.0 / kVelScale;
   const double vx = (double)(a.vx[g] - S.vcom_fx[0]) * inv, vy = (double)(a.vy[g] - S.vcom_fx[1]) * inv,
                vz = (double)(a.vz[g] - S.vcom_fx[2]) * inv;
   const double m = a.mass[l];

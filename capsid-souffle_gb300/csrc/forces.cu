@@ -37,35 +37,31 @@ __device__ __forceinline__ float3 dvec(int4 a, int4 b, float unit) {
 
 // Nose-Hoover chain link update, update_chain_xi (src/functions.cpp:33-58).  The two
 // exponentials of the reference are exp(-dt xi/2) and exp(-dt xi/4); the first is the square of
-// the second.
-__device__ void chain_xi(double* xi, const double* q, const double* dof, const double* t, int j,
-                         double dt, double ke) {
-  if (q[j] == 0) return;
-  const double e4 = exp(-0.25 * dt * xi[j + 1]);
+// the second.  1/Q comes precomputed from the host (no division on the device).
+__device__ void chain_xi(SysState& s, double* xi, int j, double dt) {
+  if (s.q[j] == 0) return;
+  const double e4 = exp_small(-0.25 * dt * xi[j + 1]);
   const double e2 = e4 * e4;
-  if (j != 0) {
-    xi[j] = xi[j] * e2 + 0.5 * dt * (1.0 / q[j]) * (q[j - 1] * xi[j - 1] * xi[j - 1] - dof[j] * t[j]) * e4;
-  } else {
-    xi[j] = xi[j] * e2 + 0.5 * dt * (1.0 / q[j]) * (2 * ke - dof[j] * t[j]) * e4;
-  }
+  const double g = (j != 0) ? s.q[j - 1] * xi[j - 1] * xi[j - 1] - s.dof[j] * s.t[j]
+                            : 2 * s.ke - s.dof[j] * s.t[j];
+  xi[j] = xi[j] * e2 + 0.5 * dt * s.inv_q[j] * g * e4;
 }
 
 // Backward half at the start of a step (src/md.cpp:401-406), from (xi, eta) into (xi_b, eta_b),
-// then the step's kick coefficients: expfac, delta = 1 - expfac and c = dt sqrt(expfac)/(2 m)
-// per template bead, in the fixed-point forms the kernels use.
-__device__ void nhc_backward(SysState& s, double dt, const double* inv_mass, long long* kick_c, int np) {
+// then the step's kick factors: expfac, delta = 1 - expfac (2^62 units) and
+// c0 = dt sqrt(expfac)/2 (2^64 units; the per-bead coefficient is c0 / m).
+__device__ void nhc_backward(SysState& s, double dt) {
   for (int j = 0; j < s.m; j++) {
     s.xi_b[j] = s.xi[j];
     s.eta_b[j] = s.eta[j];
   }
-  for (int j = s.m - 1; j > -1; j--) chain_xi(s.xi_b, s.q, s.dof, s.t, j, dt, s.ke);
+  for (int j = s.m - 1; j > -1; j--) chain_xi(s, s.xi_b, j, dt);
   for (int j = 0; j < s.m; j++)
     if (s.q[j] != 0) s.eta_b[j] = s.eta_b[j] + 0.5 * dt * s.xi_b[j];
   const double x = -0.5 * dt * s.xi_b[0];
-  s.expfac = exp(x);
-  s.delta_fx = __double2ll_rn(-expm1(x) * 4611686018427387904.0);  // (1 - expfac) 2^62
-  const double c0 = 0.5 * dt * sqrt(s.expfac) * 4611686018427387904.0;
-  for (int l = 0; l < np; l++) kick_c[l] = __double2ll_rn(c0 * inv_mass[l]);
+  s.expfac = exp_small(x);
+  s.delta_fx = __double2ll_rn(-expm1_small(x) * 4611686018427387904.0);
+  s.kick_c0 = 0.5 * dt * exp_small(0.5 * x) * 18446744073709551616.0;
 }
 
 // Forward half at the end of a step (src/md.cpp:457-460), from (xi_b, eta_b) into (xi, eta).
@@ -76,7 +72,7 @@ __device__ void nhc_forward(SysState& s, double dt) {
   }
   for (int j = 0; j < s.m; j++)
     if (s.q[j] != 0) s.eta[j] = s.eta[j] + 0.5 * dt * s.xi[j];
-  for (int j = 0; j < s.m; j++) chain_xi(s.xi, s.q, s.dof, s.t, j, dt, s.ke);
+  for (int j = 0; j < s.m; j++) chain_xi(s, s.xi, j, dt);
 }
 
 // int64 warp sum with a fixed xor tree (exact, so any order gives the same bits)
@@ -313,9 +309,9 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
         long long vx = a.vx[g], vy = a.vy[g], vz = a.vz[g];
         if (a.mode == 1) {  // v <- v exp(-dt xi/2) + F dt sqrt(expfac)/(2m)  (src/bead.h:113-117)
           const long long c = kick_c[l];
-          vx = vx - mul_shr(vx, delta_fx, 62) + mul_shr(Fx, c, 62);
-          vy = vy - mul_shr(vy, delta_fx, 62) + mul_shr(Fy, c, 62);
-          vz = vz - mul_shr(vz, delta_fx, 62) + mul_shr(Fz, c, 62);
+          vx = vx - mul_shr(vx, delta_fx, 62) + mul_shr(Fx, c, 56);
+          vy = vy - mul_shr(vy, delta_fx, 62) + mul_shr(Fy, c, 56);
+          vz = vz - mul_shr(vz, delta_fx, 62) + mul_shr(Fz, c, 56);
           a.vx[g] = vx;
           a.vy[g] = vy;
           a.vz[g] = vz;
@@ -323,8 +319,10 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
           py_acc += vy;
           pz_acc += vz;
         }
-        const float ux = fx32_to_f32(vx), uy = fx32_to_f32(vy), uz = fx32_to_f32(vz);
-        ke_acc += f32_to_fx32(0.5f * s_mass[l] * (ux * ux + uy * uy + uz * uz));
+        const float ux = vel_to_f32(vx), uy = vel_to_f32(vy), uz = vel_to_f32(vz);
+        const float v2 = ux * ux + uy * uy + uz * uz;
+        if (!(v2 < 1.0e12f)) atomicOr(a.err, kErrNonFinite);  // |v| beyond 1e6: a blown-up run
+        ke_acc += f32_to_fx32(0.5f * s_mass[l] * v2);
       }
     }
   }
@@ -388,31 +386,37 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     s_red[wid * 4 + 3] = pz_acc;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  long long k = 0, x = 0, y = 0, z = 0;
-  for (int q = 0; q < nw; q++) {
-    k += s_red[q * 4];
-    x += s_red[q * 4 + 1];
-    y += s_red[q * 4 + 2];
-    z += s_red[q * 4 + 3];
-  }
   SysState& S = a.state[w.sys];
-  S.done = 0;
-  S.ke = (double)k * (1.0 / kTwo32);
-  if (a.mode == 1) {
-    nhc_forward(S, P.dt);
-    // mean velocity, removed from every bead before the next kick (src/md.cpp:505-514)
-    const double n = (double)S.n_beads;
-    S.vcom_fx[0] = __double2ll_rn((double)x / n);
-    S.vcom_fx[1] = __double2ll_rn((double)y / n);
-    S.vcom_fx[2] = __double2ll_rn((double)z / n);
-    const double vx = (double)x / n / kTwo32, vy = (double)y / n / kTwo32, vz = (double)z / n / kTwo32;
-    S.vcom_mag = sqrt(vx * vx + vy * vy + vz * vz);
-    S.steps += 1;
-  } else {
-    S.vcom_fx[0] = S.vcom_fx[1] = S.vcom_fx[2] = 0;
+  __shared__ double s_c0;
+  if (threadIdx.x == 0) {
+    long long k = 0, x = 0, y = 0, z = 0;
+    for (int q = 0; q < nw; q++) {
+      k += s_red[q * 4];
+      x += s_red[q * 4 + 1];
+      y += s_red[q * 4 + 2];
+      z += s_red[q * 4 + 3];
+    }
+    S.done = 0;
+    S.ke = (double)k * (1.0 / kTwo32);
+    if (a.mode == 1) {
+      nhc_forward(S, P.dt);
+      // mean velocity, removed from every bead before the next kick (src/md.cpp:505-514)
+      const double vx = (double)x * S.inv_n, vy = (double)y * S.inv_n, vz = (double)z * S.inv_n;
+      S.vcom_fx[0] = __double2ll_rn(vx);
+      S.vcom_fx[1] = __double2ll_rn(vy);
+      S.vcom_fx[2] = __double2ll_rn(vz);
+      S.vcom_mag = sqrt(vx * vx + vy * vy + vz * vz) * (1.0 / kVelScale);
+      S.steps += 1;
+    } else {
+      S.vcom_fx[0] = S.vcom_fx[1] = S.vcom_fx[2] = 0;
+    }
+    nhc_backward(S, P.dt);
+    s_c0 = S.kick_c0;
   }
-  nhc_backward(S, P.dt, a.inv_mass_d, a.kick_c + (size_t)w.sys * np, np);
+  __syncthreads();
+  // per-bead kick coefficients c0 / m, one template bead per thread
+  long long* kc = a.kick_c + (size_t)w.sys * np;
+  for (int l = threadIdx.x; l < np; l += blockDim.x) kc[l] = __double2ll_rn(s_c0 * a.inv_mass_d[l]);
 }
 
 // First half-kick and drift with periodic wrap (src/md.cpp:409-414, src/bead.h:72-81,113-117),
@@ -433,9 +437,9 @@ __global__ void __launch_bounds__(256) k_drift(DriftArgs a) {
     const int l = t % a.np;
     const long long c = kick_c[l];
     long long vx = a.vx[g] - vcx, vy = a.vy[g] - vcy, vz = a.vz[g] - vcz;
-    vx = vx - mul_shr(vx, delta_fx, 62) + mul_shr(a.fx[g], c, 62);
-    vy = vy - mul_shr(vy, delta_fx, 62) + mul_shr(a.fy[g], c, 62);
-    vz = vz - mul_shr(vz, delta_fx, 62) + mul_shr(a.fz[g], c, 62);
+    vx = vx - mul_shr(vx, delta_fx, 62) + mul_shr(a.fx[g], c, 56);
+    vy = vy - mul_shr(vy, delta_fx, 62) + mul_shr(a.fy[g], c, 56);
+    vz = vz - mul_shr(vz, delta_fx, 62) + mul_shr(a.fz[g], c, 56);
     a.vx[g] = vx;
     a.vy[g] = vy;
     a.vz[g] = vz;
@@ -464,9 +468,9 @@ __global__ void k_state_in(StateArgs a) {
   a.pz[g] = Z;
   a.pos32[g] = make_int4(hi_word(X), hi_word(Y), hi_word(Z), g % a.np);
   if (a.vel_in) {
-    a.vx[g] = __double2ll_rn(a.vel_in[3 * g] * kTwo32);
-    a.vy[g] = __double2ll_rn(a.vel_in[3 * g + 1] * kTwo32);
-    a.vz[g] = __double2ll_rn(a.vel_in[3 * g + 2] * kTwo32);
+    a.vx[g] = __double2ll_rn(a.vel_in[3 * g] * kVelScale);
+    a.vy[g] = __double2ll_rn(a.vel_in[3 * g + 1] * kVelScale);
+    a.vz[g] = __double2ll_rn(a.vel_in[3 * g + 2] * kVelScale);
   } else {
     a.vx[g] = a.vy[g] = a.vz[g] = 0;
   }
@@ -487,9 +491,10 @@ __global__ void k_state_out(StateArgs a) {
     a.pos_out[3 * g + 2] = (double)a.pz[g] * P.fx_to_len;
   }
   if (a.vel_out) {
-    a.vel_out[3 * g] = (double)(a.vx[g] - S.vcom_fx[0]) * inv;
-    a.vel_out[3 * g + 1] = (double)(a.vy[g] - S.vcom_fx[1]) * inv;
-    a.vel_out[3 * g + 2] = (double)(a.vz[g] - S.vcom_fx[2]) * inv;
+    const double iv = 1.0 / kVelScale;
+    a.vel_out[3 * g] = (double)(a.vx[g] - S.vcom_fx[0]) * iv;
+    a.vel_out[3 * g + 1] = (double)(a.vy[g] - S.vcom_fx[1]) * iv;
+    a.vel_out[3 * g + 2] = (double)(a.vz[g] - S.vcom_fx[2]) * iv;
   }
   if (a.force_out) {
     a.force_out[3 * g] = (double)a.fx_in[g] * inv;

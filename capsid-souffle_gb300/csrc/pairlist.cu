@@ -195,105 +195,90 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
     __syncthreads();
     const int j_local = j - p.sub0;
     const bool same = (j == i);
-    // The stale-r2 reuse of src/functions.cpp:97 can only trigger when subunit 0 of the system
-    // is involved; those blocks take the exact sequential-semantics path below.
+    // exact squared distance between bead gi and staged bead jj of subunit j
+    auto d2_exact = [&](int gi, int jj) {
+      const double ex = fixed_diff(a.px[gi], sx[jj], p.fx_to_len);
+      const double ey = fixed_diff(a.py[gi], sy[jj], p.fx_to_len);
+      const double ez = fixed_diff(a.pz[gi], sz[jj], p.fx_to_len);
+      return ex * ex + ey * ey + ez * ez;
+    };
+    // r2 < r_list^2, decided in float unless within the margin of the cut-off
+    auto inside = [&](int gi, int4 pi, int jj) {
+      const int4 pj = s32[jj];
+      const float dx = hi_diff(pi.x, pj.x, unit), dy = hi_diff(pi.y, pj.y, unit), dz = hi_diff(pi.z, pj.z, unit);
+      const float r2f = dx * dx + dy * dy + dz * dz;
+      if (fabsf(r2f - nl2f) > margin) return r2f < nl2f;
+      return d2_exact(gi, jj) < p.nl2;
+    };
+    // The stale-r2 reuse of src/functions.cpp:97 can only trigger when subunit 0 of the system is
+    // involved.  The test there compares a local index with a global id, so a distance is
+    // recomputed unless (i is subunit 0 and ii is its centre) or (j is subunit 0 and jj is its
+    // centre); otherwise the r2 of the most recently computed pair (row-major over the block) is
+    // reused, starting from the centre-centre distance (or 0 when i == j).  Only two exact
+    // distances per row are ever needed for that: the row's last computed pair (carried into
+    // later rows) and the computed pair just before the stale column.
     const bool quirk = p.quirks && (i_local == 0 || j_local == 0);
-    if (!quirk) {
-      for (int r = 0, ii = threadIdx.x; ii < np; ii += blockDim.x, r++) {
-        const int gi = i * np + ii;
-        const int4 pi = a.pos32[gi];
-        const long long xi = a.px[gi], yi = a.py[gi], zi = a.pz[gi];
-        const bool qi = sq[ii] != 0.0f;
-        for (int jj = 0; jj < np; jj++) {
-          if (same) {
-            if (!(jj != ii && qi && sq[jj] != 0.0f)) continue;  // electrostatic only (:94-96)
-          }
-          const int4 pj = s32[jj];
-          float dx = hi_diff(pi.x, pj.x, unit), dy = hi_diff(pi.y, pj.y, unit),
-                dz = hi_diff(pi.z, pj.z, unit);
-          float r2f = dx * dx + dy * dy + dz * dz;
-          bool in;
-          if (fabsf(r2f - nl2f) > margin) {
-            in = r2f < nl2f;
-          } else {
-            double ex = fixed_diff(xi, sx[jj], p.fx_to_len), ey = fixed_diff(yi, sy[jj], p.fx_to_len),
-                   ez = fixed_diff(zi, sz[jj], p.fx_to_len);
-            in = (ex * ex + ey * ey + ez * ez) < p.nl2;
-          }
-          if (!in) continue;
-          if (same) {
-            mask_rows[ii * a.words + (jj >> 5)] |= 1u << (jj & 31);
-          } else {
-            int k = inter_n[r];
-            if (k < a.inter_cap) a.inter_ids[(size_t)k * a.n_beads_total + gi] = j * np + jj;
-            inter_n[r] = k + 1;
-          }
-        }
-      }
-    } else {
-      // Exact semantics of the reference loop for this (i, j) block, in double.  The test at
-      // src/functions.cpp:97 compares a local index with a global id, so a distance is
-      // recomputed only when not (i is subunit 0 and ii is its centre) and not (j is subunit 0
-      // and jj is its centre); otherwise the r2 of the most recent computed pair (in row-major
-      // order over the block) is reused, starting from the centre distance (or 0 when i == j).
-      const int cl = p.center_local;
-      const bool i0 = (i_local == 0), j0 = (j_local == 0);
-      double init_r2 = 0.0;
+    const int cl = p.center_local;
+    const bool i0 = quirk && (i_local == 0), j0 = quirk && (j_local == 0);
+    double init_r2 = 0.0;
+    if (quirk) {
       if (!same) {
-        int cj = j * np + cl;
-        double ex = fixed_diff(cxi, a.px[cj], p.fx_to_len), ey = fixed_diff(cyi, a.py[cj], p.fx_to_len),
-               ez = fixed_diff(czi, a.pz[cj], p.fx_to_len);
+        const int cj = j * np + cl;
+        const double ex = fixed_diff(cxi, a.px[cj], p.fx_to_len), ey = fixed_diff(cyi, a.py[cj], p.fx_to_len),
+                     ez = fixed_diff(czi, a.pz[cj], p.fx_to_len);
         init_r2 = ex * ex + ey * ey + ez * ez;
       }
-      // pass 1: last computed r2 of every row
-      for (int ii = threadIdx.x; ii < np; ii += blockDim.x) {
+      for (int ii = threadIdx.x; ii < np; ii += blockDim.x) {  // pass 1
         const int gi = i * np + ii;
         const bool qi = sq[ii] != 0.0f;
         double last = 0.0;
         int has = 0;
         if (!(i0 && ii == cl)) {
-          for (int jj = 0; jj < np; jj++) {
-            bool cond = same ? (jj != ii && qi && sq[jj] != 0.0f) : true;
-            if (!cond || (j0 && jj == cl)) continue;
-            double ex = fixed_diff(a.px[gi], sx[jj], p.fx_to_len),
-                   ey = fixed_diff(a.py[gi], sy[jj], p.fx_to_len),
-                   ez = fixed_diff(a.pz[gi], sz[jj], p.fx_to_len);
-            last = ex * ex + ey * ey + ez * ez;
-            has = 1;
+          for (int jj = np - 1; jj >= 0; jj--) {
+            const bool cond = same ? (jj != ii && qi && sq[jj] != 0.0f) : true;
+            if (cond && !(j0 && jj == cl)) {
+              last = d2_exact(gi, jj);
+              has = 1;
+              break;
+            }
           }
         }
         row_last[ii] = last;
         row_has[ii] = has;
       }
       __syncthreads();
-      // pass 2: each row starts from the carried value of the nearest earlier computing row
-      for (int r = 0, ii = threadIdx.x; ii < np; ii += blockDim.x, r++) {
-        const int gi = i * np + ii;
-        const bool qi = sq[ii] != 0.0f;
-        double r2 = init_r2;
+    }
+    for (int r = 0, ii = threadIdx.x; ii < np; ii += blockDim.x, r++) {
+      const int gi = i * np + ii;
+      const int4 pi = a.pos32[gi];
+      const bool qi = sq[ii] != 0.0f;
+      double carried = init_r2;
+      if (quirk)
         for (int k = ii - 1; k >= 0; k--)
           if (row_has[k]) {
-            r2 = row_last[k];
+            carried = row_last[k];
             break;
           }
-        const bool row_stale = (i0 && ii == cl);
-        for (int jj = 0; jj < np; jj++) {
-          bool cond = same ? (jj != ii && qi && sq[jj] != 0.0f) : true;
-          if (!cond) continue;
-          if (!row_stale && !(j0 && jj == cl)) {
-            double ex = fixed_diff(a.px[gi], sx[jj], p.fx_to_len),
-                   ey = fixed_diff(a.py[gi], sy[jj], p.fx_to_len),
-                   ez = fixed_diff(a.pz[gi], sz[jj], p.fx_to_len);
-            r2 = ex * ex + ey * ey + ez * ez;
-          }
-          if (!(r2 < p.nl2)) continue;
-          if (same) {
-            mask_rows[ii * a.words + (jj >> 5)] |= 1u << (jj & 31);
-          } else {
-            int k = inter_n[r];
-            if (k < a.inter_cap) a.inter_ids[(size_t)k * a.n_beads_total + gi] = j * np + jj;
-            inter_n[r] = k + 1;
-          }
+      const bool row_stale = i0 && ii == cl;
+      int prev_jj = -1;  // last computed pair of this row
+      for (int jj = 0; jj < np; jj++) {
+        if (same && !(jj != ii && qi && sq[jj] != 0.0f)) continue;  // electrostatic only (:94-96)
+        bool in;
+        if (row_stale) {
+          in = carried < p.nl2;
+        } else if (j0 && jj == cl) {
+          in = (prev_jj >= 0 ? d2_exact(gi, prev_jj) : carried) < p.nl2;
+        } else {
+          in = inside(gi, pi, jj);
+          prev_jj = jj;
+        }
+        if (!in) continue;
+        if (same) {
+          mask_rows[ii * a.words + (jj >> 5)] |= 1u << (jj & 31);
+        } else {
+          int k = inter_n[r];
+          if (k < a.inter_cap) a.inter_ids[(size_t)k * a.n_beads_total + gi] = j * np + jj;
+          inter_n[r] = k + 1;
         }
       }
     }

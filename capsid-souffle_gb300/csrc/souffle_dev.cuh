@@ -82,6 +82,9 @@ struct SysState {
   int m;                 // chain length
   int n_beads;           // beads in this system
   double q[kMaxChain], t[kMaxChain], dof[kMaxChain];
+  double inv_q[kMaxChain];  // 1 / q (0 for the massless dummy link), set on the host
+  double inv_n;             // 1 / n_beads
+  double kick_c0;           // dt sqrt(expfac) / 2 * 2^64 of the next step (per-bead c = c0 / m)
   double xi[kMaxChain], eta[kMaxChain];
   double xi_b[kMaxChain], eta_b[kMaxChain];
   double ke;             // particle_ke carried between steps (src/md.cpp:456)
@@ -166,11 +169,52 @@ __device__ __forceinline__ long long f32_to_fx32(float v) {
   return (long long)(((unsigned long long)(long long)__float2int_rz(hi) << 32) + lo);
 }
 
-// int64 in units of 2^-32 to float, using only 32-bit conversions.
-__device__ __forceinline__ float fx32_to_f32(long long x) {
+// exp(x) for the thermostat's small arguments (x = -dt xi / 4 or -dt xi / 2): for |x| <= 1/16
+// the Taylor series of e^x truncated after x^11, evaluated by Horner's rule (11 dependent
+// multiply-adds, truncation error below x^12/12! < 4e-24 relative); larger |x| use exp().  On
+// GB300 a serial chain of FP64 operations is slow, so a short fixed polynomial beats a general
+// exponential on the thermostat's critical path.
+__host__ __device__ inline double exp_small(double x) {
+  if (!(x >= -0.0625 && x <= 0.0625)) return exp(x);
+  double p = 1.0 / 39916800.0;  // 1/11!
+  p = fma(p, x, 1.0 / 3628800.0);
+  p = fma(p, x, 1.0 / 362880.0);
+  p = fma(p, x, 1.0 / 40320.0);
+  p = fma(p, x, 1.0 / 5040.0);
+  p = fma(p, x, 1.0 / 720.0);
+  p = fma(p, x, 1.0 / 120.0);
+  p = fma(p, x, 1.0 / 24.0);
+  p = fma(p, x, 1.0 / 6.0);
+  p = fma(p, x, 0.5);
+  p = fma(p, x, 1.0);
+  return fma(p, x, 1.0);
+}
+
+// e^x - 1 by the same series (x times the polynomial, no cancellation), expm1() beyond 1/16.
+__host__ __device__ inline double expm1_small(double x) {
+  if (!(x >= -0.0625 && x <= 0.0625)) return expm1(x);
+  double p = 1.0 / 39916800.0;
+  p = fma(p, x, 1.0 / 3628800.0);
+  p = fma(p, x, 1.0 / 362880.0);
+  p = fma(p, x, 1.0 / 40320.0);
+  p = fma(p, x, 1.0 / 5040.0);
+  p = fma(p, x, 1.0 / 720.0);
+  p = fma(p, x, 1.0 / 120.0);
+  p = fma(p, x, 1.0 / 24.0);
+  p = fma(p, x, 1.0 / 6.0);
+  p = fma(p, x, 0.5);
+  p = fma(p, x, 1.0);
+  return p * x;
+}
+
+// Velocities are int64 in units of 2^-40 (resolution 9.1e-13, range +-8.4e6 in LJ units).
+constexpr double kVelScale = 1099511627776.0;  // 2^40
+
+// int64 velocity (2^-40 units) to float, using only 32-bit conversions.
+__device__ __forceinline__ float vel_to_f32(long long x) {
   const int hi = (int)(x >> 32);
   const unsigned int lo = (unsigned int)x;
-  return fmaf((float)lo, 2.3283064365386963e-10f, (float)hi);
+  return fmaf((float)lo, 9.094947017729282e-13f, (float)hi * 0.00390625f);
 }
 
 }  // namespace souffle

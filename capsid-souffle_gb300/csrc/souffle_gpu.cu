@@ -27,6 +27,7 @@ souffle_status fail(souffle_status s, const std::string& msg) {
   return s;
 }
 
+
 #define CUDA_TRY(x)                                                                         \
   do {                                                                                      \
     cudaError_t e_ = (x);                                                                   \
@@ -544,13 +545,14 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
     q.quirks = (h->opt.compat_quirks >= 0) ? 1 : 0;
     q.center_local = p.center_local;
     q.dt = p.dt;
-    // x_fixed advances by v dt 2^64 / L = v_fixed dt 2^32 / L: the multiplier in 2^-40 units
-    const double dx = p.dt * kTwo32 / p.box;
+    // x_fixed advances by v dt 2^64 / L = v_fixed dt 2^24 / L (v_fixed in 2^-40 units): the
+    // multiplier, itself in 2^-40 units
+    const double dx = p.dt * 16777216.0 / p.box;
     if (!(dx < 8388608.0))
-      return fail(SOUFFLE_ERR_BAD_INPUT, "time step too large for the box (dt 2^32 / L >= 2^23)");
+      return fail(SOUFFLE_ERR_BAD_INPUT, "time step too large for the box (dt 2^24 / L >= 2^23)");
     q.drift_fx = (long long)std::llrint(dx * 1099511627776.0);
     for (int i = 0; i < np; i++)
-      if (!(0.5 * p.dt * 1.5 / tpl->bead_mass[i] < 2.0))
+      if (!(0.5 * p.dt * 1.5 / tpl->bead_mass[i] < 0.5))
         return fail(SOUFFLE_ERR_BAD_INPUT, "dt / (2 m) too large for the fixed-point kick");
     h->sp.push_back(q);
     for (int i = 0; i < p.n_subunits; i++) sub_sys[sub0 + i] = k;
@@ -926,6 +928,8 @@ souffle_status souffle_gpu_md_begin(souffle_gpu_system* h) {
       S.dof[m++] = n3;
       S.m = m;
     }
+    for (int j = 0; j < S.m; j++) S.inv_q[j] = S.q[j] != 0 ? 1.0 / S.q[j] : 0.0;
+    S.inv_n = 1.0 / S.n_beads;
   }
   CUDA_TRY(cudaMemcpyAsync(h->d_state.p, st.data(), sizeof(SysState) * h->n_sys, cudaMemcpyHostToDevice, h->stream));
   // initial forces with a rebuild (src/md.cpp:241) and particle_ke (src/md.cpp:258); the last

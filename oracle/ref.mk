@@ -34,7 +34,22 @@ $(OUT)/ref_run: $(HERE)harness/ref_run_main.cpp $(LIBOBJ) $(OUT)/obj/md.o
 $(OUT)/ref_dump: $(HERE)harness/ref_dump_main.cpp $(LIBOBJ)
 	$(CXX) $(CXXFLAGS) $(INC) $^ -o $@
 
+# Link-substitution check of the drop-in binding: the reference driver with src/forces.cpp
+# replaced by capsid-souffle_gb300/dropin/forces_gb300.cpp, linked to libsouffle_gb300.so.
+GB300 := $(HERE)../capsid-souffle_gb300
+GB300LIB := $(GB300)/_build
+DROPOBJ := $(filter-out $(OUT)/obj/forces.o,$(LIBOBJ))
+
+$(OUT)/obj/forces_gb300.o: $(GB300)/dropin/forces_gb300.cpp
+	@mkdir -p $(OUT)/obj
+	$(CXX) $(CXXFLAGS) $(INC) -I$(HERE)../include -c $< -o $@
+
+$(OUT)/ref_run_gb300: $(HERE)harness/ref_run_main.cpp $(DROPOBJ) $(OUT)/obj/md.o $(OUT)/obj/forces_gb300.o
+	$(CXX) $(CXXFLAGS) $(INC) $^ -L$(GB300LIB) -lsouffle_gb300 -Wl,-rpath,$(abspath $(GB300LIB)) -o $@
+
+dropin: $(OUT)/ref_run_gb300
+
 clean:
 	rm -rf $(OUT)
 
-.PHONY: all clean
+.PHONY: all clean dropin

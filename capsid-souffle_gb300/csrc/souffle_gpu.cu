@@ -27,6 +27,15 @@ souffle_status fail(souffle_status s, const std::string& msg) {
   return s;
 }
 
+}  // namespace
+
+namespace souffle {
+// Lets entry points defined in other files report through souffle_gpu_last_error().
+void record_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace souffle
+
+namespace {
+
 
 #define CUDA_TRY(x)                                                                         \
   do {                                                                                      \

@@ -27,7 +27,7 @@ EXPORTED = [
     "souffle_gpu_pairlist_stats", "souffle_gpu_energies", "souffle_gpu_kinetic_energy",
     "souffle_gpu_md_begin", "souffle_gpu_md_steps", "souffle_gpu_md_scalars",
     "souffle_gpu_synchronize", "souffle_gpu_last_error", "souffle_gpu_stream",
-    "souffle_gpu_md_profile",
+    "souffle_gpu_md_profile", "souffle_gpu_kinetic_energy_noalloc",
 ]
 
 

@@ -175,6 +175,22 @@ typedef struct souffle_kernel_times {
 souffle_status souffle_gpu_md_profile(souffle_gpu_system* h, int64_t first_step, int32_t n_steps,
                                       souffle_kernel_times* out);
 
+/* Kinetic energy and velocity sum of a caller-owned device array, for callers that must not
+ * allocate device memory after start-up (a loop that reserves all its GPU memory up front, or a
+ * framework that owns the device heap).  No counterpart in the reference: it is the
+ * particle_kinetic_energy reduction with its per-block scratch in a fixed array inside the
+ * library (about 64 KB per GPU, held until exit) instead of a handle's buffers.
+ *   vel    device pointer, n_beads x 3 doubles (xyz interleaved)
+ *   mass   device pointer, n_beads doubles, or NULL for unit masses
+ *   out    device pointer, 4 doubles: sum 1/2 m |v|^2, sum vx, sum vy, sum vz
+ *   stream cudaStream_t (NULL = default stream); the call is asynchronous on it
+ * At most 4,194,304 beads (SOUFFLE_ERR_BAD_INPUT beyond).  Nothing is allocated or freed.  The
+ * first call on a device looks up the scratch address for that device, so make it before any
+ * stream capture.  All calls share the scratch: calls that overlap on the GPU race; order them
+ * on one stream.  The result is bitwise the same on every call for the same input. */
+souffle_status souffle_gpu_kinetic_energy_noalloc(const double* vel, const double* mass, int64_t n_beads,
+                                                  double* out, void* stream);
+
 /* Text of the last error on this thread. */
 const char* souffle_gpu_last_error(void);
 

@@ -35,27 +35,30 @@ __device__ __forceinline__ float3 dvec(int4 a, int4 b, float unit) {
   return f3(hi_diff(a.x, b.x, unit), hi_diff(a.y, b.y, unit), hi_diff(a.z, b.z, unit));
 }
 
-// Nose-Hoover chain link update, update_chain_xi (src/functions.cpp:33-58).  The two
-// exponentials of the reference are exp(-dt xi/2) and exp(-dt xi/4); the first is the square of
-// the second.  1/Q comes precomputed from the host (no division on the device).
-__device__ void chain_xi(SysState& s, double* xi, int j, double dt) {
-  if (s.q[j] == 0) return;
-  const double e4 = exp_small(-0.25 * dt * xi[j + 1]);
-  const double e2 = e4 * e4;
-  const double g = (j != 0) ? s.q[j - 1] * xi[j - 1] * xi[j - 1] - s.dof[j] * s.t[j]
-                            : 2 * s.ke - s.dof[j] * s.t[j];
-  xi[j] = xi[j] * e2 + 0.5 * dt * s.inv_q[j] * g * e4;
+// Nose-Hoover chain link update, update_chain_xi (src/functions.cpp:33-58):
+//   xi_j <- xi_j e^{-dt xi_{j+1}/2} + dt/(2 Q_j) G_j e^{-dt xi_{j+1}/4}
+// with G_0 = 2 KE - dof_0 T and G_j = Q_{j-1} xi_{j-1}^2 - dof_j T; the first exponential is the
+// square of the second, and 1/Q comes precomputed from the host (no division on the device).
+__device__ __forceinline__ double chain_g(const SysState& s, const double* xi, int j) {
+  return (j != 0) ? s.q[j - 1] * xi[j - 1] * xi[j - 1] - s.dof[j] * s.t[j] : 2 * s.ke - s.dof[j] * s.t[j];
 }
 
-// Backward half at the start of a step (src/md.cpp:401-406), from (xi, eta) into (xi_b, eta_b),
-// then the step's kick factors: expfac, delta = 1 - expfac (2^62 units) and
-// c0 = dt sqrt(expfac)/2 (2^64 units; the per-bead coefficient is c0 / m).
+// Backward half at the start of a step (src/md.cpp:401-406), from (xi, eta) into (xi_b, eta_b):
+// links j = M-1 .. 0, each reading the freshly updated xi_{j+1}; G_j reads xi_{j-1} before it
+// changes, so all G_j are formed first.  Then the step's kick factors: expfac,
+// delta = 1 - expfac (2^62 units) and c0 = dt sqrt(expfac)/2 (2^64 units; per bead c0 / m).
 __device__ void nhc_backward(SysState& s, double dt) {
+  double g[kMaxChain];
   for (int j = 0; j < s.m; j++) {
     s.xi_b[j] = s.xi[j];
     s.eta_b[j] = s.eta[j];
+    g[j] = (s.q[j] != 0) ? chain_g(s, s.xi, j) : 0.0;
   }
-  for (int j = s.m - 1; j > -1; j--) chain_xi(s, s.xi_b, j, dt);
+  for (int j = s.m - 1; j > -1; j--) {
+    if (s.q[j] == 0) continue;
+    const double e4 = exp_small(-0.25 * dt * s.xi_b[j + 1]);
+    s.xi_b[j] = s.xi_b[j] * (e4 * e4) + 0.5 * dt * s.inv_q[j] * g[j] * e4;
+  }
   for (int j = 0; j < s.m; j++)
     if (s.q[j] != 0) s.eta_b[j] = s.eta_b[j] + 0.5 * dt * s.xi_b[j];
   const double x = -0.5 * dt * s.xi_b[0];
@@ -64,15 +67,20 @@ __device__ void nhc_backward(SysState& s, double dt) {
   s.kick_c0 = 0.5 * dt * exp_small(0.5 * x) * 18446744073709551616.0;
 }
 
-// Forward half at the end of a step (src/md.cpp:457-460), from (xi_b, eta_b) into (xi, eta).
+// Forward half at the end of a step (src/md.cpp:457-460), from (xi_b, eta_b) into (xi, eta):
+// links j = 0 .. M-1, each reading xi_{j+1} before it changes, so every exponential is formed
+// first and only G_j (from the freshly updated xi_{j-1}) is on the serial path.
 __device__ void nhc_forward(SysState& s, double dt) {
+  double e4[kMaxChain];
   for (int j = 0; j < s.m; j++) {
     s.xi[j] = s.xi_b[j];
-    s.eta[j] = s.eta_b[j];
+    s.eta[j] = s.eta_b[j] + (s.q[j] != 0 ? 0.5 * dt * s.xi_b[j] : 0.0);
+    e4[j] = (s.q[j] != 0) ? exp_small(-0.25 * dt * s.xi_b[j + 1]) : 1.0;
   }
-  for (int j = 0; j < s.m; j++)
-    if (s.q[j] != 0) s.eta[j] = s.eta[j] + 0.5 * dt * s.xi[j];
-  for (int j = 0; j < s.m; j++) chain_xi(s, s.xi, j, dt);
+  for (int j = 0; j < s.m; j++) {
+    if (s.q[j] == 0) continue;
+    s.xi[j] = s.xi[j] * (e4[j] * e4[j]) + 0.5 * dt * s.inv_q[j] * chain_g(s, s.xi, j) * e4[j];
+  }
 }
 
 // int64 warp sum with a fixed xor tree (exact, so any order gives the same bits)
@@ -98,7 +106,8 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   float4* s_face = s_edge + a.max_sub * ne;                         // [max_sub * nf]
   float4* s_bend = s_face + a.max_sub * nf;                         // [max_sub * nb * 4]
   int4* s_pos = reinterpret_cast<int4*>(s_bend + a.max_sub * nb * 4);  // [max_sub * np]
-  long long* s_red = reinterpret_cast<long long*>(s_pos + a.max_sub * np);  // [4 * 32]
+  float4* s_rel = reinterpret_cast<float4*>(s_pos + a.max_sub * np);   // [max_sub * np]
+  long long* s_red = reinterpret_cast<long long*>(s_rel + a.max_sub * np);  // [4 * 32]
   float* s_tf = reinterpret_cast<float*>(s_red + 4 * 32);           // [n_float], n_float % 4 == 0
   int* s_ti = reinterpret_cast<int*>(s_tf + L.n_float);             // [n_int], n_int % 4 == 0
   float* s_w = reinterpret_cast<float*>(s_ti + L.n_int);            // [np]
@@ -112,10 +121,20 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     for (int t = threadIdx.x; t < (L.n_float >> 2); t += blockDim.x) sf[t] = __ldg(gf + t);
   }
   for (int t = threadIdx.x; t < np; t += blockDim.x) s_w[t] = a.dh_w[w.sys * np + t];
-  for (int t = threadIdx.x; t < nbead; t += blockDim.x) s_pos[t] = a.pos32[bead0 + t];
+  const float unit = P.unit32;
+  // the tile: exact high words for the bonded terms, and for the intra-subunit Debye-Hueckel
+  // loop float coordinates relative to the subunit's centre bead (|r| within the subunit radius)
+  // with the bead's DH weight in .w
+  for (int t = threadIdx.x; t < nbead; t += blockDim.x) {
+    const int4 p = a.pos32[bead0 + t];
+    const int l = t % np;
+    const int4 c = __ldg(&a.pos32[bead0 + (t - l) + P.center_local]);
+    s_pos[t] = p;
+    s_rel[t] = make_float4(hi_diff(p.x, c.x, unit), hi_diff(p.y, c.y, unit), hi_diff(p.z, c.z, unit),
+                           __ldg(&a.dh_w[w.sys * np + l]));
+  }
   __syncthreads();
 
-  const float unit = P.unit32;
   const int* e_pack = s_ti + L.o_edge;
   const int* f_b = s_ti + L.o_face;
   const int* bq = s_ti + L.o_bend;
@@ -244,18 +263,21 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       // thread's parity of the row
       float3 fe = f3(0.f, 0.f, 0.f);
       const float wi = s_w[l];
+      const float4* sr = s_rel + s * np;
+      const float4 ri = sr[l];
       const unsigned int* mrow = a.intra_mask + ((size_t)(w.sub_begin + s) * np + l) * words;
       for (int wd = 0; wd < words; wd++) {
         unsigned int m = __ldg(mrow + wd) & parity;
         while (m) {
           const int jj = (wd << 5) + __ffs(m) - 1;
           m &= m - 1;
-          const float3 d = dvec(pi, sp[jj], unit);
+          const float4 rj = sr[jj];
+          const float3 d = f3(ri.x - rj.x, ri.y - rj.y, ri.z - rj.z);
           const float r2 = dot3(d, d);
           if (r2 < ecut_el2) {
             const float ir = rsqrtf(r2);
             const float r = r2 * ir;
-            const float c = wi * s_w[jj] * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
+            const float c = ri.w * rj.w * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
             fe = fe + d * c;
           }
         }
@@ -386,7 +408,18 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     s_red[wid * 4 + 3] = pz_acc;
   }
   __syncthreads();
-  SysState& S = a.state[w.sys];
+  // The thermostat update is a serial chain of FP64 operations on about a hundred state words;
+  // run it on a shared-memory copy (every CTA thread helps copy in and out) rather than through
+  // dependent global-memory round trips.
+  __shared__ SysState s_state;
+  {
+    static_assert(sizeof(SysState) % 16 == 0, "SysState is copied as int4");
+    const int4* src = reinterpret_cast<const int4*>(a.state + w.sys);
+    int4* dst = reinterpret_cast<int4*>(&s_state);
+    for (int q = threadIdx.x; q < (int)(sizeof(SysState) / 16); q += blockDim.x) dst[q] = __ldcg(src + q);
+  }
+  __syncthreads();
+  SysState& S = s_state;
   __shared__ double s_c0;
   if (threadIdx.x == 0) {
     long long k = 0, x = 0, y = 0, z = 0;
@@ -414,6 +447,11 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     s_c0 = S.kick_c0;
   }
   __syncthreads();
+  {
+    const int4* src = reinterpret_cast<const int4*>(&s_state);
+    int4* dst = reinterpret_cast<int4*>(a.state + w.sys);
+    for (int q = threadIdx.x; q < (int)(sizeof(SysState) / 16); q += blockDim.x) dst[q] = src[q];
+  }
   // per-bead kick coefficients c0 / m, one template bead per thread
   long long* kc = a.kick_c + (size_t)w.sys * np;
   for (int l = threadIdx.x; l < np; l += blockDim.x) kc[l] = __double2ll_rn(s_c0 * a.inv_mass_d[l]);

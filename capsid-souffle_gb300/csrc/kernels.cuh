@@ -20,6 +20,7 @@ struct CellArgs {
   int* sub_cell;          // [S_total]
   int* cell_subs;         // [S_total]
   int total_cells;
+  int n_sys;
 };
 
 struct CandArgs {

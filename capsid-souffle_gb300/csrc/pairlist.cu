@@ -35,16 +35,20 @@ __global__ void k_cells_count(CellArgs a) {
   a.sub_rank[s] = atomicAdd(&a.cell_count[cell], 1);
 }
 
-// Single-CTA exclusive scan over all cells (a few thousand to a few hundred thousand).
+// Exclusive scan of cell counts, one CTA per system: a system's cells hold only its own
+// subunits, which are contiguous, so its scan starts at the system's first subunit and the
+// segments line up into one global cell_start array.
 __global__ void k_cells_scan(CellArgs a) {
   __shared__ int warp_sums[32];
   __shared__ int carry;
-  if (threadIdx.x == 0) carry = 0;
+  const SysParams& P = a.sys[blockIdx.x];
+  const int c0 = P.cell0, nc = P.ncell * P.ncell * P.ncell;
+  if (threadIdx.x == 0) carry = P.sub0;
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int base = 0; base < a.total_cells; base += blockDim.x) {
+  for (int base = 0; base < nc; base += blockDim.x) {
     int i = base + threadIdx.x;
-    int v = (i < a.total_cells) ? a.cell_count[i] : 0;
+    int v = (i < nc) ? a.cell_count[c0 + i] : 0;
     int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -64,12 +68,13 @@ __global__ void k_cells_scan(CellArgs a) {
     }
     __syncthreads();
     int excl = x - v + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
-    if (i < a.total_cells) a.cell_start[i] = excl;
+    if (i < nc) a.cell_start[c0 + i] = excl;
     __syncthreads();
     if (threadIdx.x == blockDim.x - 1) carry = excl + v;
     __syncthreads();
   }
-  if (threadIdx.x == 0) a.cell_start[a.total_cells] = carry;
+  // the end sentinel of the last system (other systems' ends are the next system's first start)
+  if (threadIdx.x == 0 && c0 + nc == a.total_cells) a.cell_start[a.total_cells] = carry;
 }
 
 __global__ void k_cells_scatter(CellArgs a) {
@@ -303,7 +308,7 @@ namespace souffle {
 void launch_cells_count(const CellArgs& a, int grid, int block, cudaStream_t s) {
   k_cells_count<<<grid, block, 0, s>>>(a);
 }
-void launch_cells_scan(const CellArgs& a, cudaStream_t s) { k_cells_scan<<<1, 1024, 0, s>>>(a); }
+void launch_cells_scan(const CellArgs& a, cudaStream_t s) { k_cells_scan<<<a.n_sys, 512, 0, s>>>(a); }
 void launch_cells_scatter(const CellArgs& a, int grid, int block, cudaStream_t s) {
   k_cells_scatter<<<grid, block, 0, s>>>(a);
 }

@@ -78,7 +78,7 @@ struct SysParams {
 // xi_b/eta_b is the chain after the backward half of the next step (what the next step
 // integrates with).  Both halves only need particle_ke, so the backward half of step a+1 is
 // applied right after the forward half of step a.
-struct SysState {
+struct __align__(16) SysState {
   int m;                 // chain length
   int n_beads;           // beads in this system
   double q[kMaxChain], t[kMaxChain], dof[kMaxChain];
@@ -169,42 +169,44 @@ __device__ __forceinline__ long long f32_to_fx32(float v) {
   return (long long)(((unsigned long long)(long long)__float2int_rz(hi) << 32) + lo);
 }
 
-// exp(x) for the thermostat's small arguments (x = -dt xi / 4 or -dt xi / 2): for |x| <= 1/16
-// the Taylor series of e^x truncated after x^11, evaluated by Horner's rule (11 dependent
-// multiply-adds, truncation error below x^12/12! < 4e-24 relative); larger |x| use exp().  On
-// GB300 a serial chain of FP64 operations is slow, so a short fixed polynomial beats a general
-// exponential on the thermostat's critical path.
-__host__ __device__ inline double exp_small(double x) {
-  if (!(x >= -0.0625 && x <= 0.0625)) return exp(x);
-  double p = 1.0 / 39916800.0;  // 1/11!
-  p = fma(p, x, 1.0 / 3628800.0);
-  p = fma(p, x, 1.0 / 362880.0);
-  p = fma(p, x, 1.0 / 40320.0);
-  p = fma(p, x, 1.0 / 5040.0);
-  p = fma(p, x, 1.0 / 720.0);
-  p = fma(p, x, 1.0 / 120.0);
-  p = fma(p, x, 1.0 / 24.0);
-  p = fma(p, x, 1.0 / 6.0);
-  p = fma(p, x, 0.5);
-  p = fma(p, x, 1.0);
-  return fma(p, x, 1.0);
+// (e^x - 1) / x for the thermostat's small arguments (x = -dt xi / 4 or -dt xi / 2), by the
+// Taylor series of e^x.  |x| <= 2^-9: terms through x^6/7! (truncation below x^7/8! < 2e-23
+// relative); |x| <= 1/16: through x^10/11! (below x^11/12! < 4e-24).  The polynomials use
+// Estrin's scheme, so the dependent chain is 3-4 multiply-adds deep instead of 7-11: on GB300 a
+// dependent FP64 operation takes on the order of a hundred cycles, and these exponentials sit on
+// the serial thermostat path that every MD step waits for.
+__host__ __device__ inline double expm1_over_x_series(double x) {
+  const double x2 = x * x;
+  if (x >= -0.001953125 && x <= 0.001953125) {
+    // 1 + x/2 + x^2/6 + x^3/24 + x^4/120 + x^5/720 + x^6/5040
+    const double a = fma(x, 1.0 / 2.0, 1.0);
+    const double b = fma(x, 1.0 / 24.0, 1.0 / 6.0);
+    const double c = fma(x, 1.0 / 720.0, 1.0 / 120.0);
+    const double x4 = x2 * x2;
+    return fma(x4, fma(x2, 1.0 / 5040.0, c), fma(x2, b, a));
+  }
+  // 1 + x/2 + ... + x^10/11!
+  const double a = fma(x, 1.0 / 2.0, 1.0);
+  const double b = fma(x, 1.0 / 24.0, 1.0 / 6.0);
+  const double c = fma(x, 1.0 / 720.0, 1.0 / 120.0);
+  const double d = fma(x, 1.0 / 40320.0, 1.0 / 5040.0);
+  const double e = fma(x, 1.0 / 3628800.0, 1.0 / 362880.0);
+  const double x4 = x2 * x2;
+  const double lo = fma(x2, b, a);
+  const double hi = fma(x2, d, c);
+  const double top = fma(x2, 1.0 / 39916800.0, e);
+  return fma(x4, fma(x4, top, hi), lo);
 }
 
-// e^x - 1 by the same series (x times the polynomial, no cancellation), expm1() beyond 1/16.
+__host__ __device__ inline double exp_small(double x) {
+  if (!(x >= -0.0625 && x <= 0.0625)) return exp(x);
+  return fma(x, expm1_over_x_series(x), 1.0);
+}
+
+// e^x - 1 without cancellation: x times the same series; expm1() beyond 1/16.
 __host__ __device__ inline double expm1_small(double x) {
   if (!(x >= -0.0625 && x <= 0.0625)) return expm1(x);
-  double p = 1.0 / 39916800.0;
-  p = fma(p, x, 1.0 / 3628800.0);
-  p = fma(p, x, 1.0 / 362880.0);
-  p = fma(p, x, 1.0 / 40320.0);
-  p = fma(p, x, 1.0 / 5040.0);
-  p = fma(p, x, 1.0 / 720.0);
-  p = fma(p, x, 1.0 / 120.0);
-  p = fma(p, x, 1.0 / 24.0);
-  p = fma(p, x, 1.0 / 6.0);
-  p = fma(p, x, 0.5);
-  p = fma(p, x, 1.0);
-  return p * x;
+  return x * expm1_over_x_series(x);
 }
 
 // Velocities are int64 in units of 2^-40 (resolution 9.1e-13, range +-8.4e6 in LJ units).

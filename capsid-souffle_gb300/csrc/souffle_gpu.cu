@@ -367,6 +367,7 @@ CellArgs cell_args(souffle_gpu_system* h) {
   a.sub_cell = h->sub_cell.p;
   a.cell_subs = h->cell_subs.p;
   a.total_cells = h->total_cells;
+  a.n_sys = h->n_sys;
   return a;
 }
 
@@ -622,7 +623,7 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(cudaMemset(h->force.p, 0, sizeof(long long) * 3 * N));
 
   h->force_smem = sizeof(float4) * h->subs_per_cta * (L.ne + L.nf + 4 * L.nbend) +
-                  sizeof(int4) * h->subs_per_cta * np + sizeof(double) * 4 * 32 +
+                  (sizeof(int4) + sizeof(float4)) * h->subs_per_cta * np + sizeof(long long) * 4 * 32 +
                   sizeof(float) * (np + L.n_float) + sizeof(int) * L.n_int;
   h->pair_smem = np * (3 * sizeof(long long) + sizeof(int4) + sizeof(double) + sizeof(int) + sizeof(float));
   if (h->force_smem > 200 * 1024) return fail(SOUFFLE_ERR_BAD_INPUT, "template too large for shared memory");

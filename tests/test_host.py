@@ -93,6 +93,34 @@ def test_salt_for_debye_length_inverts_kappa():
         assert abs(1 / state.debye_kappa(c) - lam) < 1e-12
 
 
+def test_thermostat_exponentials_match_libm(tmp_path):
+    """exp_small / expm1_small (truncated Taylor series, Estrin) agree with libm to ~2 ulp."""
+    import math
+    import random
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc")
+    if not nvcc:
+        pytest.skip("nvcc not available")
+    src = tmp_path / "es.cu"
+    src.write_text('#include <cmath>\n#include "souffle_dev.cuh"\n'
+                   'extern "C" double e1(double x) { return souffle::exp_small(x); }\n'
+                   'extern "C" double e2(double x) { return souffle::expm1_small(x); }\n')
+    so = tmp_path / "es.so"
+    subprocess.run([nvcc, "-shared", "-Xcompiler", "-fPIC", "-I",
+                    os.path.join(REPO, "capsid-souffle_gb300", "csrc"), str(src), "-o", str(so)], check=True)
+    lib = ctypes.CDLL(str(so))
+    for f in (lib.e1, lib.e2):
+        f.restype = ctypes.c_double
+        f.argtypes = [ctypes.c_double]
+    rng = random.Random(1)
+    xs = [rng.uniform(-0.0625, 0.0625) for _ in range(20000)] + [-0.0625, 0.0625, 1e-12, -3e-5, 0.2, -1.5]
+    for x in xs:
+        assert abs(lib.e1(x) - math.exp(x)) <= 5e-16 * math.exp(x)
+        if x != 0:
+            assert abs(lib.e2(x) - math.expm1(x)) <= 5e-16 * abs(math.expm1(x)) + 1e-300
+
+
 def test_replica_draws_are_seeded_and_in_range():
     from souffle_gb300 import workloads
     a = workloads.replicas(4, seed=5)

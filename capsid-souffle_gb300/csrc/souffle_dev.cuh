@@ -198,15 +198,53 @@ __host__ __device__ inline double expm1_over_x_series(double x) {
   return fma(x4, fma(x4, top, hi), lo);
 }
 
+// e^x for |x| <= 708: Cody-Waite reduction x = k ln2 + r with ln2 split into a 53-bit head and
+// its tail (|r| <= ln2/2), e^r = 1 + r S(r) with S the series of (e^r - 1)/r through r^12/13!
+// (truncation below r^13/14! < 1.3e-17), evaluated by Estrin's scheme, then an exact scaling by
+// 2^k built from the exponent bits.  About 11 dependent FP64 operations.
+// (e^r - 1)/r through r^12/13! by Estrin's scheme, for |r| <= ln2/2.
+__host__ __device__ inline double expm1_over_r_s13(double r) {
+  const double r2 = r * r, r4 = r2 * r2, r8 = r4 * r4;
+  const double p01 = fma(r, 1.0 / 2.0, 1.0);
+  const double p23 = fma(r, 1.0 / 24.0, 1.0 / 6.0);
+  const double p45 = fma(r, 1.0 / 720.0, 1.0 / 120.0);
+  const double p67 = fma(r, 1.0 / 40320.0, 1.0 / 5040.0);
+  const double p89 = fma(r, 1.0 / 3628800.0, 1.0 / 362880.0);
+  const double pab = fma(r, 1.0 / 479001600.0, 1.0 / 39916800.0);
+  return fma(r8, fma(r4, 1.0 / 6227020800.0, fma(r2, pab, p89)),
+             fma(r4, fma(r2, p67, p45), fma(r2, p23, p01)));
+}
+
+__host__ __device__ inline double exp_reduced(double x) {
+  if (!(x > -708.0 && x < 708.0)) return exp(x);  // overflow, underflow, NaN: the library
+  const double k = rint(x * 1.4426950408889634074);
+  const double r = fma(-k, 2.319046813846299558e-17, fma(-k, 0.69314718055994528623, x));
+  const double er = fma(r, expm1_over_r_s13(r), 1.0);
+  // 2^k for |k| <= 1022, split in two factors so k = +-1022 stays in range
+  const long long ki = (long long)k;
+  const long long k1 = ki / 2, k2 = ki - k1;
+#ifdef __CUDA_ARCH__
+  const double s1 = __longlong_as_double((k1 + 1023) << 52), s2 = __longlong_as_double((k2 + 1023) << 52);
+#else
+  double s1, s2;
+  const long long b1 = (k1 + 1023) << 52, b2 = (k2 + 1023) << 52;
+  __builtin_memcpy(&s1, &b1, 8);
+  __builtin_memcpy(&s2, &b2, 8);
+#endif
+  return (er * s1) * s2;
+}
+
 __host__ __device__ inline double exp_small(double x) {
-  if (!(x >= -0.0625 && x <= 0.0625)) return exp(x);
+  if (!(x >= -0.0625 && x <= 0.0625)) return exp_reduced(x);
   return fma(x, expm1_over_x_series(x), 1.0);
 }
 
-// e^x - 1 without cancellation: x times the same series; expm1() beyond 1/16.
+// e^x - 1 without cancellation: x times a series up to |x| = ln2/2, beyond which e^x - 1 is
+// at least 0.29 in magnitude and the subtraction loses under two bits.
 __host__ __device__ inline double expm1_small(double x) {
-  if (!(x >= -0.0625 && x <= 0.0625)) return expm1(x);
-  return x * expm1_over_x_series(x);
+  if (x >= -0.0625 && x <= 0.0625) return x * expm1_over_x_series(x);
+  if (x >= -0.34657359027997264 && x <= 0.34657359027997264) return x * expm1_over_r_s13(x);
+  return exp_reduced(x) - 1.0;
 }
 
 // Velocities are int64 in units of 2^-40 (resolution 9.1e-13, range +-8.4e6 in LJ units).

@@ -105,20 +105,26 @@ def test_thermostat_exponentials_match_libm(tmp_path):
     src = tmp_path / "es.cu"
     src.write_text('#include <cmath>\n#include "souffle_dev.cuh"\n'
                    'extern "C" double e1(double x) { return souffle::exp_small(x); }\n'
-                   'extern "C" double e2(double x) { return souffle::expm1_small(x); }\n')
+                   'extern "C" double e2(double x) { return souffle::expm1_small(x); }\n'
+                   'extern "C" double e3(double x) { return souffle::exp_reduced(x); }\n')
     so = tmp_path / "es.so"
     subprocess.run([nvcc, "-shared", "-Xcompiler", "-fPIC", "-I",
                     os.path.join(REPO, "capsid-souffle_gb300", "csrc"), str(src), "-o", str(so)], check=True)
     lib = ctypes.CDLL(str(so))
-    for f in (lib.e1, lib.e2):
+    for f in (lib.e1, lib.e2, lib.e3):
         f.restype = ctypes.c_double
         f.argtypes = [ctypes.c_double]
     rng = random.Random(1)
-    xs = [rng.uniform(-0.0625, 0.0625) for _ in range(20000)] + [-0.0625, 0.0625, 1e-12, -3e-5, 0.2, -1.5]
+    xs = ([rng.uniform(-0.0625, 0.0625) for _ in range(10000)] + [rng.uniform(-1, 1) for _ in range(10000)]
+          + [rng.uniform(-700, 700) for _ in range(10000)]
+          + [-0.0625, 0.0625, 1e-12, -3e-5, 0.2, -1.5, 0.3466, -0.3466, 707.0, -707.0])
+    ulp = 2.220446049250313e-16
     for x in xs:
-        assert abs(lib.e1(x) - math.exp(x)) <= 5e-16 * math.exp(x)
+        ex = math.exp(x)
+        assert abs(lib.e1(x) - ex) <= 2 * ulp * ex
+        assert abs(lib.e3(x) - ex) <= 2 * ulp * ex
         if x != 0:
-            assert abs(lib.e2(x) - math.expm1(x)) <= 5e-16 * abs(math.expm1(x)) + 1e-300
+            assert abs(lib.e2(x) - math.expm1(x)) <= 4 * ulp * abs(math.expm1(x)) + 1e-300
 
 
 def test_replica_draws_are_seeded_and_in_range():

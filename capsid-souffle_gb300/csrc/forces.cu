@@ -282,34 +282,48 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
           }
         }
       }
-      // inter-subunit pairs: DH + LJ/WCA, entries k = h, h+2, ...
+      // inter-subunit pairs: DH + LJ/WCA.  The bead's list is one contiguous row; thread h takes
+      // one half of it, in batches of four with every id load, then every position load, in
+      // flight before any use (the gathers are L2 round trips).
       float3 fp = f3(0.f, 0.f, 0.f);
       const int si = species[l];
       const int nint = a.inter_count[g];
       const int att_row = L.lj_att_bits[si];
-      for (int k = h; k < nint; k += 2) {
-        const int j = a.inter_ids[(size_t)k * a.n_beads_total + g];
-        const int4 pj = __ldg(&a.pos32[j]);
-        const int lj = pj.w;
-        const float3 d = dvec(pi, pj, unit);
-        const float r2 = dot3(d, d);
-        float c = 0.f;
-        const float wj = s_w[lj];
-        if (wi * wj != 0.f && r2 < ecut_el2) {
-          const float ir = rsqrtf(r2);
-          const float r = r2 * ir;
-          c = wi * wj * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
+      const int* row = a.inter_ids + (size_t)g * a.inter_cap;
+      const int khalf = (nint + 1) >> 1;
+      const int k0 = h ? khalf : 0, k1 = h ? nint : khalf;
+      for (int k = k0; k < k1; k += 4) {
+        int jn[4];
+        int4 pn[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) jn[u] = (k + u < k1) ? __ldg(row + k + u) : -1;
+#pragma unroll
+        for (int u = 0; u < 4; u++) pn[u] = (jn[u] >= 0) ? __ldg(&a.pos32[jn[u]]) : pi;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if (jn[u] < 0) continue;
+          const int4 pj = pn[u];
+          const int lj = pj.w;
+          const float3 d = dvec(pi, pj, unit);
+          const float r2 = dot3(d, d);
+          float c = 0.f;
+          const float wj = s_w[lj];
+          if (wi * wj != 0.f && r2 < ecut_el2) {
+            const float ir = rsqrtf(r2);
+            const float r = r2 * ir;
+            c = wi * wj * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
+          }
+          const int sj = species[lj];
+          const int pidx = si * kMaxSpecies + sj;
+          if (r2 < pt.cut2[pidx]) {
+            const bool att = (att_row >> sj) & 1;
+            const float eps = att ? (((L.type7_bits >> sj) & 1) ? 50.0f : P.elj_att) : 1.0f;
+            const float ir2 = 1.0f / r2;
+            const float s6 = pt.sig6[pidx] * ir2 * ir2 * ir2;
+            c += 48.0f * eps * s6 * (s6 - 0.5f) * ir2;
+          }
+          fp = fp + d * c;
         }
-        const int sj = species[lj];
-        const int pidx = si * kMaxSpecies + sj;
-        if (r2 < pt.cut2[pidx]) {
-          const bool att = (att_row >> sj) & 1;
-          const float eps = att ? (((L.type7_bits >> sj) & 1) ? 50.0f : P.elj_att) : 1.0f;
-          const float ir2 = 1.0f / r2;
-          const float s6 = pt.sig6[pidx] * ir2 * ir2 * ir2;
-          c += 48.0f * eps * s6 * (s6 - 0.5f) * ir2;
-        }
-        fp = fp + d * c;
       }
       const float tx = fown.x + fe.x + fp.x, ty = fown.y + fe.y + fp.y, tz = fown.z + fe.z + fp.z;
       if (!(isfinite(tx) && isfinite(ty) && isfinite(tz)) ||

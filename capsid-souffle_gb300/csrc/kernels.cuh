@@ -44,7 +44,7 @@ struct PairArgs {
   const int* cand_count;
   int cand_cap;
   unsigned int* intra_mask;  // [S_total * np * words]
-  int* inter_ids;            // [cap * N]
+  int* inter_ids;            // [N][cap] row-major
   int* inter_count;          // [N]
   int* ref_len;              // [N] reference list length (intra + inter)
   int inter_cap;
@@ -61,8 +61,9 @@ struct ForceArgs {
   const int2* sys_slots;     // per system: first partial slot, slot count
   const int4* pos32;
   const unsigned int* intra_mask;
-  const int* inter_ids;
+  const int* inter_ids;      // [N][inter_cap] row-major, ascending
   const int* inter_count;
+  int inter_cap;
   const float* dh_w;         // [n_sys * np] q * exp(kappa sigma/2)/(1 + kappa sigma/2) * sqrt(lb)
   const PairTable* pt;
   const double* inv_mass_d;  // [np] (thermostat thread only)

@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
           mask_rows[ii * a.words + (jj >> 5)] |= 1u << (jj & 31);
         } else {
           int k = inter_n[r];
-          if (k < a.inter_cap) a.inter_ids[(size_t)k * a.n_beads_total + gi] = j * np + jj;
+          if (k < a.inter_cap) a.inter_ids[(size_t)gi * a.inter_cap + k] = j * np + jj;
           inter_n[r] = k + 1;
         }
       }

@@ -423,6 +423,7 @@ ForceArgs force_args(souffle_gpu_system* h, int mode, bool want_parts) {
   a.intra_mask = h->intra_mask.p;
   a.inter_ids = h->inter_ids.p;
   a.inter_count = h->inter_count.p;
+  a.inter_cap = h->inter_cap;
   a.dh_w = h->dh_w.p;
   a.pt = h->pt.p;
   a.inv_mass_d = h->inv_mass.p;
@@ -781,11 +782,12 @@ souffle_status souffle_gpu_get_pairlist(souffle_gpu_system* h, int32_t cap, int3
     std::vector<int> out;
     int k = 0;
     const int n_in = icnt[g];
-    while (k < n_in && iids[(size_t)k * N + g] < lo) out.push_back(iids[(size_t)k++ * N + g]);
+    const int* row = iids.data() + (size_t)g * h->inter_cap;  // row-major [N][cap]
+    while (k < n_in && row[k] < lo) out.push_back(row[k++]);
     for (int jj = 0; jj < np; jj++)
       if (mask[((size_t)sub * np + l) * words + (jj >> 5)] >> (jj & 31) & 1u) out.push_back(lo + jj);
     while (k < n_in) {
-      int v = iids[(size_t)k++ * N + g];
+      int v = row[k++];
       (void)hi;
       out.push_back(v);
     }

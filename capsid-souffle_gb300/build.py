@@ -44,7 +44,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     headers.append(os.path.join(INCLUDE, "souffle_gpu.h"))
-    common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE,
+    common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE,
                      "-I", CSRC, "--expt-relaxed-constexpr"]
     if verbose:
         common += ["-Xptxas", "-v"]

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
+#include "thermostat.cuh"
 
 namespace souffle {
 
@@ -33,54 +34,6 @@ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
 }
 __device__ __forceinline__ float3 dvec(int4 a, int4 b, float unit) {
   return f3(hi_diff(a.x, b.x, unit), hi_diff(a.y, b.y, unit), hi_diff(a.z, b.z, unit));
-}
-
-// Nose-Hoover chain link update, update_chain_xi (src/functions.cpp:33-58):
-//   xi_j <- xi_j e^{-dt xi_{j+1}/2} + dt/(2 Q_j) G_j e^{-dt xi_{j+1}/4}
-// with G_0 = 2 KE - dof_0 T and G_j = Q_{j-1} xi_{j-1}^2 - dof_j T; the first exponential is the
-// square of the second, and 1/Q comes precomputed from the host (no division on the device).
-__device__ __forceinline__ double chain_g(const SysState& s, const double* xi, int j) {
-  return (j != 0) ? s.q[j - 1] * xi[j - 1] * xi[j - 1] - s.dof[j] * s.t[j] : 2 * s.ke - s.dof[j] * s.t[j];
-}
-
-// Backward half at the start of a step (src/md.cpp:401-406), from (xi, eta) into (xi_b, eta_b):
-// links j = M-1 .. 0, each reading the freshly updated xi_{j+1}; G_j reads xi_{j-1} before it
-// changes, so all G_j are formed first.  Then the step's kick factors: expfac,
-// delta = 1 - expfac (2^62 units) and c0 = dt sqrt(expfac)/2 (2^64 units; per bead c0 / m).
-__device__ void nhc_backward(SysState& s, double dt) {
-  double g[kMaxChain];
-  for (int j = 0; j < s.m; j++) {
-    s.xi_b[j] = s.xi[j];
-    s.eta_b[j] = s.eta[j];
-    g[j] = (s.q[j] != 0) ? chain_g(s, s.xi, j) : 0.0;
-  }
-  for (int j = s.m - 1; j > -1; j--) {
-    if (s.q[j] == 0) continue;
-    const double e4 = exp_small(-0.25 * dt * s.xi_b[j + 1]);
-    s.xi_b[j] = s.xi_b[j] * (e4 * e4) + 0.5 * dt * s.inv_q[j] * g[j] * e4;
-  }
-  for (int j = 0; j < s.m; j++)
-    if (s.q[j] != 0) s.eta_b[j] = s.eta_b[j] + 0.5 * dt * s.xi_b[j];
-  const double x = -0.5 * dt * s.xi_b[0];
-  s.expfac = exp_small(x);
-  s.delta_fx = __double2ll_rn(-expm1_small(x) * 4611686018427387904.0);
-  s.kick_c0 = 0.5 * dt * exp_small(0.5 * x) * 18446744073709551616.0;
-}
-
-// Forward half at the end of a step (src/md.cpp:457-460), from (xi_b, eta_b) into (xi, eta):
-// links j = 0 .. M-1, each reading xi_{j+1} before it changes, so every exponential is formed
-// first and only G_j (from the freshly updated xi_{j-1}) is on the serial path.
-__device__ void nhc_forward(SysState& s, double dt) {
-  double e4[kMaxChain];
-  for (int j = 0; j < s.m; j++) {
-    s.xi[j] = s.xi_b[j];
-    s.eta[j] = s.eta_b[j] + (s.q[j] != 0 ? 0.5 * dt * s.xi_b[j] : 0.0);
-    e4[j] = (s.q[j] != 0) ? exp_small(-0.25 * dt * s.xi_b[j + 1]) : 1.0;
-  }
-  for (int j = 0; j < s.m; j++) {
-    if (s.q[j] == 0) continue;
-    s.xi[j] = s.xi[j] * (e4[j] * e4[j]) + 0.5 * dt * s.inv_q[j] * chain_g(s, s.xi, j) * e4[j];
-  }
 }
 
 // int64 warp sum with a fixed xor tree (exact, so any order gives the same bits)
@@ -397,11 +350,20 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   __syncthreads();
   if (!last) return;
 
-  // Last CTA of this system: all threads sum the slots (exact int64), then thread 0 applies the
-  // thermostat and COM updates.
+  // Last CTA of this system: all threads sum the slots (exact int64) while the system's state
+  // is copied into shared memory; then warp 0 runs the thermostat chain (one lane per link) and
+  // warp 1 the centre-of-mass velocity.
   __threadfence();
+  __shared__ SysState s_state;
+  static_assert(sizeof(SysState) % 16 == 0, "SysState is copied as int4");
+  constexpr int kStateVecs = (int)(sizeof(SysState) / 16);
+  const int4* st_src = reinterpret_cast<const int4*>(a.state + w.sys);
+  int4* st_dst = reinterpret_cast<int4*>(&s_state);
+  int4 st_reg = make_int4(0, 0, 0, 0);  // in flight together with the slot loads below
+  if (threadIdx.x < kStateVecs) st_reg = __ldcg(st_src + threadIdx.x);
   const int2 sl = a.sys_slots[w.sys];
   ke_acc = px_acc = py_acc = pz_acc = 0;
+#pragma unroll 4
   for (int q = threadIdx.x; q < sl.y; q += blockDim.x) {
     const longlong2* src = reinterpret_cast<const longlong2*>(a.partial) + 2 * (size_t)(sl.x + q);
     const longlong2 v0 = __ldcg(src), v1 = __ldcg(src + 1);  // L2 (coherent), not L1
@@ -410,6 +372,8 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     py_acc += v1.x;
     pz_acc += v1.y;
   }
+  if (threadIdx.x < kStateVecs) st_dst[threadIdx.x] = st_reg;
+  for (int q = threadIdx.x + blockDim.x; q < kStateVecs; q += blockDim.x) st_dst[q] = __ldcg(st_src + q);
   ke_acc = warp_sum_ll(ke_acc);
   px_acc = warp_sum_ll(px_acc);
   py_acc = warp_sum_ll(py_acc);
@@ -422,53 +386,47 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     s_red[wid * 4 + 3] = pz_acc;
   }
   __syncthreads();
-  // The thermostat update is a serial chain of FP64 operations on about a hundred state words;
-  // run it on a shared-memory copy (every CTA thread helps copy in and out) rather than through
-  // dependent global-memory round trips.
-  __shared__ SysState s_state;
-  {
-    static_assert(sizeof(SysState) % 16 == 0, "SysState is copied as int4");
-    const int4* src = reinterpret_cast<const int4*>(a.state + w.sys);
-    int4* dst = reinterpret_cast<int4*>(&s_state);
-    for (int q = threadIdx.x; q < (int)(sizeof(SysState) / 16); q += blockDim.x) dst[q] = __ldcg(src + q);
-  }
-  __syncthreads();
   SysState& S = s_state;
-  __shared__ double s_c0;
-  if (threadIdx.x == 0) {
-    long long k = 0, x = 0, y = 0, z = 0;
+  const int vcom_warp = nw > 1 ? 1 : 0;
+  if (wid == 0) {
+    if (lane == 0) {
+      long long k = 0;
+      for (int q = 0; q < nw; q++) k += s_red[q * 4];
+      S.done = 0;
+      S.ke = df_from_fixed(k, 2.3283064365386963e-10f);  // 2^-32
+      if (a.mode == 1) S.steps += 1;
+    }
+    __syncwarp();
+    if (a.mode == 1) nhc_forward_warp(S, lane);
+    if (!nhc_backward_warp(S, lane)) atomicOr(a.err, kErrNonFinite);
+  }
+  if (wid == vcom_warp && lane == 0) {
+    long long x = 0, y = 0, z = 0;
     for (int q = 0; q < nw; q++) {
-      k += s_red[q * 4];
       x += s_red[q * 4 + 1];
       y += s_red[q * 4 + 2];
       z += s_red[q * 4 + 3];
     }
-    S.done = 0;
-    S.ke = (double)k * (1.0 / kTwo32);
     if (a.mode == 1) {
-      nhc_forward(S, P.dt);
       // mean velocity, removed from every bead before the next kick (src/md.cpp:505-514)
       const double vx = (double)x * S.inv_n, vy = (double)y * S.inv_n, vz = (double)z * S.inv_n;
       S.vcom_fx[0] = __double2ll_rn(vx);
       S.vcom_fx[1] = __double2ll_rn(vy);
       S.vcom_fx[2] = __double2ll_rn(vz);
       S.vcom_mag = sqrt(vx * vx + vy * vy + vz * vz) * (1.0 / kVelScale);
-      S.steps += 1;
     } else {
       S.vcom_fx[0] = S.vcom_fx[1] = S.vcom_fx[2] = 0;
     }
-    nhc_backward(S, P.dt);
-    s_c0 = S.kick_c0;
   }
   __syncthreads();
-  {
-    const int4* src = reinterpret_cast<const int4*>(&s_state);
-    int4* dst = reinterpret_cast<int4*>(a.state + w.sys);
-    for (int q = threadIdx.x; q < (int)(sizeof(SysState) / 16); q += blockDim.x) dst[q] = src[q];
-  }
+  for (int q = threadIdx.x; q < kStateVecs; q += blockDim.x) reinterpret_cast<int4*>(a.state + w.sys)[q] = st_dst[q];
   // per-bead kick coefficients c0 / m, one template bead per thread
   long long* kc = a.kick_c + (size_t)w.sys * np;
-  for (int l = threadIdx.x; l < np; l += blockDim.x) kc[l] = __double2ll_rn(s_c0 * a.inv_mass_d[l]);
+  for (int l = threadIdx.x; l < np; l += blockDim.x) {
+    long long c = 0;
+    if (!nhc_kick_coefficient(S.kick_c0, a.inv_mass[l], c)) atomicOr(a.err, kErrNonFinite);
+    kc[l] = c;
+  }
 }
 
 // First half-kick and drift with periodic wrap (src/md.cpp:409-414, src/bead.h:72-81,113-117),

@@ -66,7 +66,7 @@ struct ForceArgs {
   int inter_cap;
   const float* dh_w;         // [n_sys * np] q * exp(kappa sigma/2)/(1 + kappa sigma/2) * sqrt(lb)
   const PairTable* pt;
-  const double* inv_mass_d;  // [np] (thermostat thread only)
+  const dfloat* inv_mass;    // [np] 1 / m as double-float (kick coefficients)
   long long* kick_c;         // [n_sys * np] dt sqrt(expfac) / (2 m) * 2^62, written by the last CTA
   long long* fx; long long* fy; long long* fz;   // force, 2^-32 units
   long long* vx; long long* vy; long long* vz;   // velocity, 2^-32 units

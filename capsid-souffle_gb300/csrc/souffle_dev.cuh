@@ -7,13 +7,15 @@
 //                  src/functions.h:42-56, for any |d| < L/2).
 //   pos32[N]       int4 {x>>32, y>>32, z>>32, meta}: the rounded high words read by the pair
 //                  kernels with one 16-byte load; meta = template-local bead index.
-//   vel[3][N]      double velocities.
-//   force[3][N]    double total force (written from the 64-bit fixed-point sum).
+//   vel[3][N]      int64 velocities in units of 2^-40.
+//   force[3][N]    int64 total force in units of 2^-32 (an exact fixed-point sum).
 //   intra_mask     per subunit, np rows of ceil(np/32) words: bit jj of row ii is set when the
 //                  intra-subunit pair (ii, jj) is on bead ii's reference pair list.
-//   inter_ids      [cap][N] column-major global ids of inter-subunit neighbours, ascending.
+//   inter_ids      [N][cap] row-major global ids of inter-subunit neighbours, ascending.
 #pragma once
 #include <cstdint>
+
+#include "dfloat.cuh"
 
 namespace souffle {
 
@@ -77,20 +79,25 @@ struct SysParams {
 // xi/eta is the chain after the forward half of the last step (what energy output reads);
 // xi_b/eta_b is the chain after the backward half of the next step (what the next step
 // integrates with).  Both halves only need particle_ke, so the backward half of step a+1 is
-// applied right after the forward half of step a.
+// applied right after the forward half of step a.  The chain is carried in double-float (hi + lo
+// FP32 pairs, ~48-bit significand): its update is a serial dependency chain, and GB300's FP64
+// latency would put several microseconds of it on every step.
 struct __align__(16) SysState {
   int m;                 // chain length
   int n_beads;           // beads in this system
-  double q[kMaxChain], t[kMaxChain], dof[kMaxChain];
-  double inv_q[kMaxChain];  // 1 / q (0 for the massless dummy link), set on the host
-  double inv_n;             // 1 / n_beads
-  double kick_c0;           // dt sqrt(expfac) / 2 * 2^64 of the next step (per-bead c = c0 / m)
-  double xi[kMaxChain], eta[kMaxChain];
-  double xi_b[kMaxChain], eta_b[kMaxChain];
-  double ke;             // particle_ke carried between steps (src/md.cpp:456)
-  double expfac;         // exp(-dt xi0 / 2) for the next step (src/md.cpp:406)
-  long long delta_fx;    // (1 - expfac) * 2^62 for the integer kicks
-  long long vcom_fx[3];  // mean velocity (2^-32 units) still to subtract from vel (0 once applied)
+  double q[kMaxChain], t[kMaxChain], dof[kMaxChain];  // the chain's Q, T, dof (host copies)
+  dfloat c_q[kMaxChain];          // Q_j                  (constants for the device update,
+  dfloat c_dof_t[kMaxChain];      // dof_j T_j             set on the host at md_begin)
+  dfloat c_hdt_inv_q[kMaxChain];  // dt / (2 Q_j), 0 for the massless dummy link
+  dfloat c_hdt;                   // dt / 2
+  dfloat c_mqdt;                  // -dt / 4
+  double inv_n;                   // 1 / n_beads
+  dfloat xi[kMaxChain], eta[kMaxChain];
+  dfloat xi_b[kMaxChain], eta_b[kMaxChain];
+  dfloat ke;             // particle_ke carried between steps (src/md.cpp:456)
+  dfloat kick_c0;        // dt sqrt(expfac) / 2 of the next step (per-bead kick c = c0 / m)
+  long long delta_fx;    // (1 - expfac) * 2^62 for the integer kicks, expfac = exp(-dt xi0 / 2)
+  long long vcom_fx[3];  // mean velocity (2^-40 units) still to subtract from vel (0 once applied)
   double vcom_mag;       // |mean velocity| removed at the last step (src/md.cpp:623)
   unsigned int done;     // arrival counter for the last-block reduction
   unsigned int steps;    // MD steps completed since md_begin

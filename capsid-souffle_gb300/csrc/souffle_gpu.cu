@@ -15,6 +15,7 @@
 #include "souffle_gpu.h"
 
 #include "kernels.cuh"
+#include "thermostat.cuh"
 
 using namespace souffle;
 
@@ -221,7 +222,8 @@ struct souffle_gpu_system {
   DevBuf<int> cell_count, cell_start, sub_rank, sub_cell, cell_subs;
   DevBuf<float> dh_w;
   DevBuf<PairTable> pt;
-  DevBuf<double> inv_mass, mass_d, q_d, sigma_d, len0_d;
+  DevBuf<dfloat> inv_mass;
+  DevBuf<double> mass_d, q_d, sigma_d, len0_d;
   DevBuf<int> type_d, lj_d;
   DevBuf<double> e_bead, e_tot;
   DevBuf<unsigned int> err;
@@ -317,10 +319,10 @@ souffle_status upload(souffle_gpu_system* h) {
   CUDA_TRY(h->dh_w.alloc(w.size()));
   CUDA_TRY(cudaMemcpy(h->dh_w.p, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
 
-  std::vector<double> im(T.np);
-  for (int i = 0; i < T.np; i++) im[i] = 1.0 / T.mass[i];
+  std::vector<dfloat> im(T.np);
+  for (int i = 0; i < T.np; i++) im[i] = df_from(1.0 / T.mass[i]);
   CUDA_TRY(h->inv_mass.alloc(T.np));
-  CUDA_TRY(cudaMemcpy(h->inv_mass.p, im.data(), T.np * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(h->inv_mass.p, im.data(), T.np * sizeof(dfloat), cudaMemcpyHostToDevice));
   CUDA_TRY(h->mass_d.alloc(T.np));
   CUDA_TRY(cudaMemcpy(h->mass_d.p, T.mass.data(), T.np * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(h->q_d.alloc(T.np));
@@ -426,7 +428,7 @@ ForceArgs force_args(souffle_gpu_system* h, int mode, bool want_parts) {
   a.inter_cap = h->inter_cap;
   a.dh_w = h->dh_w.p;
   a.pt = h->pt.p;
-  a.inv_mass_d = h->inv_mass.p;
+  a.inv_mass = h->inv_mass.p;
   a.kick_c = h->kick_c.p;
   const int64_t N = h->N;
   a.fx = h->force.p;
@@ -563,7 +565,7 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
       return fail(SOUFFLE_ERR_BAD_INPUT, "time step too large for the box (dt 2^24 / L >= 2^23)");
     q.drift_fx = (long long)std::llrint(dx * 1099511627776.0);
     for (int i = 0; i < np; i++)
-      if (!(0.5 * p.dt * 1.5 / tpl->bead_mass[i] < 0.5))
+      if (!(0.5 * p.dt * 1.5 / tpl->bead_mass[i] < 0.45))  // kick coefficient below 0.49 * 2^64
         return fail(SOUFFLE_ERR_BAD_INPUT, "dt / (2 m) too large for the fixed-point kick");
     h->sp.push_back(q);
     for (int i = 0; i < p.n_subunits; i++) sub_sys[sub0 + i] = k;
@@ -889,8 +891,9 @@ souffle_status souffle_gpu_energies(souffle_gpu_system* h, int32_t system, souff
     // THERMOSTAT::potential_energy / kinetic_energy (src/thermostat.h:43-52), kB = 1
     double tpe = 0, tke = 0;
     for (int j = 0; j < S.m; j++) {
-      tpe += S.dof[j] * 1.0 * S.t[j] * S.eta[j];
-      tke += 0.5 * S.q[j] * S.xi[j] * S.xi[j];
+      const double eta = df_to(S.eta[j]), xi = df_to(S.xi[j]);
+      tpe += S.dof[j] * 1.0 * S.t[j] * eta;
+      tke += 0.5 * S.q[j] * xi * xi;
     }
     out->thermo_pe = tpe;
     out->thermo_ke = tke;
@@ -940,7 +943,7 @@ souffle_status souffle_gpu_md_begin(souffle_gpu_system* h) {
       S.dof[m++] = n3;
       S.m = m;
     }
-    for (int j = 0; j < S.m; j++) S.inv_q[j] = S.q[j] != 0 ? 1.0 / S.q[j] : 0.0;
+    nhc_set_constants(S, p.dt);
     S.inv_n = 1.0 / S.n_beads;
   }
   CUDA_TRY(cudaMemcpyAsync(h->d_state.p, st.data(), sizeof(SysState) * h->n_sys, cudaMemcpyHostToDevice, h->stream));
@@ -1046,8 +1049,8 @@ souffle_status souffle_gpu_md_scalars(souffle_gpu_system* h, int32_t system, dou
   SysState S;
   CUDA_TRY(cudaMemcpyAsync(&S, h->d_state.p + system, sizeof(S), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
-  if (ke) *ke = S.ke;
-  if (xi0) *xi0 = S.xi[0];
+  if (ke) *ke = df_to(S.ke);
+  if (xi0) *xi0 = df_to(S.xi[0]);
   if (vcom) *vcom = S.vcom_mag;
   return SOUFFLE_OK;
 }

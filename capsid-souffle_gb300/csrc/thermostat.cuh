@@ -1,0 +1,163 @@
+// Nose-Hoover chain updates of one system in double-float arithmetic, run by the last CTA of
+// each system after the kinetic energy of the step is known.
+//
+// Link update, update_chain_xi (src/functions.cpp:33-58):
+//   xi_j <- xi_j e^{-dt xi_{j+1}/2} + dt/(2 Q_j) G_j e^{-dt xi_{j+1}/4}
+//         = e4 (xi_j e4 + c_j G_j),  e4 = e^{-dt xi_{j+1}/4},  c_j = dt/(2 Q_j)
+// with G_0 = 2 KE - dof_0 T and G_j = Q_{j-1} xi_{j-1}^2 - dof_j T.  Links with Q_j = 0 (the dummy
+// end link) are never updated.
+//
+// Two forms with the same operations in the same order, so they give bitwise equal results:
+// serial functions (host-callable; the CPU checks against FP64 use them) and warp functions for
+// the device, where lane j holds link j: exponentials, G terms and eta updates run on all lanes
+// at once and only the link recurrence passes from lane to lane.
+#pragma once
+#include "souffle_dev.cuh"
+
+namespace souffle {
+
+__host__ __device__ inline bool nhc_active(const SysState& s, int j) { return s.c_q[j].hi != 0.0f; }
+
+// G_j, with prev = xi_{j-1} (unused for j = 0)
+__host__ __device__ inline dfloat nhc_g(const SysState& s, dfloat prev, int j) {
+  if (j == 0) return df_add(dfloat{2.0f * s.ke.hi, 2.0f * s.ke.lo}, df_neg(s.c_dof_t[0]));
+  return df_add(df_mul(s.c_q[j - 1], df_mul(prev, prev)), df_neg(s.c_dof_t[j]));
+}
+
+// e^{-dt xn / 4}; exactly 1 when xn is 0 (the dummy link's xi never moves from 0)
+__host__ __device__ inline dfloat nhc_e4(const SysState& s, dfloat xn) {
+  if (xn.hi == 0.0f && xn.lo == 0.0f) return dfloat{1.0f, 0.0f};
+  return df_exp(df_mul(s.c_mqdt, xn));
+}
+
+__host__ __device__ inline dfloat nhc_link(dfloat x, dfloat e4, dfloat cg) {
+  return df_mul(e4, df_add(df_mul(x, e4), cg));
+}
+
+__host__ __device__ inline dfloat nhc_eta(const SysState& s, dfloat eta, dfloat x) {
+  return df_add(eta, df_mul(s.c_hdt, x));
+}
+
+// Kick factors of the next step from xi_0 after the backward half, h = -dt xi_0 / 4:
+// sqrt(expfac) = e^h, 1 - expfac = -(e^h - 1)(e^h + 1), kick_c0 = dt e^h / 2.  Returns false when
+// they leave the range the fixed-point kick can represent.
+__host__ __device__ inline bool nhc_kick_factors(SysState& s, dfloat xb0) {
+  const dfloat u = df_expm1(df_mul(s.c_mqdt, xb0));
+  const dfloat one_minus = df_neg(df_mul(u, df_add(u, dfloat{2.0f, 0.0f})));
+  s.kick_c0 = df_mul(s.c_hdt, df_add(u, dfloat{1.0f, 0.0f}));
+  // |1 - expfac| < 1.9 keeps delta * 2^62 inside int64; NaN fails the comparison
+  if (!(fabsf(one_minus.hi) < 1.9f) || !(fabsf(s.kick_c0.hi) < 1.0e6f)) return false;
+  s.delta_fx = df_to_fixed(one_minus, 4611686018427387904.0f);  // 2^62
+  return true;
+}
+
+// Forward half at the end of a step (src/md.cpp:457-460), from (xi_b, eta_b) into (xi, eta):
+// links j = 0 .. M-1, each reading xi_{j+1} before it changes (so all exponentials come first)
+// and G_j from the freshly updated xi_{j-1}.
+__host__ __device__ inline void nhc_forward(SysState& s) {
+  dfloat e4[kMaxChain], p[kMaxChain];
+  for (int j = 0; j < s.m; j++) {
+    const bool on = nhc_active(s, j);
+    s.eta[j] = on ? nhc_eta(s, s.eta_b[j], s.xi_b[j]) : s.eta_b[j];
+    if (on) {
+      e4[j] = nhc_e4(s, s.xi_b[j + 1]);
+      p[j] = df_mul(s.xi_b[j], e4[j]);
+    }
+  }
+  dfloat prev = {0.0f, 0.0f};
+  for (int j = 0; j < s.m; j++) {
+    dfloat x = s.xi_b[j];
+    if (nhc_active(s, j)) x = df_mul(e4[j], df_add(p[j], df_mul(s.c_hdt_inv_q[j], nhc_g(s, prev, j))));
+    s.xi[j] = x;
+    prev = x;
+  }
+}
+
+// Backward half at the start of a step (src/md.cpp:401-406), from (xi, eta) into (xi_b, eta_b):
+// links j = M-1 .. 0, each reading the freshly updated xi_{j+1}; G_j reads xi_{j-1} before it
+// changes, so all G_j come first.  Then the step's kick factors.
+__host__ __device__ inline bool nhc_backward(SysState& s) {
+  dfloat cg[kMaxChain];
+  for (int j = 0; j < s.m; j++)
+    if (nhc_active(s, j))
+      cg[j] = df_mul(s.c_hdt_inv_q[j], nhc_g(s, j > 0 ? s.xi[j - 1] : dfloat{0.0f, 0.0f}, j));
+  dfloat next = {0.0f, 0.0f};
+  for (int j = s.m - 1; j > -1; j--) {
+    dfloat x = s.xi[j];
+    if (nhc_active(s, j)) x = nhc_link(x, nhc_e4(s, next), cg[j]);
+    s.xi_b[j] = x;
+    next = x;
+  }
+  for (int j = 0; j < s.m; j++) s.eta_b[j] = nhc_active(s, j) ? nhc_eta(s, s.eta[j], s.xi_b[j]) : s.eta[j];
+  return nhc_kick_factors(s, s.xi_b[0]);
+}
+
+#ifdef __CUDACC__
+static_assert(kMaxChain <= 32, "one lane per chain link");
+
+__device__ inline dfloat df_shfl(dfloat v, int src) {
+  return {__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+// nhc_forward with lane j holding link j; all 32 lanes of one warp call it together (m <= 32).
+__device__ inline void nhc_forward_warp(SysState& s, int lane) {
+  const int m = s.m;
+  const bool mine = lane < m;
+  const bool on = mine && nhc_active(s, lane);
+  const dfloat xb = mine ? s.xi_b[lane] : dfloat{0.0f, 0.0f};
+  dfloat e4 = {1.0f, 0.0f}, p = {0.0f, 0.0f};
+  if (mine) s.eta[lane] = on ? nhc_eta(s, s.eta_b[lane], xb) : s.eta_b[lane];
+  if (on) {
+    e4 = nhc_e4(s, s.xi_b[lane + 1]);
+    p = df_mul(xb, e4);
+  }
+  dfloat x = xb, prev = {0.0f, 0.0f};
+  for (int j = 0; j < m; j++) {
+    if (lane == j && on) x = df_mul(e4, df_add(p, df_mul(s.c_hdt_inv_q[j], nhc_g(s, prev, j))));
+    prev = df_shfl(x, j);
+  }
+  if (mine) s.xi[lane] = x;
+}
+
+// nhc_backward with lane j holding link j; the kick factors are set by lane 0, whose return
+// value is the one that counts.
+__device__ inline bool nhc_backward_warp(SysState& s, int lane) {
+  __syncwarp();  // xi / eta written by other lanes (the forward half) are visible from here on
+  const int m = s.m;
+  const bool mine = lane < m;
+  const bool on = mine && nhc_active(s, lane);
+  dfloat x = mine ? s.xi[lane] : dfloat{0.0f, 0.0f}, cg = {0.0f, 0.0f};
+  if (on) cg = df_mul(s.c_hdt_inv_q[lane], nhc_g(s, lane > 0 ? s.xi[lane - 1] : dfloat{0.0f, 0.0f}, lane));
+  dfloat next = {0.0f, 0.0f};
+  for (int j = m - 1; j > -1; j--) {
+    if (lane == j && on) x = nhc_link(x, nhc_e4(s, next), cg);
+    next = df_shfl(x, j);
+  }
+  if (mine) {
+    s.xi_b[lane] = x;
+    s.eta_b[lane] = on ? nhc_eta(s, s.eta[lane], x) : s.eta[lane];
+  }
+  return lane == 0 ? nhc_kick_factors(s, next) : true;
+}
+#endif
+
+// Host side: chain constants of one system from its parameters (src/md.cpp:187-196).
+inline void nhc_set_constants(SysState& s, double dt) {
+  for (int j = 0; j < s.m; j++) {
+    s.c_q[j] = df_from(s.q[j]);
+    s.c_dof_t[j] = df_from(s.dof[j] * s.t[j]);
+    s.c_hdt_inv_q[j] = s.q[j] != 0 ? df_from(0.5 * dt / s.q[j]) : dfloat{0.0f, 0.0f};
+  }
+  s.c_hdt = df_from(0.5 * dt);
+  s.c_mqdt = df_from(-0.25 * dt);
+}
+
+// Per-bead kick coefficient c0 / m in 2^-64 units; false when it does not fit int64.
+__host__ __device__ inline bool nhc_kick_coefficient(dfloat c0, dfloat inv_mass, long long& out) {
+  const dfloat c = df_mul(c0, inv_mass);
+  if (!(fabsf(c.hi) < 0.49f)) return false;  // < 2^63 - 2^40 in 2^-64 units, NaN excluded
+  out = df_to_fixed(c, 18446744073709551616.0f);  // 2^64
+  return true;
+}
+
+}  // namespace souffle

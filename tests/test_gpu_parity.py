@@ -181,3 +181,26 @@ def test_bad_template_is_rejected():
     with pytest.raises(gpu.SouffleError) as e:
         gpu.GpuSystem(t, [gpu.system_params(opt, d, 20, 5)])
     assert e.value.code == 1
+
+
+def test_thermostat_chain_bitwise_equals_host_double_float(tmp_path):
+    """The device chain (one lane per link) against the same double-float arithmetic run serially
+    on the host, fed the kinetic energies the GPU produced: every step's xi_0 is bitwise equal."""
+    from conftest import build_thermostat_lib, chain_of, run_host_chain
+    lib = build_thermostat_lib(tmp_path)
+    g = load_golden("plain_small")
+    s, t, opt, d = _gpu(g)
+    s.md_begin()
+    ke0, _, _ = s.md_scalars()
+    kes, xis = [ke0], []
+    for a in range(60):
+        s.md_steps(a, 1)
+        ke, xi0, _ = s.md_scalars()
+        kes.append(ke)
+        xis.append(xi0)
+    n3 = 3.0 * t.n_beads * int(g["n_sub"])
+    q, temp, dof = chain_of(int(opt.q), opt.Q, d.T_reduced, n3)
+    rc, rows = run_host_chain(lib, q, temp, dof, opt.t, kes)
+    assert rc == 60
+    assert np.array_equal(rows[:, 0], np.array(xis)), np.abs(rows[:, 0] - np.array(xis)).max()
+    assert np.abs(np.array(xis)).max() > 0

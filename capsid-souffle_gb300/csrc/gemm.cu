@@ -1,0 +1,208 @@
+// tcgen05 GEMM: one CTA per 128 x BN output tile, 128 threads.
+//   warp 0, lane 0  TMA producer: 128 x 64 A and BN x 64 B tiles (128-byte swizzle) into a
+//                   4-stage shared-memory ring, one mbarrier per stage ("full")
+//   warp 1, lane 0  MMA issuer: four K = 16 tcgen05.mma per stage into an FP32 accumulator in
+//                   tensor memory; tcgen05.commit frees the stage ("empty") and, after the last
+//                   stage, signals the epilogue ("accum")
+//   warps 0-3       epilogue: warp w reads accumulator lanes 32w..32w+31 (one output row per
+//                   thread) with tcgen05.ld, applies bias / activation and stores
+// K tails and M/N edges are zero-filled by TMA (out-of-bounds box elements) and masked in the
+// epilogue.  All waits are bounded (umma.cuh); a timeout sets bit 0 of the error flag.
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "gemm.cuh"
+#include "umma.cuh"
+
+namespace souffle {
+
+constexpr int kBM = 128, kBK = 64, kStages = 4;
+
+template <int BN>
+struct GemmTile {
+  static constexpr int kA = kBM * kBK * 2;  // bytes of one A stage
+  static constexpr int kB = BN * kBK * 2;
+  static constexpr int kStage = kA + kB;
+  static constexpr int kBars = 2 * kStages + 1;
+  static constexpr int kSmem = 1024 + kStages * kStage + kBars * 8 + 16;
+  static constexpr int kTmemCols = BN <= 128 ? 128 : 256;
+  static_assert(kStage % 1024 == 0, "stages stay on 1024-byte boundaries (128-byte swizzle atoms)");
+};
+
+__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + expf(-z)); }
+
+template <int BN>
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_bf16(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmEpi e) {
+  using G = GemmTile<BN>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  const uint32_t bars = base + kStages * G::kStage;  // full[s], empty[s], accum
+  const uint32_t tmem_slot = bars + G::kBars * 8;
+  volatile uint32_t* tmem_slot_ptr = reinterpret_cast<volatile uint32_t*>(smem_raw + (tmem_slot - raw));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m_rows = e.m_dyn ? min(e.M, *e.m_dyn) : e.M;
+  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+  if (m0 >= m_rows) return;  // uniform over the CTA, before any allocation
+  const int nk = (e.K + kBK - 1) / kBK;
+  const uint32_t full0 = bars, empty0 = bars + 8 * kStages, accum = bars + 16 * kStages;
+
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, G::kTmemCols);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 32) {
+    for (int s = 0; s < kStages; s++) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(accum, 1);
+    mbar_fence_init();
+  }
+  if (threadIdx.x == 64) {
+    tma_prefetch_map(&ta);
+    tma_prefetch_map(&tb);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot_ptr;
+
+  bool ok = true;
+  if (warp == 0 && lane == 0) {
+    int issued = 0;
+    for (int kt = 0; kt < nk; kt++) {
+      const int s = kt % kStages;
+      const uint32_t use = (uint32_t)(kt / kStages);
+      if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      const uint32_t a_s = base + s * G::kStage;
+      mbar_expect_tx(full0 + 8 * s, G::kStage);
+      tma_load_2d(a_s, &ta, kt * kBK, m0, full0 + 8 * s);
+      tma_load_2d(a_s + G::kA, &tb, kt * kBK, n0, full0 + 8 * s);
+      issued = kt + 1;
+    }
+    // every copy this thread started has landed before the CTA can leave
+    for (int kt = (issued > kStages ? issued - kStages : 0); kt < issued; kt++)
+      if (!mbar_wait(full0 + 8 * (kt % kStages), (uint32_t)(kt / kStages) & 1u)) ok = false;
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = umma_idesc_bf16(kBM, BN);
+    for (int kt = 0; kt < nk; kt++) {
+      const int s = kt % kStages;
+      if (!mbar_wait(full0 + 8 * s, (uint32_t)(kt / kStages) & 1u)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a_s = base + s * G::kStage;
+      const uint64_t ad = sw128_kmajor_desc(a_s), bd = sw128_kmajor_desc(a_s + G::kA);
+#pragma unroll
+      for (int j = 0; j < kBK / 16; j++) umma_bf16(tmem, ad + 2 * j, bd + 2 * j, idesc, (kt | j) != 0 ? 1u : 0u);
+      umma_commit(empty0 + 8 * s);
+    }
+    umma_commit(accum);  // after every MMA issued above has completed
+  }
+  if (!ok) atomicOr(e.err, 1u);
+  __syncwarp();
+
+  if (mbar_wait(accum, 0)) {
+    tc_fence_after();
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int c = 0; c < BN; c += 16) {
+      if (n0 + c >= e.N) break;  // uniform over the warp
+      float v[16];
+      tmem_ld16(t_row + (uint32_t)c, v);
+      if (row >= m_rows || !ok) continue;
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        const int n = n0 + c + i;
+        if (n >= e.N) break;
+        float x = v[i];
+        if (e.bias) x += e.bias[n];
+        if (e.act == kActSilu) {
+          if (e.z_out) e.z_out[(size_t)row * e.ldz + n] = x;
+          x = x * sigmoidf_(x);
+        } else if (e.act == kActSiluGrad) {
+          const float z = e.zin[(size_t)row * e.ldzin + n];
+          const float sg = sigmoidf_(z);
+          x *= sg * (1.0f + z * (1.0f - sg));
+        }
+        if (e.out_f32) e.out_f32[(size_t)row * e.ldo + n] = x;
+        if (e.out_bf16) e.out_bf16[(size_t)row * e.ld_bf16 + n] = __float2bfloat16_rn(x);
+        if (e.out_bf16_t) e.out_bf16_t[(size_t)n * e.ldt + row] = __float2bfloat16_rn(x);
+      }
+    }
+  } else {
+    atomicOr(e.err, 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, G::kTmemCols);
+  }
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// [rows][cols] BF16 matrix with row stride ld elements; box = 64 columns x box_rows rows
+bool make_map(CUtensorMap* m, const void* p, int rows, int cols, int ld, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(p), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, const GemmEpi& e, cudaStream_t st) {
+  using G = GemmTile<BN>;
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    attr = cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::kSmem);
+  });
+  if (attr != cudaSuccess) return attr;
+  CUtensorMap ta, tb;
+  if (!make_map(&ta, A, e.M, e.K, lda, kBM) || !make_map(&tb, B, e.N, e.K, ldb, BN)) return cudaErrorInvalidValue;
+  dim3 grid((e.M + kBM - 1) / kBM, (e.N + BN - 1) / BN);
+  k_gemm_bf16<BN><<<grid, 128, G::kSmem, st>>>(ta, tb, e);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t gemm_bf16(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, const GemmEpi& e,
+                      cudaStream_t stream) {
+  if (e.M < 1 || e.N < 1 || e.K < 1 || !e.err || lda < e.K || ldb < e.K || lda % 8 || ldb % 8 ||
+      (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15))
+    return cudaErrorInvalidValue;
+  if ((e.out_f32 && e.ldo < e.N) || (e.out_bf16 && e.ld_bf16 < e.N) || (e.out_bf16_t && e.ldt < e.M) ||
+      (e.z_out && e.ldz < e.N) || (e.act == kActSiluGrad && (!e.zin || e.ldzin < e.N)))
+    return cudaErrorInvalidValue;
+  return e.N > 128 ? launch<256>(A, lda, B, ldb, e, stream) : launch<128>(A, lda, B, ldb, e, stream);
+}
+
+}  // namespace souffle

@@ -14,6 +14,7 @@
 #include "souffle_dev.cuh"
 #include "souffle_gpu.h"
 
+#include "devbuf.cuh"
 #include "kernels.cuh"
 #include "thermostat.cuh"
 
@@ -44,24 +45,6 @@ namespace {
     if (e_ != cudaSuccess)                                                                  \
       return fail(SOUFFLE_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));     \
   } while (0)
-
-template <class T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  cudaError_t alloc(size_t count) {
-    free();
-    n = count;
-    if (count == 0) return cudaSuccess;
-    return cudaMalloc(&p, sizeof(T) * count);
-  }
-  void free() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  ~DevBuf() { free(); }
-};
 
 // Template tables derived on the host, following generate_lattice (src/initialize.cpp:317-401).
 struct HostTemplate {

@@ -28,6 +28,10 @@ EXPORTED = [
     "souffle_gpu_md_begin", "souffle_gpu_md_steps", "souffle_gpu_md_scalars",
     "souffle_gpu_synchronize", "souffle_gpu_last_error", "souffle_gpu_stream",
     "souffle_gpu_md_profile", "souffle_gpu_kinetic_energy_noalloc",
+    # include/souffle_surrogate.h
+    "souffle_mlp_create", "souffle_mlp_destroy", "souffle_mlp_param_count", "souffle_mlp_get_params",
+    "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_gradients", "souffle_mlp_train_step",
+    "souffle_gemm_bf16",
 ]
 
 
@@ -108,8 +112,21 @@ def load() -> C.CDLL:
     lib.souffle_gpu_stream.restype = C.c_void_p
     lib.souffle_gpu_stream.argtypes = [vp]
     lib.souffle_gpu_md_profile.argtypes = [vp, C.c_int64, C.c_int32, C.POINTER(KernelTimes_)]
+    fp = C.POINTER(C.c_float)
+    lib.souffle_mlp_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_int32,
+                                       C.POINTER(vp)]
+    lib.souffle_mlp_destroy.argtypes = [vp]
+    lib.souffle_mlp_param_count.restype = C.c_int64
+    lib.souffle_mlp_param_count.argtypes = [vp]
+    lib.souffle_mlp_get_params.argtypes = [vp, fp, C.c_int64]
+    lib.souffle_mlp_set_params.argtypes = [vp, fp, C.c_int64]
+    lib.souffle_mlp_forward.argtypes = [vp, vp, C.c_int32, vp]
+    lib.souffle_mlp_gradients.argtypes = [vp, vp, vp, C.c_int32, fp, fp]
+    lib.souffle_mlp_train_step.argtypes = [vp, vp, vp, C.c_int32, C.c_float, fp]
+    lib.souffle_gemm_bf16.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
     for name in EXPORTED:
-        if name not in ("souffle_gpu_last_error", "souffle_gpu_num_beads", "souffle_gpu_stream"):
+        if name not in ("souffle_gpu_last_error", "souffle_gpu_num_beads", "souffle_gpu_stream",
+                        "souffle_mlp_param_count"):
             getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -244,3 +261,55 @@ class GpuSystem:
         k = KernelTimes_()
         _check(self.lib.souffle_gpu_md_profile(self.h, int(first_step), int(n_steps), C.byref(k)))
         return {f: getattr(k, f) for f, _ in KernelTimes_._fields_}
+
+
+class Mlp:
+    """The surrogate network (include/souffle_surrogate.h).  Device arrays are passed as raw
+    pointers (integers), e.g. ``tensor.data_ptr()`` of a contiguous float32 CUDA tensor."""
+
+    def __init__(self, n_in: int, n_out: int, max_batch: int, seed: int = 1, width: int = 256, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        _check(self.lib.souffle_mlp_create(n_in, width, n_out, max_batch, seed, device, C.byref(self.h)))
+        self.n_in, self.n_out, self.width = n_in, n_out, width
+        self.n_params = int(self.lib.souffle_mlp_param_count(self.h))
+
+    def close(self):
+        if self.h:
+            self.lib.souffle_mlp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.n_params, dtype=np.float32)
+        _check(self.lib.souffle_mlp_get_params(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), self.n_params))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(self.lib.souffle_mlp_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float)), self.n_params))
+
+    def forward(self, x_ptr: int, m: int, y_ptr: int) -> None:
+        _check(self.lib.souffle_mlp_forward(self.h, C.c_void_p(x_ptr), m, C.c_void_p(y_ptr)))
+
+    def gradients(self, x_ptr: int, t_ptr: int, m: int):
+        g = np.empty(self.n_params, dtype=np.float32)
+        loss = C.c_float()
+        _check(self.lib.souffle_mlp_gradients(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), m, C.byref(loss),
+                                              g.ctypes.data_as(C.POINTER(C.c_float))))
+        return float(loss.value), g
+
+    def train_step(self, x_ptr: int, t_ptr: int, m: int, lr: float) -> float:
+        loss = C.c_float()
+        _check(self.lib.souffle_mlp_train_step(self.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), m, lr, C.byref(loss)))
+        return float(loss.value)
+
+
+def gemm_bf16(a_ptr: int, b_ptr: int, m: int, n: int, k: int, c_ptr: int, device: int = 0) -> None:
+    """C [m][n] = A [m][k] B [n][k]^T on the tensor cores (device pointers)."""
+    _check(load().souffle_gemm_bf16(C.c_void_p(a_ptr), C.c_void_p(b_ptr), m, n, k, C.c_void_p(c_ptr), device))

@@ -10,8 +10,12 @@ from conftest import REPO, load_golden, golden_workload
 
 
 def _header_symbols():
-    text = open(os.path.join(REPO, "include", "souffle_gpu.h")).read()
-    return sorted(set(re.findall(r"\b(souffle_gpu_\w+)\s*\(", text)))
+    syms = set()
+    for name in sorted(os.listdir(os.path.join(REPO, "include"))):
+        if name.endswith(".h"):
+            text = open(os.path.join(REPO, "include", name)).read()
+            syms |= set(re.findall(r"\b(souffle_(?:gpu|mlp|gemm|surrogate)_\w+)\s*\(", text))
+    return sorted(syms)
 
 
 def test_library_exports_every_declared_symbol():

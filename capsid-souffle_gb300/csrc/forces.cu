@@ -278,6 +278,10 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
           fp = fp + d * c;
         }
       }
+      if (a.surr_f && h == 0) {  // far-field subunit pairs from the learned surrogate
+        const float4 sv = a.surr_f[g];
+        fp = fp + f3(sv.x, sv.y, sv.z);
+      }
       const float tx = fown.x + fe.x + fp.x, ty = fown.y + fe.y + fp.y, tz = fown.z + fe.z + fp.z;
       if (!(isfinite(tx) && isfinite(ty) && isfinite(tz)) ||
           fmaxf(fmaxf(fabsf(tx), fabsf(ty)), fabsf(tz)) > 1.0e9f)

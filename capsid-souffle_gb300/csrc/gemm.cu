@@ -7,7 +7,7 @@
 //   warps 0-3       epilogue: warp w reads accumulator lanes 32w..32w+31 (one output row per
 //                   thread) with tcgen05.ld, applies bias / activation and stores
 // K tails and M/N edges are zero-filled by TMA (out-of-bounds box elements) and masked in the
-// epilogue.  All waits are bounded (umma.cuh); a timeout sets bit 0 of the error flag.
+// epilogue.  All waits are bounded (umma.cuh); a timeout sets err_bit in the error flag word.
 #include <cudaTypedefs.h>
 
 #include <mutex>
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(128, 1)
     }
     umma_commit(accum);  // after every MMA issued above has completed
   }
-  if (!ok) atomicOr(e.err, 1u);
+  if (!ok) atomicOr(e.err, e.err_bit);
   __syncwarp();
 
   if (mbar_wait(accum, 0)) {
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(128, 1)
       }
     }
   } else {
-    atomicOr(e.err, 1u);
+    atomicOr(e.err, e.err_bit);
   }
   tc_fence_before();
   __syncthreads();

@@ -26,7 +26,8 @@ struct GemmEpi {
   int ld_bf16 = 0;
   __nv_bfloat16* out_bf16_t = nullptr;  // transposed [N][ldt]
   int ldt = 0;
-  unsigned int* err = nullptr;    // device flag: bit 0 = a bounded wait ran out
+  unsigned int* err = nullptr;    // device flag word
+  unsigned int err_bit = 1u;      // set in *err when a bounded wait ran out
 };
 
 // Launches on the stream; A/B base addresses 16-byte aligned, lda/ldb multiples of 8 elements.

@@ -46,6 +46,8 @@ struct PairArgs {
   unsigned int* intra_mask;  // [S_total * np * words]
   int* inter_ids;            // [N][cap] row-major
   int* inter_count;          // [N]
+  const unsigned char* cand_far = nullptr;  // [S_total * cand_cap]: candidate left to the surrogate
+  const int* far_ok = nullptr;              // the far flags apply (no far-list overflow)
   int* ref_len;              // [N] reference list length (intra + inter)
   int inter_cap;
   unsigned int* err;
@@ -62,6 +64,7 @@ struct ForceArgs {
   const int4* pos32;
   const unsigned int* intra_mask;
   const int* inter_ids;      // [N][inter_cap] row-major, ascending
+  const float4* surr_f = nullptr;  // [N] far-field forces from the surrogate, or null
   const int* inter_count;
   int inter_cap;
   const float* dh_w;         // [n_sys * np] q * exp(kappa sigma/2)/(1 + kappa sigma/2) * sqrt(lb)

@@ -186,15 +186,19 @@ souffle_status check_gemm_err(souffle_mlp* h) {
   return SOUFFLE_OK;
 }
 
-// forward over m rows of act[0]; keep = store z and transposed activations for the backward pass
-souffle_status forward(souffle_mlp* h, int m, bool keep) {
+// forward over m rows of act[0] (rows >= *m_dyn skipped when given); keep = store z and
+// transposed activations for the backward pass
+cudaError_t forward_on(souffle_mlp* h, int m, bool keep, cudaStream_t st, const int* m_dyn, unsigned int* err,
+                       unsigned int err_bit = 1u) {
   for (int l = 0; l < kLayers; l++) {
     GemmEpi e;
     e.M = m;
+    e.m_dyn = m_dyn;
     e.N = (l == kLayers - 1) ? h->out_pad[l] : h->out[l];
     e.K = h->in[l];
     e.bias = h->b[l].p;
-    e.err = h->err.p;
+    e.err = err;
+    e.err_bit = err_bit;
     if (l < kLayers - 1) {
       e.act = kActSilu;
       e.out_bf16 = h->act[l + 1].p;
@@ -209,8 +213,14 @@ souffle_status forward(souffle_mlp* h, int m, bool keep) {
       e.out_f32 = h->y.p;
       e.ldo = h->out_pad[l];
     }
-    MLP_TRY(gemm_bf16(h->act[l].p, h->in_ld[l], h->wb[l].p, h->in_ld[l], e, h->stream));
+    const cudaError_t r = gemm_bf16(h->act[l].p, h->in_ld[l], h->wb[l].p, h->in_ld[l], e, st);
+    if (r != cudaSuccess) return r;
   }
+  return cudaSuccess;
+}
+
+souffle_status forward(souffle_mlp* h, int m, bool keep) {
+  MLP_TRY(forward_on(h, m, keep, h->stream, nullptr, h->err.p));
   return SOUFFLE_OK;
 }
 
@@ -282,6 +292,34 @@ souffle_status refresh_bf16(souffle_mlp* h, float lr) {
 }
 
 }  // namespace
+
+namespace souffle {
+
+constexpr unsigned int kErrSurrogateBit = 8u;  // the system's error word: surrogate network timeout
+
+// For the surrogate inside a system handle: forward over m_cap rows of x on the caller's stream,
+// rows >= *m_dyn skipped, output left in the network's buffer (*y, row stride *ldy).  Enqueues
+// only, so it can be captured in a CUDA graph.
+cudaError_t mlp_forward_async(souffle_mlp* h, const float* x, int m_cap, const int* m_dyn, unsigned int* err,
+                              cudaStream_t st, const float** y, int* ldy) {
+  if (m_cap < 1 || m_cap > h->cap) return cudaErrorInvalidValue;
+  k_pack_input<<<blocks((long long)m_cap * h->n_in, 256), 256, 0, st>>>(x, m_cap, h->n_in, h->act[0].p, h->in_ld[0],
+                                                                       nullptr, h->cap);
+  cudaError_t r = cudaGetLastError();
+  if (r != cudaSuccess) return r;
+  r = forward_on(h, m_cap, false, st, m_dyn, err, kErrSurrogateBit);
+  *y = h->y.p;
+  *ldy = h->out_pad[kLayers - 1];
+  return r;
+}
+
+void mlp_dims(const souffle_mlp* h, int* n_in, int* n_out, int* cap) {
+  *n_in = h->n_in;
+  *n_out = h->n_out;
+  *cap = h->cap;
+}
+
+}  // namespace souffle
 
 extern "C" {
 

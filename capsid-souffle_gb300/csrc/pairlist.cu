@@ -187,8 +187,10 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
   const int ci_global = i * np + p.center_local;
   const long long cxi = a.px[ci_global], cyi = a.py[ci_global], czi = a.pz[ci_global];
 
+  const bool skip_far = a.cand_far && *a.far_ok;
   for (int c = 0; c < ncand; c++) {
     const int j = cand[c];
+    if (skip_far && a.cand_far[(size_t)i * a.cand_cap + c]) continue;  // uniform over the CTA
     __syncthreads();
     for (int t = threadIdx.x; t < np; t += blockDim.x) {
       int g = j * np + t;

@@ -120,6 +120,7 @@ enum : unsigned int {
   kErrInterOverflow = 1u,
   kErrCandOverflow = 2u,
   kErrNonFinite = 4u,
+  kErrSurrogate = 8u,  // a bounded wait of the surrogate network's tensor-core kernels ran out
 };
 
 __host__ __device__ inline long long fixed_from_fraction(double f) {

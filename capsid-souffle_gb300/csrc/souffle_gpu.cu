@@ -16,6 +16,8 @@
 
 #include "devbuf.cuh"
 #include "kernels.cuh"
+#include "surrogate.cuh"
+#include "system.cuh"
 #include "thermostat.cuh"
 
 using namespace souffle;
@@ -45,23 +47,6 @@ namespace {
     if (e_ != cudaSuccess)                                                                  \
       return fail(SOUFFLE_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));     \
   } while (0)
-
-// Template tables derived on the host, following generate_lattice (src/initialize.cpp:317-401).
-struct HostTemplate {
-  int np = 0, ne = 0, nf = 0, n_lj = 0;
-  std::vector<int> type, edge, edge_type, face, lj;
-  std::vector<double> q, sigma, mass, len0;
-  std::vector<int> edge_f0, edge_f1;   // faces of each edge, face order
-  std::vector<int> bend_edge;          // bending edges in template order
-  std::vector<int> bend;               // [nb*4] b0, b1, across0, across1
-  std::vector<int> bendf;              // [nb*2]
-  std::vector<int> species;            // per bead
-  int nspecies = 0;
-  std::vector<double> sp_sigma;
-  std::vector<int> sp_type;
-  int maxdeg = 1, maxrole = 1;
-  std::vector<int> bead_edges, bead_roles;
-};
 
 souffle_status derive_template(const souffle_template* t, HostTemplate& h) {
   if (!t || t->np <= 0 || t->np > kMaxNp || t->ne < 0 || t->nf < 0 || t->n_lj < 0)
@@ -167,56 +152,6 @@ souffle_status derive_template(const souffle_template* t, HostTemplate& h) {
 }
 
 }  // namespace
-
-struct souffle_gpu_system {
-  HostTemplate tpl;
-  TplLayout L{};
-  std::vector<souffle_params> prm;
-  std::vector<SysParams> sp;
-  souffle_options opt{};
-  int n_sys = 0;
-  int64_t N = 0;
-  int S = 0;
-  int subs_per_cta = 1;
-  int threads = 128;
-  int total_cells = 0;
-  std::vector<WorkItem> work;
-  std::vector<int2> slots;
-  int inter_cap = 96, cand_cap = 128;
-  size_t force_smem = 0, pair_smem = 0;
-  cudaStream_t stream = nullptr;
-  bool began = false, have_state = false;
-  // device
-  DevBuf<int> tpl_i;
-  DevBuf<float> tpl_f;
-  DevBuf<SysParams> d_sys;
-  DevBuf<SysState> d_state;
-  DevBuf<WorkItem> d_work;
-  DevBuf<int2> d_slots;
-  DevBuf<int> d_sub_sys, d_bead_sys;
-  DevBuf<long long> pos_fx;
-  DevBuf<int4> pos32;
-  DevBuf<long long> vel, force, partial, kick_c;   // 2^-32 fixed point
-  DevBuf<float> sbforce;
-  DevBuf<double> staging;
-  DevBuf<unsigned int> intra_mask;
-  DevBuf<int> inter_ids, inter_count, ref_len;
-  DevBuf<int> cand, cand_count;
-  DevBuf<int> cell_count, cell_start, sub_rank, sub_cell, cell_subs;
-  DevBuf<float> dh_w;
-  DevBuf<PairTable> pt;
-  DevBuf<dfloat> inv_mass;
-  DevBuf<double> mass_d, q_d, sigma_d, len0_d;
-  DevBuf<int> type_d, lj_d;
-  DevBuf<double> e_bead, e_tot;
-  DevBuf<unsigned int> err;
-  // graphs keyed by window length
-  std::map<int, cudaGraphExec_t> graphs;
-  ~souffle_gpu_system() {
-    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
 
 namespace {
 
@@ -332,6 +267,7 @@ souffle_status check_err(souffle_gpu_system* h) {
       return fail(SOUFFLE_ERR_NL_OVERFLOW, "inter-subunit pair list exceeded inter_capacity");
     if (e & kErrCandOverflow)
       return fail(SOUFFLE_ERR_NL_OVERFLOW, "candidate subunit list exceeded cand_capacity");
+    if (e & kErrSurrogate) return fail(SOUFFLE_ERR_CUDA, "surrogate network: a bounded wait ran out");
   }
   return SOUFFLE_OK;
 }
@@ -356,7 +292,7 @@ CellArgs cell_args(souffle_gpu_system* h) {
   return a;
 }
 
-void launch_rebuild(souffle_gpu_system* h) {
+void launch_candidates_all(souffle_gpu_system* h) {
   cudaStream_t st = h->stream;
   CellArgs c = cell_args(h);
   cudaMemsetAsync(h->cell_count.p, 0, sizeof(int) * h->total_cells, st);
@@ -371,6 +307,12 @@ void launch_rebuild(souffle_gpu_system* h) {
   ca.cand_count = h->cand_count.p;
   ca.err = h->err.p;
   launch_candidates(ca, gb, tb, st);
+}
+
+void launch_rebuild(souffle_gpu_system* h) {
+  cudaStream_t st = h->stream;
+  CellArgs c = cell_args(h);
+  launch_candidates_all(h);
   PairArgs pa{};
   pa.px = c.px;
   pa.py = c.py;
@@ -392,7 +334,9 @@ void launch_rebuild(souffle_gpu_system* h) {
   pa.ref_len = h->ref_len.p;
   pa.inter_cap = h->inter_cap;
   pa.err = h->err.p;
+  if (surrogate_enabled(h)) surrogate_classify(h, pa);
   launch_pairs(pa, h->S, h->pair_smem, st);
+  if (surrogate_enabled(h)) surrogate_compact(h);
 }
 
 ForceArgs force_args(souffle_gpu_system* h, int mode, bool want_parts) {
@@ -457,13 +401,32 @@ DriftArgs drift_args(souffle_gpu_system* h) {
   return a;
 }
 
-void launch_step(souffle_gpu_system* h, bool rebuild) {
+// k_forces, preceded by the surrogate's far-field forces when it is on
+void launch_forces_all(souffle_gpu_system* h, int mode, bool want_parts, bool judge = false) {
+  ForceArgs fa = force_args(h, mode, want_parts);
+  if (surrogate_enabled(h)) {
+    surrogate_forces(h, fa);
+    if (judge) surrogate_judge(h);
+  }
+  launch_forces(fa, (int)h->work.size(), h->threads, h->force_smem, h->stream);
+}
+
+void launch_step(souffle_gpu_system* h, bool rebuild, bool judge) {
   launch_drift(drift_args(h), (int)h->work.size(), h->threads, h->stream);
   if (rebuild) launch_rebuild(h);
-  launch_forces(force_args(h, 1, false), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+  launch_forces_all(h, 1, false, judge);
 }
 
 }  // namespace
+
+namespace souffle {
+souffle_status check_status(souffle_gpu_system* h) { return check_err(h); }
+souffle_status rebuild_candidates(souffle_gpu_system* h) {
+  launch_candidates_all(h);
+  CUDA_TRY(cudaGetLastError());
+  return SOUFFLE_OK;
+}
+}  // namespace souffle
 
 extern "C" {
 
@@ -727,7 +690,7 @@ souffle_status souffle_gpu_forces(souffle_gpu_system* h, int32_t rebuild, double
   souffle_status s = SOUFFLE_OK;
   for (int attempt = 0; attempt < 4; attempt++) {
     if (rebuild) launch_rebuild(h);
-    launch_forces(force_args(h, 0, parts), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+    launch_forces_all(h, 0, parts);
     CUDA_TRY(cudaGetLastError());
     s = check_err(h);
     // a forces-only call changes no state, so an overflowing list is rebuilt with twice the room
@@ -933,7 +896,7 @@ souffle_status souffle_gpu_md_begin(souffle_gpu_system* h) {
   // initial forces with a rebuild (src/md.cpp:241) and particle_ke (src/md.cpp:258); the last
   // CTA then applies the backward half of the first step
   launch_rebuild(h);
-  launch_forces(force_args(h, 2, false), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+  launch_forces_all(h, 2, false);
   CUDA_TRY(cudaGetLastError());
   souffle_status s = check_err(h);
   if (s != SOUFFLE_OK) return s;
@@ -952,12 +915,15 @@ souffle_status souffle_gpu_md_steps(souffle_gpu_system* h, int64_t first_step, i
   // graphs: key 2*len + rebuild-first; a whole rebuild window is one graph of B steps, any other
   // step is a one-step graph with or without the rebuild
   auto run_graph = [&](int len, bool rebuild_first) -> souffle_status {
-    const int key = 2 * len + (rebuild_first ? 1 : 0);
+    unsigned long long judge_mask = 0;
+    for (int k = 0; k < len && k < 64; k++)
+      if (surrogate_judge_due(h, a + k)) judge_mask |= 1ull << k;
+    const std::pair<int, unsigned long long> key(2 * len + (rebuild_first ? 1 : 0), judge_mask);
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
       cudaGraph_t g;
       CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < len; k++) launch_step(h, k == 0 && rebuild_first);
+      for (int k = 0; k < len; k++) launch_step(h, k == 0 && rebuild_first, (judge_mask >> k) & 1ull);
       CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
       cudaGraphExec_t ge;
       CUDA_TRY(cudaGraphInstantiate(&ge, g, 0));
@@ -969,7 +935,7 @@ souffle_status souffle_gpu_md_steps(souffle_gpu_system* h, int64_t first_step, i
   };
   while (a < end) {
     souffle_status s;
-    if (a % B == 0 && end - a >= B) {
+    if (a % B == 0 && end - a >= B && B <= 64) {
       s = run_graph(B, true);
       a += B;
     } else {
@@ -1001,7 +967,7 @@ souffle_status souffle_gpu_md_profile(souffle_gpu_system* h, int64_t first_step,
     cudaEventRecord(ev[1], h->stream);
     if (rb) launch_rebuild(h);
     cudaEventRecord(ev[2], h->stream);
-    launch_forces(force_args(h, 1, false), (int)h->work.size(), h->threads, h->force_smem, h->stream);
+    launch_forces_all(h, 1, false, surrogate_judge_due(h, a));
     cudaEventRecord(ev[3], h->stream);
     if (cudaEventSynchronize(ev[3]) != cudaSuccess) {
       st = fail(SOUFFLE_ERR_CUDA, "event synchronize failed");

@@ -1,0 +1,1132 @@
+// Learned far-field surrogate inside a system handle (include/souffle_surrogate.h).
+//
+// Per rebuild:  k_far_classify   closest bead distance of every candidate subunit pair (warp per
+//                                pair, FP32 from the exact integer position differences); far
+//                                pairs are flagged so k_pairs leaves them out of the pair list
+//               k_far_scan       per-subunit far counts -> offsets (one CTA), overflow check
+//               k_far_write      the far-pair list (A, B) in candidate order, grouped by A
+// Per step:     k_sub_frames     per subunit: centre of mass, body frame, 12 elastic-mode
+//                                amplitudes, inverse of J = sum |d|^2 I - d d^T (warp per subunit)
+//               k_far_descr      64-float descriptors of the far pairs, normalised
+//               network forward  tcgen05 GEMMs (mlp.cu), rows beyond the far-pair count skipped
+//               k_far_apply      forces on each subunit's beads from its far pairs, summed in
+//                                pair order (warp per subunit), for k_forces to add
+// Judge:        k_far_judge      exact re-evaluation of one far pair in judge_stride against the
+//                                network's output, per distance class
+//               k_judge_decide   relative RMS error per class; classes above the tolerance
+//                                revert to exact at the next rebuild
+// Training:     k_far_targets    exact forces of far pairs as (F, tau, residuals) in A's frame
+//               souffle_surrogate_fit normalises the data set and trains with mlp.cu's kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "devbuf.cuh"
+#include "kernels.cuh"
+#include "souffle_surrogate.h"
+#include "surrogate.cuh"
+#include "system.cuh"
+
+namespace souffle {
+void record_error(const std::string& msg);
+cudaError_t mlp_forward_async(souffle_mlp* h, const float* x, int m_cap, const int* m_dyn, unsigned int* err,
+                              cudaStream_t st, const float** y, int* ldy);
+void mlp_dims(const souffle_mlp* h, int* n_in, int* n_out, int* cap);
+}  // namespace souffle
+
+namespace souffle {
+
+constexpr int kDesc = 64, kModes = 12, kClasses = 4, kFrame = 36;
+constexpr int kBeadsPerLane = 3;  // np <= 96
+
+struct FarArgs {
+  int np, S, cand_cap, far_cap, n_out;
+  float r_switch;
+  const int4* pos32;
+  const SysParams* sys;
+  const int* sub_sys;
+  const int* cand;
+  const int* cand_count;
+  unsigned char* cand_far;
+  float* cand_dmin;
+  int* far_count;
+  int* far_start;   // [S + 1]
+  int* far_total;   // [0] pairs in the list, [1] pairs found, [2] list valid (1) or overflowed (0)
+  int2* far_pair;
+  float* far_dmin;
+  const int* class_off;  // [kClasses] or null (collect: every class)
+  float* frame;          // [S][kFrame]
+  const float* modes;    // [kModes][np][3]
+  const float* rest;     // [np][3]
+  int anchor1, anchor2;
+  float* x;              // [far_cap][kDesc]
+  const float* x_mean;   // null: raw descriptors
+  const float* x_istd;
+  const float* y;        // network output [far_cap][ldy], normalised
+  int ldy;
+  const float* t_mean;
+  const float* t_std;
+  float4* sf;            // [N] far-field force per bead
+  float* targets;        // [far_cap][n_out] raw
+  // exact pair physics (as k_forces)
+  const float* dh_w;
+  const int* species;
+  const PairTable* pt;
+  TplLayout L;
+  // judge
+  int judge_stride;
+  float judge_tol;
+  int* judge_counter;
+  double* judge_acc;     // [kClasses][2]
+  int* judge_n;          // [kClasses]
+  int* class_off_w;      // [kClasses] written by the decision
+  float* judge_err;      // [kClasses]
+  long long* judged;
+  unsigned int* err;
+};
+
+__device__ __forceinline__ float3 f3_(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return f3_(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return f3_(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 mul3(float3 a, float s) { return f3_(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot3_(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3_(float3 a, float3 b) {
+  return f3_(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 norm3(float3 a) { return mul3(a, rsqrtf(fmaxf(dot3_(a, a), 1e-30f))); }
+__device__ __forceinline__ float3 dpos(int4 a, int4 b, float unit) {  // position a - position b
+  return f3_(hi_diff(a.x, b.x, unit), hi_diff(a.y, b.y, unit), hi_diff(a.z, b.z, unit));
+}
+__device__ __forceinline__ float wsum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float3 wsum3(float3 v) { return f3_(wsum(v.x), wsum(v.y), wsum(v.z)); }
+__device__ __forceinline__ int dist_class(float d, float r_sw) {
+  return min(kClasses - 1, max(0, (int)((d - r_sw) * 2.0f)));
+}
+
+struct Frame {
+  float3 e1, e2, e3, m;
+  float Ji[9];
+};
+__device__ __forceinline__ Frame load_frame(const float* f) {
+  Frame F;
+  F.e1 = f3_(f[0], f[1], f[2]);
+  F.e2 = f3_(f[3], f[4], f[5]);
+  F.e3 = f3_(f[6], f[7], f[8]);
+#pragma unroll
+  for (int k = 0; k < 9; k++) F.Ji[k] = f[21 + k];
+  F.m = f3_(f[30], f[31], f[32]);
+  return F;
+}
+__device__ __forceinline__ float3 to_body(const Frame& F, float3 v) {
+  return f3_(dot3_(F.e1, v), dot3_(F.e2, v), dot3_(F.e3, v));
+}
+__device__ __forceinline__ float3 to_lab(const Frame& F, float3 g) {
+  return add3(add3(mul3(F.e1, g.x), mul3(F.e2, g.y)), mul3(F.e3, g.z));
+}
+__device__ __forceinline__ float3 mat3(const float* M, float3 v) {
+  return f3_(M[0] * v.x + M[1] * v.y + M[2] * v.z, M[3] * v.x + M[4] * v.y + M[5] * v.z,
+             M[6] * v.x + M[7] * v.y + M[8] * v.z);
+}
+
+// body-frame positions (relative to the centre of mass) of the beads this lane owns
+__device__ __forceinline__ void body_coords(const FarArgs& a, int s, const Frame& F, int lane, float3 (&e)[kBeadsPerLane],
+                                            int4 (&p)[kBeadsPerLane]) {
+  const SysParams& P = a.sys[a.sub_sys[s]];
+  const int4 pc = a.pos32[(size_t)s * a.np + P.center_local];
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) {
+    const int l = lane + 32 * k;
+    e[k] = f3_(0.f, 0.f, 0.f);
+    p[k] = pc;
+    if (l < a.np) {
+      p[k] = a.pos32[(size_t)s * a.np + l];
+      e[k] = to_body(F, sub3(dpos(p[k], pc, P.unit32), F.m));
+    }
+  }
+}
+
+// ---- rebuild -------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_far_classify(FarArgs a) {
+  extern __shared__ int4 s_pa[];  // [np]
+  __shared__ int s_cnt;
+  const int i = blockIdx.x, np = a.np;
+  for (int t = threadIdx.x; t < np; t += blockDim.x) s_pa[t] = a.pos32[(size_t)i * np + t];
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  const float unit = a.sys[a.sub_sys[i]].unit32;
+  const int ncand = a.cand_count[i];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  int my_far = 0;
+  for (int c = warp; c < ncand; c += nw) {
+    const int j = a.cand[(size_t)i * a.cand_cap + c];
+    float d2 = 3.0e38f;
+    if (j != i) {
+      for (int jj = lane; jj < np; jj += 32) {
+        const int4 pj = a.pos32[(size_t)j * np + jj];
+        for (int ii = 0; ii < np; ii++) {
+          const float3 d = dpos(s_pa[ii], pj, unit);
+          d2 = fminf(d2, dot3_(d, d));
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) d2 = fminf(d2, __shfl_xor_sync(0xffffffffu, d2, o));
+    }
+    if (lane == 0) {
+      const float dmin = sqrtf(d2);
+      bool far = (j != i) && dmin >= a.r_switch;
+      if (far && a.class_off && a.class_off[dist_class(dmin, a.r_switch)]) far = false;
+      a.cand_far[(size_t)i * a.cand_cap + c] = far ? 1 : 0;
+      a.cand_dmin[(size_t)i * a.cand_cap + c] = dmin;
+      my_far += far ? 1 : 0;
+    }
+  }
+  if (lane == 0) atomicAdd(&s_cnt, my_far);
+  __syncthreads();
+  if (threadIdx.x == 0) a.far_count[i] = s_cnt;
+}
+
+// exclusive scan of far_count over all subunits in one CTA of 1024 threads
+__global__ void __launch_bounds__(1024) k_far_scan(FarArgs a) {
+  __shared__ int s[1024];
+  const int n = a.S, t = threadIdx.x;
+  const int per = (n + 1023) / 1024;
+  const int lo = min(n, t * per), hi = min(n, lo + per);
+  int sum = 0;
+  for (int i = lo; i < hi; i++) sum += a.far_count[i];
+  s[t] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int v = t >= o ? s[t - o] : 0;
+    __syncthreads();
+    s[t] += v;
+    __syncthreads();
+  }
+  const int total = s[1023];
+  const bool ok = total <= a.far_cap;
+  int run = s[t] - sum;
+  for (int i = lo; i < hi; i++) {
+    a.far_start[i] = ok ? run : 0;
+    run += a.far_count[i];
+  }
+  if (t == 0) {
+    a.far_start[n] = ok ? total : 0;
+    a.far_total[0] = ok ? total : 0;
+    a.far_total[1] = total;
+    a.far_total[2] = ok ? 1 : 0;
+  }
+}
+
+__global__ void k_far_write(FarArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.S || !a.far_total[2]) return;
+  int k = a.far_start[i];
+  const int nc = a.cand_count[i];
+  for (int c = 0; c < nc; c++) {
+    const size_t e = (size_t)i * a.cand_cap + c;
+    if (!a.cand_far[e]) continue;
+    a.far_pair[k] = make_int2(i, a.cand[e]);
+    a.far_dmin[k] = a.cand_dmin[e];
+    k++;
+  }
+}
+
+// ---- per step ------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_sub_frames(FarArgs a) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * 4 + warp;
+  if (s >= a.S) return;
+  const int np = a.np;
+  const SysParams& P = a.sys[a.sub_sys[s]];
+  const int4 pc = a.pos32[(size_t)s * np + P.center_local];
+  float3 d[kBeadsPerLane];
+  float3 msum = f3_(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) {
+    const int l = lane + 32 * k;
+    d[k] = l < np ? dpos(a.pos32[(size_t)s * np + l], pc, P.unit32) : f3_(0.f, 0.f, 0.f);
+    msum = add3(msum, d[k]);
+  }
+  const float3 m = mul3(wsum3(msum), 1.0f / (float)np);
+  // anchors (uniform indices): broadcast from their lanes
+  float3 b1 = d[0], b2 = d[0];
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) {
+    if ((a.anchor1 >> 5) == k) b1 = d[k];
+    if ((a.anchor2 >> 5) == k) b2 = d[k];
+  }
+  b1 = f3_(__shfl_sync(0xffffffffu, b1.x, a.anchor1 & 31), __shfl_sync(0xffffffffu, b1.y, a.anchor1 & 31),
+           __shfl_sync(0xffffffffu, b1.z, a.anchor1 & 31));
+  b2 = f3_(__shfl_sync(0xffffffffu, b2.x, a.anchor2 & 31), __shfl_sync(0xffffffffu, b2.y, a.anchor2 & 31),
+           __shfl_sync(0xffffffffu, b2.z, a.anchor2 & 31));
+  Frame F;
+  F.e1 = norm3(b1);
+  F.e3 = norm3(cross3_(F.e1, b2));
+  F.e2 = cross3_(F.e3, F.e1);
+  F.m = m;
+  float alpha[kModes];
+#pragma unroll
+  for (int q = 0; q < kModes; q++) alpha[q] = 0.f;
+  float jxx = 0.f, jyy = 0.f, jzz = 0.f, jxy = 0.f, jxz = 0.f, jyz = 0.f;
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) {
+    const int l = lane + 32 * k;
+    if (l >= np) continue;
+    const float3 e = to_body(F, sub3(d[k], m));
+    const float3 u = sub3(e, f3_(a.rest[3 * l], a.rest[3 * l + 1], a.rest[3 * l + 2]));
+#pragma unroll
+    for (int q = 0; q < kModes; q++) {
+      const float* ph = a.modes + ((size_t)q * np + l) * 3;
+      alpha[q] += ph[0] * u.x + ph[1] * u.y + ph[2] * u.z;
+    }
+    jxx += e.y * e.y + e.z * e.z;
+    jyy += e.x * e.x + e.z * e.z;
+    jzz += e.x * e.x + e.y * e.y;
+    jxy -= e.x * e.y;
+    jxz -= e.x * e.z;
+    jyz -= e.y * e.z;
+  }
+#pragma unroll
+  for (int q = 0; q < kModes; q++) alpha[q] = wsum(alpha[q]);
+  jxx = wsum(jxx);
+  jyy = wsum(jyy);
+  jzz = wsum(jzz);
+  jxy = wsum(jxy);
+  jxz = wsum(jxz);
+  jyz = wsum(jyz);
+  if (lane == 0) {
+    float* f = a.frame + (size_t)s * kFrame;
+    f[0] = F.e1.x; f[1] = F.e1.y; f[2] = F.e1.z;
+    f[3] = F.e2.x; f[4] = F.e2.y; f[5] = F.e2.z;
+    f[6] = F.e3.x; f[7] = F.e3.y; f[8] = F.e3.z;
+    for (int q = 0; q < kModes; q++) f[9 + q] = alpha[q];
+    // inverse of the symmetric J by cofactors
+    const float c00 = jyy * jzz - jyz * jyz, c01 = jxz * jyz - jxy * jzz, c02 = jxy * jyz - jxz * jyy;
+    const float c11 = jxx * jzz - jxz * jxz, c12 = jxy * jxz - jxx * jyz, c22 = jxx * jyy - jxy * jxy;
+    const float det = jxx * c00 + jxy * c01 + jxz * c02;
+    const float id = fabsf(det) > 1e-20f ? 1.0f / det : 0.0f;
+    f[21] = c00 * id; f[22] = c01 * id; f[23] = c02 * id;
+    f[24] = c01 * id; f[25] = c11 * id; f[26] = c12 * id;
+    f[27] = c02 * id; f[28] = c12 * id; f[29] = c22 * id;
+    f[30] = m.x; f[31] = m.y; f[32] = m.z;
+    f[33] = f[34] = f[35] = 0.f;
+  }
+}
+
+__global__ void k_far_descr(FarArgs a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.far_total[0]) return;
+  const int2 ab = a.far_pair[p];
+  const int np = a.np;
+  const SysParams& P = a.sys[a.sub_sys[ab.x]];
+  const Frame FA = load_frame(a.frame + (size_t)ab.x * kFrame), FB = load_frame(a.frame + (size_t)ab.y * kFrame);
+  const float3 R = add3(dpos(a.pos32[(size_t)ab.y * np + P.center_local], a.pos32[(size_t)ab.x * np + P.center_local],
+                             P.unit32),
+                        sub3(FB.m, FA.m));
+  const float3 RA = to_body(FA, R), RB = to_body(FB, mul3(R, -1.0f));
+  const float r = sqrtf(fmaxf(dot3_(R, R), 1e-12f));
+  // rotation of B's frame in A's frame: Q_ij = eiA . ejB, then a unit quaternion with w >= 0
+  const float q00 = dot3_(FA.e1, FB.e1), q01 = dot3_(FA.e1, FB.e2), q02 = dot3_(FA.e1, FB.e3);
+  const float q10 = dot3_(FA.e2, FB.e1), q11 = dot3_(FA.e2, FB.e2), q12 = dot3_(FA.e2, FB.e3);
+  const float q20 = dot3_(FA.e3, FB.e1), q21 = dot3_(FA.e3, FB.e2), q22 = dot3_(FA.e3, FB.e3);
+  float qw, qx, qy, qz;
+  const float tr = q00 + q11 + q22;
+  if (tr > 0.f) {
+    const float s2 = sqrtf(tr + 1.f) * 2.f;
+    qw = 0.25f * s2; qx = (q21 - q12) / s2; qy = (q02 - q20) / s2; qz = (q10 - q01) / s2;
+  } else if (q00 > q11 && q00 > q22) {
+    const float s2 = sqrtf(1.f + q00 - q11 - q22) * 2.f;
+    qw = (q21 - q12) / s2; qx = 0.25f * s2; qy = (q01 + q10) / s2; qz = (q02 + q20) / s2;
+  } else if (q11 > q22) {
+    const float s2 = sqrtf(1.f + q11 - q00 - q22) * 2.f;
+    qw = (q02 - q20) / s2; qx = (q01 + q10) / s2; qy = 0.25f * s2; qz = (q12 + q21) / s2;
+  } else {
+    const float s2 = sqrtf(1.f + q22 - q00 - q11) * 2.f;
+    qw = (q10 - q01) / s2; qx = (q02 + q20) / s2; qy = (q12 + q21) / s2; qz = 0.25f * s2;
+  }
+  if (qw < 0.f) { qw = -qw; qx = -qx; qy = -qy; qz = -qz; }
+  float x[kDesc];
+#pragma unroll
+  for (int k = 0; k < kDesc; k++) x[k] = 0.f;
+  x[0] = RA.x; x[1] = RA.y; x[2] = RA.z;
+  x[3] = r; x[4] = 1.0f / r; x[5] = expf(-P.kappa * (r - 8.0f)) / r;
+  x[6] = qw; x[7] = qx; x[8] = qy; x[9] = qz;
+  x[10] = RB.x; x[11] = RB.y; x[12] = RB.z;
+  const float* fa = a.frame + (size_t)ab.x * kFrame;
+  const float* fb = a.frame + (size_t)ab.y * kFrame;
+#pragma unroll
+  for (int q = 0; q < kModes; q++) {
+    x[13 + q] = fa[9 + q];
+    x[25 + q] = fb[9 + q];
+  }
+  x[37] = 1.0f / P.kappa;
+  x[38] = P.elj_att;
+  x[39] = a.far_dmin[p];
+  float* out = a.x + (size_t)p * kDesc;
+#pragma unroll
+  for (int k = 0; k < kDesc; k++) out[k] = a.x_mean ? (x[k] - a.x_mean[k]) * a.x_istd[k] : x[k];
+}
+
+// force on this lane's beads of subunit A (body frame) from the network output row of one pair
+__device__ __forceinline__ void net_body_forces(const FarArgs& a, const float* row, const Frame& F,
+                                                const float3 (&e)[kBeadsPerLane], int lane, float3 (&g)[kBeadsPerLane]) {
+  auto out = [&](int k) { return row[k] * a.t_std[k] + a.t_mean[k]; };
+  const float3 Ft = f3_(out(0), out(1), out(2));
+  const float3 tau = f3_(out(3), out(4), out(5));
+  const float3 w = mat3(F.Ji, tau);
+  const float inv_np = 1.0f / (float)a.np;
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) {
+    const int l = lane + 32 * k;
+    g[k] = f3_(0.f, 0.f, 0.f);
+    if (l < a.np)
+      g[k] = add3(add3(mul3(Ft, inv_np), cross3_(w, e[k])), f3_(out(6 + 3 * l), out(7 + 3 * l), out(8 + 3 * l)));
+  }
+}
+
+__global__ void __launch_bounds__(128) k_far_apply(FarArgs a) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * 4 + warp;
+  if (s >= a.S) return;
+  const int lo = a.far_start[s], hi = a.far_start[s + 1];
+  float3 acc[kBeadsPerLane];
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) acc[k] = f3_(0.f, 0.f, 0.f);
+  Frame F{};
+  if (lo < hi) {
+    F = load_frame(a.frame + (size_t)s * kFrame);
+    float3 e[kBeadsPerLane];
+    int4 p[kBeadsPerLane];
+    body_coords(a, s, F, lane, e, p);
+    for (int q = lo; q < hi; q++) {
+      float3 g[kBeadsPerLane];
+      net_body_forces(a, a.y + (size_t)q * a.ldy, F, e, lane, g);
+#pragma unroll
+      for (int k = 0; k < kBeadsPerLane; k++) acc[k] = add3(acc[k], g[k]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) {
+    const int l = lane + 32 * k;
+    if (l >= a.np) continue;
+    const float3 f = lo < hi ? to_lab(F, acc[k]) : f3_(0.f, 0.f, 0.f);
+    a.sf[(size_t)s * a.np + l] = make_float4(f.x, f.y, f.z, 0.f);
+  }
+}
+
+// exact force on this lane's beads of A from all beads of B, within the pair-list radius: the
+// pair terms of k_forces (Debye-Hueckel, then LJ or WCA by the species table), body frame
+__device__ void exact_body_forces(const FarArgs& a, int A, int B, const Frame& F, const int4 (&p)[kBeadsPerLane],
+                                  int lane, float3 (&g)[kBeadsPerLane]) {
+  const int np = a.np;
+  const int sysid = a.sub_sys[A];
+  const SysParams& P = a.sys[sysid];
+  const float unit = P.unit32, kappa = P.kappa, ecut_el2 = P.ecut_el2, nl2 = P.nl2_f;
+  const PairTable& pt = *a.pt;
+  float3 f[kBeadsPerLane];
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) f[k] = f3_(0.f, 0.f, 0.f);
+  for (int jj = 0; jj < np; jj++) {
+    const int4 pj = a.pos32[(size_t)B * np + jj];
+    const float wj = a.dh_w[(size_t)sysid * np + jj];
+    const int sj = a.species[jj];
+#pragma unroll
+    for (int k = 0; k < kBeadsPerLane; k++) {
+      const int l = lane + 32 * k;
+      if (l >= np) continue;
+      const float3 d = dpos(p[k], pj, unit);
+      const float r2 = dot3_(d, d);
+      if (!(r2 < nl2)) continue;
+      const float wi = a.dh_w[(size_t)sysid * np + l];
+      float c = 0.f;
+      if (wi * wj != 0.f && r2 < ecut_el2) {
+        const float ir = rsqrtf(r2);
+        const float r = r2 * ir;
+        c = wi * wj * expf(-kappa * r) * (ir * ir) * (kappa + ir);
+      }
+      const int si = a.species[l];
+      const int pidx = si * kMaxSpecies + sj;
+      if (r2 < pt.cut2[pidx]) {
+        const bool att = (a.L.lj_att_bits[si] >> sj) & 1;
+        const float eps = att ? (((a.L.type7_bits >> sj) & 1) ? 50.0f : P.elj_att) : 1.0f;
+        const float ir2 = 1.0f / r2;
+        const float s6 = pt.sig6[pidx] * ir2 * ir2 * ir2;
+        c += 48.0f * eps * s6 * (s6 - 0.5f) * ir2;
+      }
+      f[k] = add3(f[k], mul3(d, c));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) g[k] = to_body(F, f[k]);
+}
+
+// training targets: (F, tau, residuals) of the exact forces, raw
+__global__ void __launch_bounds__(128) k_far_targets(FarArgs a) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = blockIdx.x * 4 + warp;
+  if (q >= a.far_total[0]) return;
+  const int2 ab = a.far_pair[q];
+  const Frame F = load_frame(a.frame + (size_t)ab.x * kFrame);
+  float3 e[kBeadsPerLane], g[kBeadsPerLane];
+  int4 p[kBeadsPerLane];
+  body_coords(a, ab.x, F, lane, e, p);
+  exact_body_forces(a, ab.x, ab.y, F, p, lane, g);
+  float3 Ft = f3_(0.f, 0.f, 0.f), tau = f3_(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) {
+    Ft = add3(Ft, g[k]);
+    tau = add3(tau, cross3_(e[k], g[k]));
+  }
+  Ft = wsum3(Ft);
+  tau = wsum3(tau);
+  const float3 w = mat3(F.Ji, tau);
+  float* t = a.targets + (size_t)q * a.n_out;
+  if (lane == 0) {
+    t[0] = Ft.x; t[1] = Ft.y; t[2] = Ft.z;
+    t[3] = tau.x; t[4] = tau.y; t[5] = tau.z;
+  }
+  const float inv_np = 1.0f / (float)a.np;
+#pragma unroll
+  for (int k = 0; k < kBeadsPerLane; k++) {
+    const int l = lane + 32 * k;
+    if (l >= a.np) continue;
+    const float3 r = sub3(sub3(g[k], mul3(Ft, inv_np)), cross3_(w, e[k]));
+    t[6 + 3 * l] = r.x;
+    t[7 + 3 * l] = r.y;
+    t[8 + 3 * l] = r.z;
+  }
+}
+
+// ---- judge ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_far_judge(FarArgs a) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * 4 + warp;
+  const int q = (*a.judge_counter % a.judge_stride) + k * a.judge_stride;
+  if (q >= a.far_total[0]) return;
+  const int2 ab = a.far_pair[q];
+  const Frame F = load_frame(a.frame + (size_t)ab.x * kFrame);
+  float3 e[kBeadsPerLane], gx[kBeadsPerLane], gn[kBeadsPerLane];
+  int4 p[kBeadsPerLane];
+  body_coords(a, ab.x, F, lane, e, p);
+  exact_body_forces(a, ab.x, ab.y, F, p, lane, gx);
+  net_body_forces(a, a.y + (size_t)q * a.ldy, F, e, lane, gn);
+  float num = 0.f, den = 0.f;
+#pragma unroll
+  for (int b = 0; b < kBeadsPerLane; b++) {
+    const float3 dd = sub3(gn[b], gx[b]);
+    num += dot3_(dd, dd);
+    den += dot3_(gx[b], gx[b]);
+  }
+  num = wsum(num);
+  den = wsum(den);
+  if (lane == 0) {
+    const int c = dist_class(a.far_dmin[q], a.r_switch);
+    atomicAdd(&a.judge_acc[2 * c], (double)num);
+    atomicAdd(&a.judge_acc[2 * c + 1], (double)den);
+    atomicAdd(&a.judge_n[c], 1);
+  }
+}
+
+__global__ void k_judge_decide(FarArgs a) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  long long n = 0;
+  for (int c = 0; c < kClasses; c++) {
+    const int nc = a.judge_n[c];
+    n += nc;
+    if (nc > 0 && a.judge_acc[2 * c + 1] > 0.0) {
+      const double e = sqrt(a.judge_acc[2 * c] / a.judge_acc[2 * c + 1]);
+      a.judge_err[c] = (float)e;
+      if (!(e <= (double)a.judge_tol)) a.class_off_w[c] = 1;
+    }
+    a.judge_acc[2 * c] = a.judge_acc[2 * c + 1] = 0.0;
+    a.judge_n[c] = 0;
+  }
+  *a.judged += n;
+  *a.judge_counter += 1;
+}
+
+// ---- training helpers ----------------------------------------------------------------------
+// per-column mean and 1/std (0 for a constant column) of data [n][cols], one CTA per column
+__global__ void k_col_stats(const float* d, int n, int cols, float* mean, float* istd, float* sd_out) {
+  __shared__ double s1[256], s2[256];
+  const int c = blockIdx.x;
+  double a = 0, b = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = d[(size_t)i * cols + c];
+    a += v;
+    b += v * v;
+  }
+  s1[threadIdx.x] = a;
+  s2[threadIdx.x] = b;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s1[threadIdx.x] += s1[threadIdx.x + o];
+      s2[threadIdx.x] += s2[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double m = s1[0] / n, var = fmax(0.0, s2[0] / n - m * m), sd = sqrt(var);
+    mean[c] = (float)m;
+    istd[c] = (sd > 1e-6 * fabs(m) && sd > 1e-30) ? (float)(1.0 / sd) : 0.0f;  // constant column: 0
+    if (sd_out) sd_out[c] = sd > 0 ? (float)sd : 1.0f;
+  }
+}
+
+// out[i] = (in[perm[i]] - mean) * istd, rows of cols floats
+__global__ void k_normalise_rows(const float* in, const int* perm, int n, int cols, const float* mean,
+                                 const float* istd, float* out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)n * cols) return;
+  const int r = (int)(i / cols), c = (int)(i - (long long)r * cols);
+  out[i] = (in[(size_t)perm[r] * cols + c] - mean[c]) * istd[c];
+}
+
+}  // namespace souffle
+
+using namespace souffle;
+
+namespace souffle {
+
+struct SurrogateCtx {
+  souffle_mlp* net = nullptr;
+  souffle_surrogate_options opt{};
+  int np = 0, n_out = 0, far_cap = 0;
+  int anchor1 = 0, anchor2 = 0;
+  bool enabled = false, have_norm = false;
+  DevBuf<float> modes, rest, x_mean, x_istd, t_mean, t_std, t_istd;
+  DevBuf<unsigned char> cand_far;
+  DevBuf<float> cand_dmin, far_dmin, frame, x;
+  DevBuf<int> far_count, far_start, far_total, class_off, judge_n, judge_counter;
+  DevBuf<int2> far_pair;
+  DevBuf<float4> sf;
+  DevBuf<double> judge_acc;
+  DevBuf<float> judge_err;
+  DevBuf<long long> judged;
+  const float* y = nullptr;  // network output (inside the network's buffers) of the last forward
+  int ldy = 0;
+};
+
+void surrogate_free(SurrogateCtx* s) { delete s; }
+
+}  // namespace souffle
+
+namespace {
+
+souffle_status sfail(souffle_status s, const std::string& msg) {
+  record_error(msg);
+  return s;
+}
+
+#define S_TRY(x)                                                                                      \
+  do {                                                                                                \
+    cudaError_t e_ = (x);                                                                             \
+    if (e_ != cudaSuccess) return sfail(SOUFFLE_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+FarArgs far_args(souffle_gpu_system* h) {
+  SurrogateCtx& c = *h->sur;
+  FarArgs a{};
+  a.np = h->tpl.np;
+  a.S = h->S;
+  a.cand_cap = h->cand_cap;
+  a.far_cap = c.far_cap;
+  a.n_out = c.n_out;
+  a.r_switch = (float)c.opt.switch_radius;
+  a.pos32 = h->pos32.p;
+  a.sys = h->d_sys.p;
+  a.sub_sys = h->d_sub_sys.p;
+  a.cand = h->cand.p;
+  a.cand_count = h->cand_count.p;
+  a.cand_far = c.cand_far.p;
+  a.cand_dmin = c.cand_dmin.p;
+  a.far_count = c.far_count.p;
+  a.far_start = c.far_start.p;
+  a.far_total = c.far_total.p;
+  a.far_pair = c.far_pair.p;
+  a.far_dmin = c.far_dmin.p;
+  a.class_off = c.class_off.p;
+  a.frame = c.frame.p;
+  a.modes = c.modes.p;
+  a.rest = c.rest.p;
+  a.anchor1 = c.anchor1;
+  a.anchor2 = c.anchor2;
+  a.x = c.x.p;
+  a.x_mean = c.x_mean.p;
+  a.x_istd = c.x_istd.p;
+  a.y = c.y;
+  a.ldy = c.ldy;
+  a.t_mean = c.t_mean.p;
+  a.t_std = c.t_std.p;
+  a.sf = c.sf.p;
+  a.dh_w = h->dh_w.p;
+  a.species = h->tpl_i.p + h->L.o_species;
+  a.pt = h->pt.p;
+  a.L = h->L;
+  a.judge_stride = c.opt.judge_stride;
+  a.judge_tol = (float)c.opt.judge_tolerance;
+  a.judge_counter = c.judge_counter.p;
+  a.judge_acc = c.judge_acc.p;
+  a.judge_n = c.judge_n.p;
+  a.class_off_w = c.class_off.p;
+  a.judge_err = c.judge_err.p;
+  a.judged = c.judged.p;
+  a.err = h->err.p;
+  return a;
+}
+
+void launch_classify(souffle_gpu_system* h, const FarArgs& a) {
+  const int np = h->tpl.np;
+  k_far_classify<<<h->S, 128, sizeof(int4) * np, h->stream>>>(a);
+  k_far_scan<<<1, 1024, 0, h->stream>>>(a);
+}
+
+// Symmetric eigen-decomposition by cyclic Jacobi rotations: A (n x n, row-major) is destroyed,
+// eigenvalues in w, eigenvectors in the columns of V.
+void jacobi_eigen(std::vector<double>& A, int n, std::vector<double>& w, std::vector<double>& V) {
+  V.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) V[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) {
+        const double v = A[(size_t)i * n + j] * A[(size_t)i * n + j];
+        tot += v;
+        if (i != j) off += v;
+      }
+    if (off <= 1e-26 * tot) break;
+    for (int p = 0; p < n - 1; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double apq = A[(size_t)p * n + q];
+        if (std::fabs(apq) < 1e-300) continue;
+        const double app = A[(size_t)p * n + p], aqq = A[(size_t)q * n + q];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; k++) {  // A <- A R (columns p, q)
+          const double akp = A[(size_t)k * n + p], akq = A[(size_t)k * n + q];
+          A[(size_t)k * n + p] = c * akp - s * akq;
+          A[(size_t)k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; k++) {  // A <- R^T A (rows p, q)
+          const double apk = A[(size_t)p * n + k], aqk = A[(size_t)q * n + k];
+          A[(size_t)p * n + k] = c * apk - s * aqk;
+          A[(size_t)q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; k++) {
+          const double vkp = V[(size_t)k * n + p], vkq = V[(size_t)k * n + q];
+          V[(size_t)k * n + p] = c * vkp - s * vkq;
+          V[(size_t)k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  w.resize(n);
+  for (int i = 0; i < n; i++) w[i] = A[(size_t)i * n + i];
+}
+
+}  // namespace
+
+namespace souffle {
+
+bool surrogate_enabled(const souffle_gpu_system* h) { return h && h->sur && h->sur->enabled; }
+
+void surrogate_classify(souffle_gpu_system* h, PairArgs& pa) {
+  FarArgs a = far_args(h);
+  launch_classify(h, a);
+  pa.cand_far = h->sur->cand_far.p;
+  pa.far_ok = h->sur->far_total.p + 2;
+}
+
+void surrogate_compact(souffle_gpu_system* h) {
+  FarArgs a = far_args(h);
+  k_far_write<<<(h->S + 127) / 128, 128, 0, h->stream>>>(a);
+}
+
+void surrogate_forces(souffle_gpu_system* h, ForceArgs& fa) {
+  SurrogateCtx& c = *h->sur;
+  FarArgs a = far_args(h);
+  const int sb = (h->S + 3) / 4;
+  k_sub_frames<<<sb, 128, 0, h->stream>>>(a);
+  k_far_descr<<<(c.far_cap + 127) / 128, 128, 0, h->stream>>>(a);
+  const float* y = nullptr;
+  int ldy = 0;
+  if (mlp_forward_async(c.net, c.x.p, c.far_cap, c.far_total.p, h->err.p, h->stream, &y, &ldy) != cudaSuccess) {
+    // parameters were validated at attach; a launch failure surfaces through cudaGetLastError
+    return;
+  }
+  c.y = y;
+  c.ldy = ldy;
+  a.y = y;
+  a.ldy = ldy;
+  k_far_apply<<<sb, 128, 0, h->stream>>>(a);
+  fa.surr_f = c.sf.p;
+}
+
+bool surrogate_judge_due(const souffle_gpu_system* h, long long step) {
+  return surrogate_enabled(h) && h->sur->opt.judge_every > 0 && (step + 1) % h->sur->opt.judge_every == 0;
+}
+
+void surrogate_judge(souffle_gpu_system* h) {
+  SurrogateCtx& c = *h->sur;
+  FarArgs a = far_args(h);
+  const int nj = (c.far_cap + c.opt.judge_stride - 1) / c.opt.judge_stride;
+  k_far_judge<<<(nj + 3) / 4, 128, 0, h->stream>>>(a);
+  k_judge_decide<<<1, 32, 0, h->stream>>>(a);
+}
+
+}  // namespace souffle
+
+extern "C" {
+
+souffle_status souffle_surrogate_attach(souffle_gpu_system* h, souffle_mlp* net, const double* rest_pos,
+                                        const souffle_surrogate_options* opt) {
+  if (!h || !net || !rest_pos) return sfail(SOUFFLE_ERR_BAD_INPUT, "null argument");
+  const int np = h->tpl.np;
+  int n_in = 0, n_out = 0, cap = 0;
+  mlp_dims(net, &n_in, &n_out, &cap);
+  if (np > 83 || n_in != kDesc || n_out != 6 + 3 * np)
+    return sfail(SOUFFLE_ERR_BAD_INPUT, "surrogate network must map 64 inputs to 6 + 3 np outputs (np <= 83)");
+  souffle_surrogate_options o{};
+  if (opt) o = *opt;
+  if (o.switch_radius <= 0) o.switch_radius = 3.5;
+  if (o.judge_every <= 0) o.judge_every = 100;
+  if (o.judge_stride <= 0) o.judge_stride = 100;
+  if (o.judge_tolerance <= 0) o.judge_tolerance = 0.2;
+  if (o.far_capacity <= 0) o.far_capacity = std::max(1024, 2 * h->S);
+  if (cap < o.far_capacity) return sfail(SOUFFLE_ERR_BAD_INPUT, "network max_batch is below far_capacity");
+  // body frame of the rest shape: centre bead, the bead farthest from it, the bead farthest
+  // from that axis
+  const int cl = h->prm[0].center_local;
+  std::vector<double> d(3 * np);
+  for (int l = 0; l < np; l++)
+    for (int k = 0; k < 3; k++) d[3 * l + k] = rest_pos[3 * l + k] - rest_pos[3 * cl + k];
+  auto nrm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+  int b1 = 0;
+  for (int l = 0; l < np; l++)
+    if (nrm(&d[3 * l]) > nrm(&d[3 * b1])) b1 = l;
+  double e1[3] = {d[3 * b1], d[3 * b1 + 1], d[3 * b1 + 2]};
+  const double n1 = nrm(e1);
+  if (!(n1 > 1e-9)) return sfail(SOUFFLE_ERR_BAD_INPUT, "degenerate rest shape");
+  for (double& v : e1) v /= n1;
+  auto cross = [](const double* a, const double* b, double* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  int b2 = 0;
+  double best = -1;
+  for (int l = 0; l < np; l++) {
+    double c[3];
+    cross(e1, &d[3 * l], c);
+    if (nrm(c) > best) {
+      best = nrm(c);
+      b2 = l;
+    }
+  }
+  if (!(best > 1e-6)) return sfail(SOUFFLE_ERR_BAD_INPUT, "rest shape is collinear");
+  double e3[3], e2[3];
+  cross(e1, &d[3 * b2], e3);
+  const double n3 = nrm(e3);
+  for (double& v : e3) v /= n3;
+  cross(e3, e1, e2);
+  double m[3] = {0, 0, 0};
+  for (int l = 0; l < np; l++)
+    for (int k = 0; k < 3; k++) m[k] += d[3 * l + k] / np;
+  std::vector<double> body(3 * np);
+  for (int l = 0; l < np; l++) {
+    const double v[3] = {d[3 * l] - m[0], d[3 * l + 1] - m[1], d[3 * l + 2] - m[2]};
+    body[3 * l] = e1[0] * v[0] + e1[1] * v[1] + e1[2] * v[2];
+    body[3 * l + 1] = e2[0] * v[0] + e2[1] * v[1] + e2[2] * v[2];
+    body[3 * l + 2] = e3[0] * v[0] + e3[1] * v[1] + e3[2] * v[2];
+  }
+  // elastic modes: Hessian of the template's spring network (unit stiffness) at the rest shape,
+  // rigid-body motions projected out, lowest 12 remaining eigenvectors
+  const int n = 3 * np;
+  std::vector<double> H((size_t)n * n, 0.0);
+  for (int e = 0; e < h->tpl.ne; e++) {
+    const int i = h->tpl.edge[2 * e], j = h->tpl.edge[2 * e + 1];
+    double u[3] = {body[3 * j] - body[3 * i], body[3 * j + 1] - body[3 * i + 1], body[3 * j + 2] - body[3 * i + 2]};
+    const double len = nrm(u);
+    if (!(len > 1e-12)) continue;
+    for (double& v : u) v /= len;
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) {
+        const double k = u[a] * u[b];
+        H[(size_t)(3 * i + a) * n + 3 * i + b] += k;
+        H[(size_t)(3 * j + a) * n + 3 * j + b] += k;
+        H[(size_t)(3 * i + a) * n + 3 * j + b] -= k;
+        H[(size_t)(3 * j + a) * n + 3 * i + b] -= k;
+      }
+  }
+  std::vector<std::vector<double>> rig;
+  for (int a = 0; a < 3; a++) {
+    std::vector<double> t(n, 0.0);
+    for (int l = 0; l < np; l++) t[3 * l + a] = 1.0;
+    rig.push_back(t);
+  }
+  for (int a = 0; a < 3; a++) {
+    std::vector<double> r(n, 0.0);
+    double ax[3] = {0, 0, 0};
+    ax[a] = 1.0;
+    for (int l = 0; l < np; l++) cross(ax, &body[3 * l], &r[3 * l]);
+    rig.push_back(r);
+  }
+  for (size_t a = 0; a < rig.size(); a++) {  // Gram-Schmidt
+    for (size_t b = 0; b < a; b++) {
+      double dp = 0;
+      for (int k = 0; k < n; k++) dp += rig[a][k] * rig[b][k];
+      for (int k = 0; k < n; k++) rig[a][k] -= dp * rig[b][k];
+    }
+    double nn = 0;
+    for (int k = 0; k < n; k++) nn += rig[a][k] * rig[a][k];
+    nn = std::sqrt(nn);
+    for (int k = 0; k < n; k++) rig[a][k] /= nn;
+  }
+  // H <- P H P, P = I - sum r r^T; rigid motions get eigenvalue 0 and are skipped below
+  std::vector<double> T((size_t)n * n);
+  auto project_rows = [&](std::vector<double>& M) {  // M <- P M
+    for (auto& r : rig)
+      for (int c = 0; c < n; c++) {
+        double dp = 0;
+        for (int k = 0; k < n; k++) dp += r[k] * M[(size_t)k * n + c];
+        for (int k = 0; k < n; k++) M[(size_t)k * n + c] -= dp * r[k];
+      }
+  };
+  project_rows(H);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) T[(size_t)i * n + j] = H[(size_t)j * n + i];
+  project_rows(T);  // (P (P H)^T) = P H P for symmetric H
+  std::vector<double> w, V;
+  jacobi_eigen(T, n, w, V);
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return w[a] < w[b]; });
+  std::vector<float> modes;
+  for (int idx : order) {
+    double in_rigid = 0;
+    for (auto& r : rig) {
+      double dp = 0;
+      for (int k = 0; k < n; k++) dp += r[k] * V[(size_t)k * n + idx];
+      in_rigid += dp * dp;
+    }
+    if (in_rigid > 0.5) continue;
+    for (int k = 0; k < n; k++) modes.push_back((float)V[(size_t)k * n + idx]);
+    if ((int)modes.size() == kModes * n) break;
+  }
+  if ((int)modes.size() != kModes * n) return sfail(SOUFFLE_ERR_BAD_INPUT, "template has fewer than 12 elastic modes");
+
+  SurrogateCtx* c = new SurrogateCtx;
+  auto bail = [&](souffle_status s) {
+    delete c;
+    return s;
+  };
+#define S_TRY_C(x)                                                                                    \
+  do {                                                                                                \
+    cudaError_t e_ = (x);                                                                             \
+    if (e_ != cudaSuccess) return bail(sfail(SOUFFLE_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_))); \
+  } while (0)
+  c->net = net;
+  c->opt = o;
+  c->np = np;
+  c->n_out = n_out;
+  c->far_cap = o.far_capacity;
+  c->anchor1 = b1;
+  c->anchor2 = b2;
+  std::vector<float> restf(body.begin(), body.end());
+  S_TRY_C(cudaSetDevice(h->opt.device));
+  S_TRY_C(c->modes.alloc(modes.size()));
+  S_TRY_C(cudaMemcpy(c->modes.p, modes.data(), modes.size() * 4, cudaMemcpyHostToDevice));
+  S_TRY_C(c->rest.alloc(restf.size()));
+  S_TRY_C(cudaMemcpy(c->rest.p, restf.data(), restf.size() * 4, cudaMemcpyHostToDevice));
+  for (auto* b : {&c->x_mean, &c->x_istd}) S_TRY_C(b->alloc(kDesc));
+  for (auto* b : {&c->t_mean, &c->t_std, &c->t_istd}) S_TRY_C(b->alloc(n_out));
+  S_TRY_C(c->cand_far.alloc((size_t)h->S * h->cand_cap));
+  S_TRY_C(c->cand_dmin.alloc((size_t)h->S * h->cand_cap));
+  S_TRY_C(c->far_count.alloc(h->S));
+  S_TRY_C(c->far_start.alloc(h->S + 1));
+  S_TRY_C(c->far_total.alloc(3));
+  S_TRY_C(cudaMemset(c->far_total.p, 0, 3 * sizeof(int)));
+  S_TRY_C(cudaMemset(c->far_start.p, 0, (h->S + 1) * sizeof(int)));
+  S_TRY_C(c->far_pair.alloc(c->far_cap));
+  S_TRY_C(c->far_dmin.alloc(c->far_cap));
+  S_TRY_C(c->frame.alloc((size_t)h->S * kFrame));
+  S_TRY_C(c->x.alloc((size_t)c->far_cap * kDesc));
+  S_TRY_C(cudaMemset(c->x.p, 0, (size_t)c->far_cap * kDesc * sizeof(float)));
+  S_TRY_C(c->sf.alloc(h->N));
+  S_TRY_C(c->class_off.alloc(kClasses));
+  S_TRY_C(cudaMemset(c->class_off.p, 0, kClasses * sizeof(int)));
+  S_TRY_C(c->judge_n.alloc(kClasses));
+  S_TRY_C(cudaMemset(c->judge_n.p, 0, kClasses * sizeof(int)));
+  S_TRY_C(c->judge_counter.alloc(1));
+  S_TRY_C(cudaMemset(c->judge_counter.p, 0, sizeof(int)));
+  S_TRY_C(c->judge_acc.alloc(2 * kClasses));
+  S_TRY_C(cudaMemset(c->judge_acc.p, 0, 2 * kClasses * sizeof(double)));
+  S_TRY_C(c->judge_err.alloc(kClasses));
+  {
+    const float neg[kClasses] = {-1.f, -1.f, -1.f, -1.f};
+    S_TRY_C(cudaMemcpy(c->judge_err.p, neg, sizeof(neg), cudaMemcpyHostToDevice));
+  }
+  S_TRY_C(c->judged.alloc(1));
+  S_TRY_C(cudaMemset(c->judged.p, 0, sizeof(long long)));
+  // one forward outside any stream capture, so the GEMM kernels' attributes are set up front
+  {
+    int zero = 0;
+    DevBuf<int> m0;
+    S_TRY_C(m0.alloc(1));
+    S_TRY_C(cudaMemcpy(m0.p, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    const float* y;
+    int ldy;
+    S_TRY_C(mlp_forward_async(net, c->x.p, c->far_cap, m0.p, h->err.p, h->stream, &y, &ldy));
+    S_TRY_C(cudaStreamSynchronize(h->stream));
+  }
+#undef S_TRY_C
+  surrogate_free(h->sur);
+  h->sur = c;
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
+  h->graphs.clear();
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_surrogate_collect(souffle_gpu_system* h, float* x_dev, float* t_dev, int32_t capacity,
+                                         int32_t* count) {
+  if (!h || !h->sur || !x_dev || !t_dev || !count || capacity < 0) return sfail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  if (h->sur->enabled) return sfail(SOUFFLE_ERR_STATE, "switch the surrogate off before collecting training data");
+  if (!h->have_state) return sfail(SOUFFLE_ERR_STATE, "no state set");
+  SurrogateCtx& c = *h->sur;
+  S_TRY(cudaSetDevice(h->opt.device));
+  // candidates at the current positions (the pair list itself is untouched)
+  souffle_status s = rebuild_candidates(h);
+  if (s != SOUFFLE_OK) return s;
+  FarArgs a = far_args(h);
+  a.class_off = nullptr;
+  a.x_mean = nullptr;
+  DevBuf<float> targets;
+  S_TRY(targets.alloc((size_t)c.far_cap * c.n_out));
+  a.targets = targets.p;
+  launch_classify(h, a);
+  k_far_write<<<(h->S + 127) / 128, 128, 0, h->stream>>>(a);
+  k_sub_frames<<<(h->S + 3) / 4, 128, 0, h->stream>>>(a);
+  k_far_descr<<<(c.far_cap + 127) / 128, 128, 0, h->stream>>>(a);
+  k_far_targets<<<(c.far_cap + 3) / 4, 128, 0, h->stream>>>(a);
+  S_TRY(cudaGetLastError());
+  int tot[3];
+  S_TRY(cudaMemcpyAsync(tot, c.far_total.p, sizeof(tot), cudaMemcpyDeviceToHost, h->stream));
+  S_TRY(cudaStreamSynchronize(h->stream));
+  const int n = std::min(tot[0], capacity);
+  if (n > 0) {
+    S_TRY(cudaMemcpyAsync(x_dev, c.x.p, sizeof(float) * n * kDesc, cudaMemcpyDeviceToDevice, h->stream));
+    S_TRY(cudaMemcpyAsync(t_dev, targets.p, sizeof(float) * (size_t)n * c.n_out, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  S_TRY(cudaMemsetAsync(c.far_total.p, 0, 3 * sizeof(int), h->stream));  // no stale far list
+  S_TRY(cudaMemsetAsync(c.far_start.p, 0, (h->S + 1) * sizeof(int), h->stream));
+  S_TRY(cudaStreamSynchronize(h->stream));
+  *count = n;
+  return check_status(h);
+}
+
+souffle_status souffle_surrogate_fit(souffle_gpu_system* h, const float* x_dev, const float* t_dev, int32_t n,
+                                     int32_t epochs, int32_t batch, float lr, uint64_t seed, float* final_loss) {
+  if (!h || !h->sur || !x_dev || !t_dev || n < 1 || epochs < 1 || batch < 1 || !(lr > 0))
+    return sfail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  SurrogateCtx& c = *h->sur;
+  int n_in = 0, n_out = 0, cap = 0;
+  mlp_dims(c.net, &n_in, &n_out, &cap);
+  if (batch > cap) return sfail(SOUFFLE_ERR_BAD_INPUT, "batch exceeds the network's max_batch");
+  S_TRY(cudaSetDevice(h->opt.device));
+  cudaStream_t st = h->stream;
+  k_col_stats<<<kDesc, 256, 0, st>>>(x_dev, n, kDesc, c.x_mean.p, c.x_istd.p, nullptr);
+  k_col_stats<<<n_out, 256, 0, st>>>(t_dev, n, n_out, c.t_mean.p, c.t_istd.p, c.t_std.p);
+  S_TRY(cudaGetLastError());
+  // targets are scaled by 1/std (constant columns kept at scale 1)
+  {
+    std::vector<float> sd(n_out), is(n_out);
+    S_TRY(cudaMemcpyAsync(sd.data(), c.t_std.p, n_out * 4, cudaMemcpyDeviceToHost, st));
+    S_TRY(cudaStreamSynchronize(st));
+    for (int k = 0; k < n_out; k++) is[k] = 1.0f / sd[k];
+    S_TRY(cudaMemcpy(c.t_istd.p, is.data(), n_out * 4, cudaMemcpyHostToDevice));
+  }
+  std::vector<int> perm(n);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::mt19937_64 rng(seed);
+  std::shuffle(perm.begin(), perm.end(), rng);
+  DevBuf<int> dperm;
+  DevBuf<float> xn, tn;
+  S_TRY(dperm.alloc(n));
+  S_TRY(xn.alloc((size_t)n * kDesc));
+  S_TRY(tn.alloc((size_t)n * n_out));
+  S_TRY(cudaMemcpy(dperm.p, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  k_normalise_rows<<<(int)(((long long)n * kDesc + 255) / 256), 256, 0, st>>>(x_dev, dperm.p, n, kDesc, c.x_mean.p,
+                                                                              c.x_istd.p, xn.p);
+  k_normalise_rows<<<(int)(((long long)n * n_out + 255) / 256), 256, 0, st>>>(t_dev, dperm.p, n, n_out, c.t_mean.p,
+                                                                              c.t_istd.p, tn.p);
+  S_TRY(cudaGetLastError());
+  S_TRY(cudaStreamSynchronize(st));
+  const int nb = (n + batch - 1) / batch;
+  std::vector<int> order(nb);
+  std::iota(order.begin(), order.end(), 0);
+  double last = 0;
+  for (int ep = 0; ep < epochs; ep++) {
+    std::shuffle(order.begin(), order.end(), rng);
+    double sum = 0;
+    for (int b : order) {
+      const int r0 = b * batch, m = std::min(batch, n - r0);
+      float loss = 0;
+      souffle_status s = souffle_mlp_train_step(c.net, xn.p + (size_t)r0 * kDesc, tn.p + (size_t)r0 * n_out, m, lr, &loss);
+      if (s != SOUFFLE_OK) return s;
+      sum += (double)loss * m;
+    }
+    last = sum / n;
+  }
+  c.have_norm = true;
+  if (final_loss) *final_loss = (float)last;
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_surrogate_enable(souffle_gpu_system* h, int32_t on) {
+  if (!h || !h->sur) return sfail(SOUFFLE_ERR_BAD_INPUT, "no surrogate attached");
+  if (on && !h->sur->have_norm) return sfail(SOUFFLE_ERR_STATE, "the surrogate has not been trained");
+  if ((bool)on != h->sur->enabled) {
+    h->sur->enabled = on != 0;
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
+    h->graphs.clear();
+    S_TRY(cudaMemsetAsync(h->sur->far_total.p, 0, 3 * sizeof(int), h->stream));
+    S_TRY(cudaMemsetAsync(h->sur->far_start.p, 0, (h->S + 1) * sizeof(int), h->stream));
+    S_TRY(cudaStreamSynchronize(h->stream));
+  }
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_surrogate_get_stats(souffle_gpu_system* h, souffle_surrogate_stats* out) {
+  if (!h || !h->sur || !out) return sfail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  SurrogateCtx& c = *h->sur;
+  int tot[3], off[kClasses];
+  float err[kClasses];
+  long long judged = 0;
+  S_TRY(cudaMemcpyAsync(tot, c.far_total.p, sizeof(tot), cudaMemcpyDeviceToHost, h->stream));
+  S_TRY(cudaMemcpyAsync(off, c.class_off.p, sizeof(off), cudaMemcpyDeviceToHost, h->stream));
+  S_TRY(cudaMemcpyAsync(err, c.judge_err.p, sizeof(err), cudaMemcpyDeviceToHost, h->stream));
+  S_TRY(cudaMemcpyAsync(&judged, c.judged.p, sizeof(judged), cudaMemcpyDeviceToHost, h->stream));
+  S_TRY(cudaStreamSynchronize(h->stream));
+  std::memset(out, 0, sizeof(*out));
+  out->enabled = c.enabled ? 1 : 0;
+  out->far_pairs = tot[0];
+  out->far_found = tot[1];
+  for (int k = 0; k < kClasses; k++) {
+    if (off[k]) out->classes_off |= 1 << k;
+    out->last_error[k] = err[k];
+  }
+  out->judged = judged;
+  return SOUFFLE_OK;
+}
+
+}  // extern "C"

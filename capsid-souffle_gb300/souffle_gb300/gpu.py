@@ -31,8 +31,19 @@ EXPORTED = [
     # include/souffle_surrogate.h
     "souffle_mlp_create", "souffle_mlp_destroy", "souffle_mlp_param_count", "souffle_mlp_get_params",
     "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_gradients", "souffle_mlp_train_step",
-    "souffle_gemm_bf16",
+    "souffle_gemm_bf16", "souffle_surrogate_attach", "souffle_surrogate_collect", "souffle_surrogate_fit",
+    "souffle_surrogate_enable", "souffle_surrogate_get_stats",
 ]
+
+
+class SurrogateOptions_(C.Structure):
+    _fields_ = [("switch_radius", C.c_double), ("far_capacity", C.c_int32), ("judge_every", C.c_int32),
+                ("judge_stride", C.c_int32), ("judge_tolerance", C.c_double)]
+
+
+class SurrogateStats_(C.Structure):
+    _fields_ = [("enabled", C.c_int32), ("far_pairs", C.c_int32), ("far_found", C.c_int32),
+                ("classes_off", C.c_int32), ("judged", C.c_int64), ("last_error", C.c_double * 4)]
 
 
 class SouffleError(RuntimeError):
@@ -124,6 +135,12 @@ def load() -> C.CDLL:
     lib.souffle_mlp_gradients.argtypes = [vp, vp, vp, C.c_int32, fp, fp]
     lib.souffle_mlp_train_step.argtypes = [vp, vp, vp, C.c_int32, C.c_float, fp]
     lib.souffle_gemm_bf16.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
+    lib.souffle_surrogate_attach.argtypes = [vp, vp, dp, C.POINTER(SurrogateOptions_)]
+    lib.souffle_surrogate_collect.argtypes = [vp, vp, vp, C.c_int32, C.POINTER(C.c_int32)]
+    lib.souffle_surrogate_fit.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
+                                          C.POINTER(C.c_float)]
+    lib.souffle_surrogate_enable.argtypes = [vp, C.c_int32]
+    lib.souffle_surrogate_get_stats.argtypes = [vp, C.POINTER(SurrogateStats_)]
     for name in EXPORTED:
         if name not in ("souffle_gpu_last_error", "souffle_gpu_num_beads", "souffle_gpu_stream",
                         "souffle_mlp_param_count"):
@@ -313,3 +330,38 @@ class Mlp:
 def gemm_bf16(a_ptr: int, b_ptr: int, m: int, n: int, k: int, c_ptr: int, device: int = 0) -> None:
     """C [m][n] = A [m][k] B [n][k]^T on the tensor cores (device pointers)."""
     _check(load().souffle_gemm_bf16(C.c_void_p(a_ptr), C.c_void_p(b_ptr), m, n, k, C.c_void_p(c_ptr), device))
+
+
+def surrogate_attach(system: "GpuSystem", net: Mlp, rest_pos: np.ndarray, switch_radius: float = 3.5,
+                     far_capacity: int = 0, judge_every: int = 100, judge_stride: int = 100,
+                     judge_tolerance: float = 0.2) -> None:
+    """Attach a trained-or-not network to a system (include/souffle_surrogate.h)."""
+    rp = np.ascontiguousarray(rest_pos, dtype=np.float64).reshape(-1)
+    o = SurrogateOptions_(switch_radius, far_capacity, judge_every, judge_stride, judge_tolerance)
+    _check(load().souffle_surrogate_attach(system.h, net.h, _dp(rp), C.byref(o)))
+    system._surrogate_net = net
+
+
+def surrogate_collect(system: "GpuSystem", x_ptr: int, t_ptr: int, capacity: int) -> int:
+    n = C.c_int32()
+    _check(load().souffle_surrogate_collect(system.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), capacity, C.byref(n)))
+    return int(n.value)
+
+
+def surrogate_fit(system: "GpuSystem", x_ptr: int, t_ptr: int, n: int, epochs: int, batch: int, lr: float,
+                  seed: int = 1) -> float:
+    loss = C.c_float()
+    _check(load().souffle_surrogate_fit(system.h, C.c_void_p(x_ptr), C.c_void_p(t_ptr), n, epochs, batch, lr, seed,
+                                        C.byref(loss)))
+    return float(loss.value)
+
+
+def surrogate_enable(system: "GpuSystem", on: bool) -> None:
+    _check(load().souffle_surrogate_enable(system.h, 1 if on else 0))
+
+
+def surrogate_stats(system: "GpuSystem") -> dict:
+    st = SurrogateStats_()
+    _check(load().souffle_surrogate_get_stats(system.h, C.byref(st)))
+    return {"enabled": bool(st.enabled), "far_pairs": st.far_pairs, "far_found": st.far_found,
+            "classes_off": st.classes_off, "judged": int(st.judged), "last_error": list(st.last_error)}

@@ -49,6 +49,61 @@ souffle_status souffle_mlp_gradients(souffle_mlp* h, const float* x_dev, const f
 souffle_status souffle_mlp_train_step(souffle_mlp* h, const float* x_dev, const float* t_dev, int32_t m, float lr,
                                       float* loss);
 
+/* ---- the surrogate inside a system handle ---------------------------------------------------
+ * A subunit pair (A, B) is "far" when its closest bead pair is at least switch_radius apart; its
+ * whole interaction (Debye-Hueckel tail; no LJ/WCA contact that far out) then comes from the
+ * network instead of the pair list, as forces on A's beads.  Pairs inside the switch radius stay
+ * exact.  Classification happens at every pair-list rebuild.
+ *
+ * Descriptor of (A, B), 64 floats in A's body frame (frame from the template's centre bead and
+ * two anchor beads): relative centre of mass, its length, inverse and screened inverse, the
+ * orientation quaternion of B relative to A, the relative centre of mass seen from B, the 12
+ * lowest elastic-mode amplitudes of A and of B (modes of the template's spring network at its
+ * rest shape), 1/kappa, epsilon, the closest bead distance; zero padding.
+ * Output, 6 + 3 np floats in A's body frame: total force F and torque tau on A, and per-bead
+ * residuals r_i; the force on bead i is F/np + (J^-1 tau) x d_i + r_i, d_i its position relative
+ * to A's centre of mass, J = sum |d|^2 I - d d^T.
+ *
+ * Judge: every judge_every steps one far pair in judge_stride is re-evaluated exactly; pairs are
+ * binned in four classes by closest distance (switch_radius + [0, 0.5), [0.5, 1), [1, 1.5),
+ * [1.5, inf)); a class whose relative RMS force error exceeds judge_tolerance reverts to exact
+ * from the next rebuild on. */
+typedef struct souffle_surrogate_options {
+  double switch_radius;    /* default 3.5 */
+  int32_t far_capacity;    /* most far pairs (0 = max(1024, 2 x subunits)); beyond it all stay exact */
+  int32_t judge_every;     /* default 100 */
+  int32_t judge_stride;    /* default 100 (1 % of the far pairs) */
+  double judge_tolerance;  /* default 0.2 */
+} souffle_surrogate_options;
+
+typedef struct souffle_surrogate_stats {
+  int32_t enabled;
+  int32_t far_pairs;       /* far pairs handled by the network since the last rebuild */
+  int32_t far_found;       /* far pairs found at the last rebuild (> far_pairs on overflow) */
+  int32_t classes_off;     /* bit c set: class c reverted to exact */
+  int64_t judged;          /* pairs re-evaluated so far */
+  double last_error[4];    /* per class: relative RMS error at the last judgement, -1 = none */
+} souffle_surrogate_stats;
+
+/* Attach a network (n_in 64, n_out 6 + 3 np, max_batch >= far_capacity) to a handle whose
+ * template rest shape is rest_pos [np][3]. */
+souffle_status souffle_surrogate_attach(souffle_gpu_system* h, souffle_mlp* net, const double* rest_pos,
+                                        const souffle_surrogate_options* opt);
+/* Training data at the current state (surrogate switched off): classifies the far pairs and
+ * writes, for up to capacity of them, raw descriptors x_dev [.][64] and exact targets
+ * t_dev [.][6 + 3 np]; *count = pairs written. */
+souffle_status souffle_surrogate_collect(souffle_gpu_system* h, float* x_dev, float* t_dev, int32_t capacity,
+                                         int32_t* count);
+/* Normalises the data set (per-feature mean and spread, kept for inference) and trains the
+ * attached network on it with Adam: epochs passes of minibatches of batch rows in a seeded
+ * order.  *final_loss = mean normalised loss of the last epoch. */
+souffle_status souffle_surrogate_fit(souffle_gpu_system* h, const float* x_dev, const float* t_dev, int32_t n,
+                                     int32_t epochs, int32_t batch, float lr, uint64_t seed, float* final_loss);
+/* Switch the trained surrogate into (1) or out of (0) the force path; takes effect from the next
+ * pair-list rebuild (souffle_gpu_forces with rebuild, or the next rebuild step). */
+souffle_status souffle_surrogate_enable(souffle_gpu_system* h, int32_t on);
+souffle_status souffle_surrogate_get_stats(souffle_gpu_system* h, souffle_surrogate_stats* out);
+
 /* Utility: C [m][n] FP32 = A [m][k] * B [n][k]^T with A, B given as FP32 device arrays, rounded to
  * BF16 and multiplied on the tensor cores (FP32 accumulation).  For tests of the GEMM itself. */
 souffle_status souffle_gemm_bf16(const float* a_dev, const float* b_dev, int32_t m, int32_t n, int32_t k,

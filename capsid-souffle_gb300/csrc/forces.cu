@@ -433,6 +433,10 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   }
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // First half-kick and drift with periodic wrap (src/md.cpp:409-414, src/bead.h:72-81,113-117),
 // with the pending centre-of-mass velocity of the previous step subtracted first.  Integer
 // arithmetic only: x += v dt is an exact multiply into the fixed-point box.
@@ -446,6 +450,22 @@ __global__ void __launch_bounds__(256) k_drift(DriftArgs a) {
   const long long* kick_c = a.kick_c + (size_t)w.sys * a.np;
   const int n = w.nsub * a.np;
   const int bead0 = w.sub_begin * a.np;
+  const int half = blockDim.x >> 1;
+  if (a.inter_ids && n <= half && (int)threadIdx.x >= half) {
+    // Idle half of the CTA: bring into L2 what k_forces of this work item reads next step, the
+    // used part of each bead's inter-subunit row and the subunits' intra-pair masks (cold after
+    // anything has evicted L2 since the last step).
+    const int k0 = threadIdx.x - half;
+    for (int t = k0; t < n; t += half) {
+      const int g = bead0 + t;
+      const int cnt = a.inter_count[g];
+      const char* row = reinterpret_cast<const char*>(a.inter_ids + (size_t)g * a.inter_cap);
+      for (int off = 0; off < cnt * 4; off += 128) prefetch_l2(row + off);
+    }
+    const char* mk = reinterpret_cast<const char*>(a.intra_mask + (size_t)bead0 * a.words);
+    for (int off = k0 * 128; off < n * a.words * 4; off += half * 128) prefetch_l2(mk + off);
+    return;
+  }
   for (int t = threadIdx.x; t < n; t += blockDim.x) {
     const int g = bead0 + t;
     const int l = t % a.np;

@@ -1,13 +1,18 @@
-// tcgen05 GEMM: one CTA per 128 x BN output tile, 128 threads.
+// tcgen05 GEMM: one CTA per 128 x BN output tile, 256 threads (8 warps).
 //   warp 0, lane 0  TMA producer: 128 x 64 A and BN x 64 B tiles (128-byte swizzle) into a
 //                   4-stage shared-memory ring, one mbarrier per stage ("full")
 //   warp 1, lane 0  MMA issuer: four K = 16 tcgen05.mma per stage into an FP32 accumulator in
 //                   tensor memory; tcgen05.commit frees the stage ("empty") and, after the last
 //                   stage, signals the epilogue ("accum")
-//   warps 0-3       epilogue: warp w reads accumulator lanes 32w..32w+31 (one output row per
-//                   thread) with tcgen05.ld, applies bias / activation and stores
-// K tails and M/N edges are zero-filled by TMA (out-of-bounds box elements) and masked in the
-// epilogue.  All waits are bounded (umma.cuh); a timeout sets err_bit in the error flag word.
+//   warps 0-7       epilogue: warp w reads accumulator lanes 32 (w % 4) .. + 31 (one output row
+//                   per thread) and half (w / 4) of the columns, 32 at a time (two tcgen05.ld in
+//                   flight, one wait), applies bias / activation, and stores through shared
+//                   memory so that global stores run along the rows
+// The epilogue is the long part of a small GEMM (it is latency-bound per thread), so it gets all
+// eight warps, the activation is a template parameter, and BN = 64 by default spreads a small M
+// over more SMs.  K tails and M/N edges are zero-filled by TMA (out-of-bounds box elements) and
+// masked in the epilogue.  All waits are bounded (umma.cuh); a timeout sets err_bit in the error
+// flag word.
 #include <cudaTypedefs.h>
 
 #include <mutex>
@@ -17,7 +22,9 @@
 
 namespace souffle {
 
-constexpr int kBM = 128, kBK = 64, kStages = 4;
+constexpr int kBM = 128, kBK = 64, kStages = 4, kThreads = 256;
+constexpr int kStageCols = 32;                  // epilogue chunk per warp
+constexpr int kStagePitch = kStageCols + 1;     // conflict-free rows and columns
 
 template <int BN>
 struct GemmTile {
@@ -26,14 +33,18 @@ struct GemmTile {
   static constexpr int kStage = kA + kB;
   static constexpr int kBars = 2 * kStages + 1;
   static constexpr int kSmem = 1024 + kStages * kStage + kBars * 8 + 16;
-  static constexpr int kTmemCols = BN <= 128 ? 128 : 256;
+  static constexpr int kTmemCols = BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+  static constexpr int kEpiBytes = (kThreads / 32) * 2 * 32 * kStagePitch * 4;
   static_assert(kStage % 1024 == 0, "stages stay on 1024-byte boundaries (128-byte swizzle atoms)");
+  static_assert(kEpiBytes <= kStages * kStage, "epilogue staging fits in the freed stages");
+  static_assert(BN % (2 * kStageCols) == 0, "each half of the columns is whole chunks");
 };
 
-__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + expf(-z)); }
+// logistic function with the fast exponential and division (the BF16 outputs carry 8 bits)
+__device__ __forceinline__ float sigmoid_fast(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
-template <int BN>
-__global__ void __launch_bounds__(128, 1)
+template <int BN, int ACT>
+__global__ void __launch_bounds__(kThreads, 1)
     k_gemm_bf16(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmEpi e) {
   using G = GemmTile<BN>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -111,31 +122,54 @@ __global__ void __launch_bounds__(128, 1)
 
   if (mbar_wait(accum, 0)) {
     tc_fence_after();
-    const int row = m0 + warp * 32 + lane;
-    const uint32_t t_row = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int c = 0; c < BN; c += 16) {
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = m0 + quarter * 32 + lane;
+    const uint32_t t_row = tmem + ((uint32_t)(quarter * 32) << 16);
+    // Row-major outputs go through shared memory (the freed pipeline stages): each thread holds
+    // one row, so storing straight from registers would touch 32 sectors per warp store.  A
+    // 32 x 32 tile per warp is written by rows and stored with the lanes along the columns.
+    // Transposed outputs are already coalesced from registers (consecutive lanes = rows).
+    float* st_x = reinterpret_cast<float*>(smem_raw + (base - raw)) + warp * (2 * 32 * kStagePitch);
+    float* st_z = st_x + 32 * kStagePitch;
+    const bool rowmajor = e.out_f32 || e.out_bf16 || e.z_out;
+    for (int c = half * (BN / 2); c < (half + 1) * (BN / 2); c += kStageCols) {
       if (n0 + c >= e.N) break;  // uniform over the warp
-      float v[16];
-      tmem_ld16(t_row + (uint32_t)c, v);
-      if (row >= m_rows || !ok) continue;
+      float v[kStageCols];
+      tmem_ld32(t_row + (uint32_t)c, v);
 #pragma unroll
-      for (int i = 0; i < 16; i++) {
+      for (int i = 0; i < kStageCols; i++) {
         const int n = n0 + c + i;
-        if (n >= e.N) break;
-        float x = v[i];
-        if (e.bias) x += e.bias[n];
-        if (e.act == kActSilu) {
-          if (e.z_out) e.z_out[(size_t)row * e.ldz + n] = x;
-          x = x * sigmoidf_(x);
-        } else if (e.act == kActSiluGrad) {
-          const float z = e.zin[(size_t)row * e.ldzin + n];
-          const float sg = sigmoidf_(z);
-          x *= sg * (1.0f + z * (1.0f - sg));
+        float x = v[i], z = 0.f;
+        if (row < m_rows && n < e.N) {
+          if (e.bias) x += e.bias[n];
+          z = x;
+          if (ACT == kActSilu) {
+            x = x * sigmoid_fast(x);
+          } else if (ACT == kActSiluGrad) {
+            const float zi = e.zin[(size_t)row * e.ldzin + n];
+            const float sg = sigmoid_fast(zi);
+            x *= sg * (1.0f + zi * (1.0f - sg));
+          }
+          if (e.out_bf16_t && ok) e.out_bf16_t[(size_t)n * e.ldt + row] = __float2bfloat16_rn(x);
         }
-        if (e.out_f32) e.out_f32[(size_t)row * e.ldo + n] = x;
-        if (e.out_bf16) e.out_bf16[(size_t)row * e.ld_bf16 + n] = __float2bfloat16_rn(x);
-        if (e.out_bf16_t) e.out_bf16_t[(size_t)n * e.ldt + row] = __float2bfloat16_rn(x);
+        st_x[lane * kStagePitch + i] = x;
+        if (e.z_out) st_z[lane * kStagePitch + i] = z;
       }
+      __syncwarp();
+      if (rowmajor && ok) {
+        const int j = lane, n = n0 + c + lane;
+        if (j < min(kStageCols, e.N - (n0 + c))) {
+          for (int r = 0; r < 32; r++) {
+            const int gr = m0 + quarter * 32 + r;
+            if (gr >= m_rows) break;
+            const float x = st_x[r * kStagePitch + j];
+            if (e.out_f32) e.out_f32[(size_t)gr * e.ldo + n] = x;
+            if (e.out_bf16) e.out_bf16[(size_t)gr * e.ld_bf16 + n] = __float2bfloat16_rn(x);
+            if (e.z_out) e.z_out[(size_t)gr * e.ldz + n] = st_z[r * kStagePitch + j];
+          }
+        }
+      }
+      __syncwarp();
     }
   } else {
     atomicOr(e.err, e.err_bit);
@@ -176,20 +210,30 @@ bool make_map(CUtensorMap* m, const void* p, int rows, int cols, int ld, int box
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int BN>
+template <int BN, int ACT>
 cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, const GemmEpi& e, cudaStream_t st) {
   using G = GemmTile<BN>;
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
   std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::kSmem);
+    attr = cudaFuncSetAttribute(k_gemm_bf16<BN, ACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::kSmem);
   });
   if (attr != cudaSuccess) return attr;
   CUtensorMap ta, tb;
   if (!make_map(&ta, A, e.M, e.K, lda, kBM) || !make_map(&tb, B, e.N, e.K, ldb, BN)) return cudaErrorInvalidValue;
   dim3 grid((e.M + kBM - 1) / kBM, (e.N + BN - 1) / BN);
-  k_gemm_bf16<BN><<<grid, 128, G::kSmem, st>>>(ta, tb, e);
+  k_gemm_bf16<BN, ACT><<<grid, kThreads, G::kSmem, st>>>(ta, tb, e);
   return cudaGetLastError();
+}
+
+template <int BN>
+cudaError_t launch_act(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, const GemmEpi& e,
+                       cudaStream_t st) {
+  switch (e.act) {
+    case kActSilu: return launch<BN, kActSilu>(A, lda, B, ldb, e, st);
+    case kActSiluGrad: return launch<BN, kActSiluGrad>(A, lda, B, ldb, e, st);
+    default: return launch<BN, kActNone>(A, lda, B, ldb, e, st);
+  }
 }
 
 }  // namespace
@@ -200,9 +244,14 @@ cudaError_t gemm_bf16(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, i
       (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15))
     return cudaErrorInvalidValue;
   if ((e.out_f32 && e.ldo < e.N) || (e.out_bf16 && e.ld_bf16 < e.N) || (e.out_bf16_t && e.ldt < e.M) ||
-      (e.z_out && e.ldz < e.N) || (e.act == kActSiluGrad && (!e.zin || e.ldzin < e.N)))
+      (e.z_out && e.ldz < e.N) || (e.act == kActSiluGrad && (!e.zin || e.ldzin < e.N)) ||
+      e.act < kActNone || e.act > kActSiluGrad)
     return cudaErrorInvalidValue;
-  return e.N > 128 ? launch<256>(A, lda, B, ldb, e, stream) : launch<128>(A, lda, B, ldb, e, stream);
+  // 64-column tiles keep small and medium problems spread over the SMs; very tall problems use
+  // 128-column tiles (fewer re-reads of A)
+  const long long tiles64 = (long long)((e.M + kBM - 1) / kBM) * ((e.N + 63) / 64);
+  return (tiles64 > 8 * 152 && e.N > 64) ? launch_act<128>(A, lda, B, ldb, e, stream)
+                                         : launch_act<64>(A, lda, B, ldb, e, stream);
 }
 
 }  // namespace souffle

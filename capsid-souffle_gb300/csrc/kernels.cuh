@@ -92,6 +92,13 @@ struct DriftArgs {
   long long* vx; long long* vy; long long* vz;
   long long* px; long long* py; long long* pz;
   int4* pos32;
+  // pair lists read by k_forces of the same work item, prefetched into L2 by the idle half of
+  // the CTA (null: no prefetch)
+  const int* inter_ids = nullptr;
+  const int* inter_count = nullptr;
+  int inter_cap = 0;
+  const unsigned int* intra_mask = nullptr;
+  int words = 0;
 };
 
 struct StateArgs {

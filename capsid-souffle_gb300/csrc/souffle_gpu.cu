@@ -398,6 +398,11 @@ DriftArgs drift_args(souffle_gpu_system* h) {
   a.py = h->pos_fx.p + N;
   a.pz = h->pos_fx.p + 2 * N;
   a.pos32 = h->pos32.p;
+  a.inter_ids = h->inter_ids.p;
+  a.inter_count = h->inter_count.p;
+  a.inter_cap = h->inter_cap;
+  a.intra_mask = h->intra_mask.p;
+  a.words = h->L.words;
   return a;
 }
 

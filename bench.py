@@ -124,6 +124,7 @@ def bench_replicas(args):
     params = [gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local) for w in reps]
     s = gpu.GpuSystem(reps[0].template, params)
     s.set_state(np.concatenate([w.state.pos for w in reps]), np.concatenate([w.state.vel for w in reps]))
+    tuning = s.autotune(trials=20)
     s.md_begin()
     n = s.n
     B = int(reps[0].opt.B)
@@ -150,7 +151,8 @@ def bench_replicas(args):
         "config": {"workload": f"replicas: {len(reps)} systems of bilayer capsomeres, {sum(sizes)} "
                                f"subunits, {n} beads, subunits per system {min(sizes)}-{max(sizes)}",
                    "l2": "working set larger than L2" if n * 300 > 129e6 else "warm L2, whole windows"},
-        "pairlist_mean_length_sampled": float(np.mean(lens)), "generation_s": gen_s}))
+        "pairlist_mean_length_sampled": float(np.mean(lens)), "generation_s": gen_s,
+        "autotune": tuning}))
 
 
 def _flushed_steps(s, ext, flush, a, k):
@@ -340,6 +342,7 @@ def main():
     p = gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local)
     s = gpu.GpuSystem(w.template, [p])
     s.set_state(w.state.pos, w.state.vel)
+    tuning = s.autotune(trials=20) if not args.profile else None
     s.md_begin()
     if args.profile:
         print(json.dumps(s.md_profile(0, args.steps)))
@@ -452,6 +455,7 @@ def main():
         "config": config,
         "e2e": e2e,
         "gpu_launches": launches,
+        "autotune": tuning,
         "warm_l2_value": warm_value,
         "kernels_ms": {"k_forces": forces_ms, "k_drift": drift_ms, "rebuild": rebuild_ms},
         "pairlist": {"mean_length": n_bar, "max_length": stats["max_length"],

@@ -422,6 +422,47 @@ void launch_step(souffle_gpu_system* h, bool rebuild, bool judge) {
   launch_forces_all(h, 1, false, judge);
 }
 
+
+size_t force_smem_for(const souffle_gpu_system* h, int subs) {
+  const TplLayout& L = h->L;
+  const int np = h->tpl.np;
+  return sizeof(float4) * subs * (L.ne + L.nf + 4 * L.nbend) + (sizeof(int4) + sizeof(float4)) * subs * np +
+         sizeof(long long) * 4 * 32 + sizeof(float) * (np + L.n_float) + sizeof(int) * L.n_int;
+}
+
+// Work items of up to `subs` subunits of one system each (one force-kernel CTA per item, in
+// system order), their partial-sum slots, the force kernel's shared memory, and `threads` threads
+// per CTA.  Cached graphs are dropped (their launch shapes change).
+souffle_status plan_work(souffle_gpu_system* h, int subs, int threads) {
+  const size_t smem = force_smem_for(h, subs);
+  if (smem > 200 * 1024) return fail(SOUFFLE_ERR_BAD_INPUT, "template too large for shared memory");
+  std::vector<WorkItem> work;
+  std::vector<int2> slots;
+  int sub0 = 0;
+  for (int k = 0; k < h->n_sys; k++) {
+    const int n = h->prm[k].n_subunits;
+    const int first = (int)work.size();
+    for (int b = 0; b < n; b += subs) work.push_back(WorkItem{k, sub0 + b, std::min(subs, n - b), (int)work.size()});
+    slots.push_back(make_int2(first, (int)work.size() - first));
+    sub0 += n;
+  }
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(h->d_work.alloc(work.size()));
+  CUDA_TRY(cudaMemcpy(h->d_work.p, work.data(), sizeof(WorkItem) * work.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->d_slots.alloc(slots.size()));
+  CUDA_TRY(cudaMemcpy(h->d_slots.p, slots.data(), sizeof(int2) * slots.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->partial.alloc(4 * work.size()));
+  CUDA_TRY(set_kernel_smem(smem, h->pair_smem));
+  h->work.swap(work);
+  h->slots.swap(slots);
+  h->subs_per_cta = subs;
+  h->threads = threads;
+  h->force_smem = smem;
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
+  h->graphs.clear();
+  return SOUFFLE_OK;
+}
+
 }  // namespace
 
 namespace souffle {
@@ -474,8 +515,13 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   for (int k = 0; k < n_systems; k++) ref_cap = std::max<int>(ref_cap, params[k].nlist_capacity);
   h->inter_cap = h->opt.inter_capacity > 0 ? h->opt.inter_capacity : ref_cap;
   h->cand_cap = h->opt.cand_capacity > 0 ? h->opt.cand_capacity : 128;
-  h->threads = 256;                        // two threads per bead in k_forces
-  h->subs_per_cta = std::max(1, 128 / np);  // up to 128 beads per CTA
+  if (h->opt.threads_per_cta != 0 &&
+      (h->opt.threads_per_cta < 64 || h->opt.threads_per_cta > 256 || h->opt.threads_per_cta % 32))
+    return fail(SOUFFLE_ERR_BAD_INPUT, "threads_per_cta must be 64..256 in steps of 32");
+  if (h->opt.subunits_per_cta < 0 || h->opt.subunits_per_cta > 16)
+    return fail(SOUFFLE_ERR_BAD_INPUT, "subunits_per_cta must be 0..16");
+  h->threads = h->opt.threads_per_cta ? h->opt.threads_per_cta : 256;  // two threads per bead
+  h->subs_per_cta = h->opt.subunits_per_cta ? h->opt.subunits_per_cta : std::max(1, 128 / np);
 
   // per-system constants, cell grids, work items
   int sub0 = 0, cell0 = 0;
@@ -521,12 +567,6 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
     h->sp.push_back(q);
     for (int i = 0; i < p.n_subunits; i++) sub_sys[sub0 + i] = k;
     for (int i = 0; i < p.n_subunits * np; i++) bead_sys[(int64_t)sub0 * np + i] = k;
-    int first_slot = (int)h->work.size();
-    for (int b = 0; b < p.n_subunits; b += h->subs_per_cta) {
-      WorkItem w{k, sub0 + b, std::min(h->subs_per_cta, p.n_subunits - b), (int)h->work.size()};
-      h->work.push_back(w);
-    }
-    h->slots.push_back(make_int2(first_slot, (int)h->work.size() - first_slot));
     sub0 += p.n_subunits;
     cell0 += nc * nc * nc;
   }
@@ -541,10 +581,6 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(cudaMemcpy(h->d_sys.p, h->sp.data(), sizeof(SysParams) * n_systems, cudaMemcpyHostToDevice));
   CUDA_TRY(h->d_state.alloc(n_systems));
   CUDA_TRY(cudaMemset(h->d_state.p, 0, sizeof(SysState) * n_systems));
-  CUDA_TRY(h->d_work.alloc(h->work.size()));
-  CUDA_TRY(cudaMemcpy(h->d_work.p, h->work.data(), sizeof(WorkItem) * h->work.size(), cudaMemcpyHostToDevice));
-  CUDA_TRY(h->d_slots.alloc(n_systems));
-  CUDA_TRY(cudaMemcpy(h->d_slots.p, h->slots.data(), sizeof(int2) * n_systems, cudaMemcpyHostToDevice));
   CUDA_TRY(h->d_sub_sys.alloc(h->S));
   CUDA_TRY(cudaMemcpy(h->d_sub_sys.p, sub_sys.data(), sizeof(int) * h->S, cudaMemcpyHostToDevice));
   CUDA_TRY(h->d_bead_sys.alloc(N));
@@ -555,7 +591,6 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(h->force.alloc(3 * N));
   CUDA_TRY(h->sbforce.alloc(6 * N));
   CUDA_TRY(h->staging.alloc(9 * N));
-  CUDA_TRY(h->partial.alloc(4 * h->work.size()));
   CUDA_TRY(h->kick_c.alloc((size_t)n_systems * np));
   CUDA_TRY(cudaMemset(h->kick_c.p, 0, sizeof(long long) * n_systems * np));
   CUDA_TRY(h->intra_mask.alloc((size_t)h->S * np * L.words));
@@ -576,12 +611,9 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(cudaMemset(h->inter_count.p, 0, sizeof(int) * N));
   CUDA_TRY(cudaMemset(h->force.p, 0, sizeof(long long) * 3 * N));
 
-  h->force_smem = sizeof(float4) * h->subs_per_cta * (L.ne + L.nf + 4 * L.nbend) +
-                  (sizeof(int4) + sizeof(float4)) * h->subs_per_cta * np + sizeof(long long) * 4 * 32 +
-                  sizeof(float) * (np + L.n_float) + sizeof(int) * L.n_int;
   h->pair_smem = np * (3 * sizeof(long long) + sizeof(int4) + sizeof(double) + sizeof(int) + sizeof(float));
-  if (h->force_smem > 200 * 1024) return fail(SOUFFLE_ERR_BAD_INPUT, "template too large for shared memory");
-  CUDA_TRY(set_kernel_smem(h->force_smem, h->pair_smem));
+  s = plan_work(h.get(), h->subs_per_cta, h->threads);
+  if (s != SOUFFLE_OK) return s;
   *out = h.release();
   return SOUFFLE_OK;
 }
@@ -1006,6 +1038,67 @@ souffle_status souffle_gpu_md_scalars(souffle_gpu_system* h, int32_t system, dou
   if (ke) *ke = df_to(S.ke);
   if (xi0) *xi0 = df_to(S.xi[0]);
   if (vcom) *vcom = S.vcom_mag;
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_autotune(souffle_gpu_system* h, int32_t trials, souffle_tuning* out) {
+  if (!h || trials < 1 || trials > 1000) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  if (!h->have_state) return fail(SOUFFLE_ERR_STATE, "no state set");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  const int np = h->tpl.np;
+  const int def_subs = std::max(1, 128 / np), def_threads = 256;
+  // candidate shapes: subunits per CTA x threads per CTA (force kernel: two threads per bead,
+  // any bead count; at most 256 threads)
+  std::vector<std::pair<int, int>> cand;
+  for (int subs : {1, 2, 3, 4, 6, 8})
+    for (int thr : {128, 192, 256}) {
+      if (force_smem_for(h, subs) > 200 * 1024) continue;
+      if (subs * np * 2 > 4 * thr) continue;  // more than two passes per thread pair
+      if (subs * np * 2 < thr / 2) continue;   // most of the CTA idle
+      cand.emplace_back(subs, thr);
+    }
+  if (std::find(cand.begin(), cand.end(), std::make_pair(def_subs, def_threads)) == cand.end())
+    cand.emplace_back(def_subs, def_threads);
+  // a rebuild at the current positions, so every shape sees the same lists
+  launch_rebuild(h);
+  souffle_status s = check_err(h);
+  if (s != SOUFFLE_OK) return s;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  double best = 1e30, def_us = 0;
+  std::pair<int, int> best_shape = cand.front();
+  for (auto& c : cand) {
+    if ((s = plan_work(h, c.first, c.second)) != SOUFFLE_OK) break;
+    for (int k = 0; k < 3; k++) launch_forces_all(h, 0, false);
+    cudaEventRecord(e0, h->stream);
+    for (int k = 0; k < trials; k++) launch_forces_all(h, 0, false);
+    cudaEventRecord(e1, h->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      s = fail(SOUFFLE_ERR_CUDA, "event synchronize failed");
+      break;
+    }
+    if ((s = check_err(h)) != SOUFFLE_OK) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double us = 1e3 * ms / trials;
+    if (c.first == def_subs && c.second == def_threads) def_us = us;
+    if (us < best) {
+      best = us;
+      best_shape = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != SOUFFLE_OK) return s;
+  if ((s = plan_work(h, best_shape.first, best_shape.second)) != SOUFFLE_OK) return s;
+  if (out) {
+    out->subunits_per_cta = best_shape.first;
+    out->threads_per_cta = best_shape.second;
+    out->forces_us = best;
+    out->default_forces_us = def_us;
+    out->candidates = (int)cand.size();
+  }
   return SOUFFLE_OK;
 }
 

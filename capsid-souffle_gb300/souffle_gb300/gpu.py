@@ -27,7 +27,7 @@ EXPORTED = [
     "souffle_gpu_pairlist_stats", "souffle_gpu_energies", "souffle_gpu_kinetic_energy",
     "souffle_gpu_md_begin", "souffle_gpu_md_steps", "souffle_gpu_md_scalars",
     "souffle_gpu_synchronize", "souffle_gpu_last_error", "souffle_gpu_stream",
-    "souffle_gpu_md_profile", "souffle_gpu_kinetic_energy_noalloc",
+    "souffle_gpu_md_profile", "souffle_gpu_kinetic_energy_noalloc", "souffle_gpu_autotune",
     # include/souffle_surrogate.h
     "souffle_mlp_create", "souffle_mlp_destroy", "souffle_mlp_param_count", "souffle_mlp_get_params",
     "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_gradients", "souffle_mlp_train_step",
@@ -73,7 +73,12 @@ class Params_(C.Structure):
 class Options_(C.Structure):
     _fields_ = [("inter_capacity", C.c_int32), ("cand_capacity", C.c_int32),
                 ("compat_quirks", C.c_int32), ("device", C.c_int32),
-                ("threads_per_cta", C.c_int32)]
+                ("threads_per_cta", C.c_int32), ("subunits_per_cta", C.c_int32)]
+
+
+class Tuning_(C.Structure):
+    _fields_ = [("subunits_per_cta", C.c_int32), ("threads_per_cta", C.c_int32), ("forces_us", C.c_double),
+                ("default_forces_us", C.c_double), ("candidates", C.c_int32)]
 
 
 class Energies_(C.Structure):
@@ -123,6 +128,7 @@ def load() -> C.CDLL:
     lib.souffle_gpu_stream.restype = C.c_void_p
     lib.souffle_gpu_stream.argtypes = [vp]
     lib.souffle_gpu_md_profile.argtypes = [vp, C.c_int64, C.c_int32, C.POINTER(KernelTimes_)]
+    lib.souffle_gpu_autotune.argtypes = [vp, C.c_int32, C.POINTER(Tuning_)]
     fp = C.POINTER(C.c_float)
     lib.souffle_mlp_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_int32,
                                        C.POINTER(vp)]
@@ -174,7 +180,8 @@ class GpuSystem:
     """A handle over one or more systems sharing one template."""
 
     def __init__(self, t: Template, params: Sequence[Params_], inter_capacity: int = 0,
-                 cand_capacity: int = 0, quirks: bool = True, device: int = 0):
+                 cand_capacity: int = 0, quirks: bool = True, device: int = 0, threads_per_cta: int = 0,
+                 subunits_per_cta: int = 0):
         self.lib = load()
         self.t = t
         self._arrs = dict(
@@ -195,7 +202,8 @@ class GpuSystem:
                         _ip(a["lj"]) if a["lj"].size else None)
         self.params = list(params)
         arr = (Params_ * len(self.params))(*self.params)
-        opts = Options_(inter_capacity, cand_capacity, 1 if quirks else -1, device, 0)
+        opts = Options_(inter_capacity, cand_capacity, 1 if quirks else -1, device, threads_per_cta,
+                        subunits_per_cta)
         h = C.c_void_p()
         _check(self.lib.souffle_gpu_create(C.byref(tpl), arr, len(self.params), C.byref(opts),
                                            C.byref(h)))
@@ -232,6 +240,12 @@ class GpuSystem:
                                            None if sf is None else _dp(sf),
                                            None if bf is None else _dp(bf)))
         return (tf, sf, bf) if parts else tf
+
+    def autotune(self, trials: int = 20) -> dict:
+        """Measure the force kernel at every candidate CTA shape and keep the fastest."""
+        t = Tuning_()
+        _check(self.lib.souffle_gpu_autotune(self.h, trials, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in Tuning_._fields_}
 
     def pairlist(self, cap: int):
         counts = np.empty(self.n, dtype=np.int32)

@@ -87,7 +87,9 @@ typedef struct souffle_options {
                              reference's stale-distance reuse for subunit 0's centre bead
                              (src/functions.cpp:97); -1 turns it off */
   int32_t device;         /* CUDA device ordinal */
-  int32_t threads_per_cta;/* force-kernel block size (0 = autotuned) */
+  int32_t threads_per_cta;/* force-kernel block size, 64..256 in steps of 32 (0 = default 256;
+                             souffle_gpu_autotune chooses it by measurement) */
+  int32_t subunits_per_cta;/* subunits per force-kernel CTA (0 = default: up to 128 beads) */
 } souffle_options;
 
 typedef struct souffle_energies {
@@ -174,6 +176,18 @@ typedef struct souffle_kernel_times {
 } souffle_kernel_times;
 souffle_status souffle_gpu_md_profile(souffle_gpu_system* h, int64_t first_step, int32_t n_steps,
                                       souffle_kernel_times* out);
+
+/* Autotuner (no reference counterpart): times the force kernel (forces only, no state change) at
+ * every candidate CTA shape -- subunits per CTA and threads per CTA -- over the handle's current
+ * state, keeps the fastest, and reports it.  trials = timed launches per shape.  The chosen shape
+ * can be passed back through souffle_options to skip the search next time. */
+typedef struct souffle_tuning {
+  int32_t subunits_per_cta, threads_per_cta;
+  double forces_us;          /* mean force-kernel time of the chosen shape */
+  double default_forces_us;  /* the same for the default shape */
+  int32_t candidates;        /* shapes measured */
+} souffle_tuning;
+souffle_status souffle_gpu_autotune(souffle_gpu_system* h, int32_t trials, souffle_tuning* out);
 
 /* Kinetic energy and velocity sum of a caller-owned device array, for callers that must not
  * allocate device memory after start-up (a loop that reserves all its GPU memory up front, or a

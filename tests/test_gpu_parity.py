@@ -204,3 +204,37 @@ def test_thermostat_chain_bitwise_equals_host_double_float(tmp_path):
     assert rc == 60
     assert np.array_equal(rows[:, 0], np.array(xis)), np.abs(rows[:, 0] - np.array(xis)).max()
     assert np.abs(np.array(xis)).max() > 0
+
+
+def test_cta_shapes_and_autotuner_give_identical_results():
+    """Every force-kernel CTA shape gives bitwise the same forces and trajectory (sums are exact
+    fixed point); the autotuner keeps the fastest shape it measured."""
+    g = load_golden("bilayer_dense")
+    ref, *_ = _gpu(g)
+    f0 = ref.forces(rebuild=True)
+    ref.md_begin()
+    ref.md_steps(0, 15)
+    p0, v0 = ref.get_state()
+    for subs, thr in [(1, 128), (2, 192), (4, 256), (6, 128)]:
+        s, *_ = _gpu(g, threads_per_cta=thr, subunits_per_cta=subs)
+        assert np.array_equal(s.forces(rebuild=True), f0), (subs, thr)
+        s.md_begin()
+        s.md_steps(0, 15)
+        p, v = s.get_state()
+        assert np.array_equal(p, p0) and np.array_equal(v, v0), (subs, thr)
+    s, *_ = _gpu(g)
+    t = s.autotune(trials=5)
+    assert t["candidates"] >= 3 and 0 < t["forces_us"] <= t["default_forces_us"]
+    assert np.array_equal(s.forces(rebuild=True), f0)
+    s.md_begin()
+    s.md_steps(0, 15)
+    p, v = s.get_state()
+    assert np.array_equal(p, p0) and np.array_equal(v, v0)
+
+
+def test_bad_cta_shape_is_rejected():
+    from souffle_gb300 import gpu
+    g = load_golden("plain_small")
+    with pytest.raises(gpu.SouffleError) as e:
+        _gpu(g, threads_per_cta=100)
+    assert e.value.code == 1

@@ -66,6 +66,20 @@ __global__ void k_energy_bonded(EnergyArgs a) {
     int r = a.tpl_i[L.o_bead_roles + l * L.maxrole + k];
     if (r < 0) break;
     int kb_ = r >> 2;
+    const double beta0 = (double)a.tpl_f[L.o_beta0 + kb_];
+    if (beta0 != 0.0) {  // rest-angle option: kb/4 (1 - cos(beta - beta0)) per quad bead
+      const int* bq = a.tpl_i + L.o_bend + 4 * kb_;
+      double v1[3], v2[3], v3[3];
+      ddiff(a, fx, base + bq[0], base + bq[2], v1[0], v1[1], v1[2]);
+      ddiff(a, fx, base + bq[1], base + bq[0], v2[0], v2[1], v2[2]);
+      ddiff(a, fx, base + bq[3], base + bq[1], v3[0], v3[1], v3[2]);
+      const double m[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+      const double n[3] = {v2[1] * v3[2] - v2[2] * v3[1], v2[2] * v3[0] - v2[0] * v3[2], v2[0] * v3[1] - v2[1] * v3[0]};
+      const double l2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+      const double beta = atan2(-l2 * (v1[0] * n[0] + v1[1] * n[1] + v1[2] * n[2]), -(m[0] * n[0] + m[1] * n[1] + m[2] * n[2]));
+      be += P.kb_d * 0.25 * (1.0 - cos(beta - beta0));
+      continue;
+    }
     double A0[3], A1[3];
     face_area(a, fx, base, bf[2 * kb_], A0);
     face_area(a, fx, base, bf[2 * kb_ + 1], A1);

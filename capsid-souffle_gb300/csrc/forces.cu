@@ -119,6 +119,27 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     const int s = t / nb, k = t - s * nb;
     const int4* sp = s_pos + s * np;
     const int b0 = bq[4 * k], b1 = bq[4 * k + 1], r2 = bq[4 * k + 2], r3 = bq[4 * k + 3];
+    const float beta0 = s_tf[L.o_beta0 + k];
+    if (beta0 != 0.f) {
+      // rest-angle option (no reference counterpart): E = kb (1 - cos(beta - beta0)) with beta
+      // the signed bend angle of (across0, b0, b1, across1); -dE/dx = -kb sin(beta - beta0)
+      // dbeta/dx, dbeta/dx the dihedral gradient (Blondel and Karplus 1996)
+      const int4 Q0 = sp[b0], Q1 = sp[b1], Q2 = sp[r2], Q3 = sp[r3];
+      const float3 v1 = dvec(Q0, Q2, unit), v2 = dvec(Q1, Q0, unit), v3 = dvec(Q3, Q1, unit);
+      const float3 m = cross3(v1, v2), n = cross3(v2, v3);
+      const float l2 = dot3(v2, v2), nv2 = sqrtf(l2);
+      const float beta = atan2f(-nv2 * dot3(v1, n), -dot3(m, n));
+      const float c = -P.kb * sinf(beta - beta0);
+      const float3 ga0 = m * (-nv2 / dot3(m, m)), ga1 = n * (nv2 / dot3(n, n));
+      const float p = dot3(v1, v2) / l2, q = dot3(v3, v2) / l2;
+      const float3 gb0 = ga0 * (-(1.0f + p)) + ga1 * q, gb1 = ga0 * p - ga1 * (1.0f + q);
+      float4* o = s_bend + (size_t)(s * nb + k) * 4;
+      o[0] = make_float4(gb0.x * c, gb0.y * c, gb0.z * c, 0.f);
+      o[1] = make_float4(gb1.x * c, gb1.y * c, gb1.z * c, 0.f);
+      o[2] = make_float4(ga0.x * c, ga0.y * c, ga0.z * c, 0.f);
+      o[3] = make_float4(ga1.x * c, ga1.y * c, ga1.z * c, 0.f);
+      continue;
+    }
     const float4 F0 = s_face[s * nf + bf[2 * k]], F1 = s_face[s * nf + bf[2 * k + 1]];
     const float a0 = F0.w, a1 = F1.w;
     const float S = 4.0f * fabsf(F0.x * F1.x + F0.y * F1.y + F0.z * F1.z);

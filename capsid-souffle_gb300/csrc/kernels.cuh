@@ -120,6 +120,7 @@ struct StateArgs {
 struct EnergyArgs {
   TplLayout L;
   const int* tpl_i;
+  const float* tpl_f;
   const SysParams* sys;
   const SysState* state;
   const long long* px; const long long* py; const long long* pz;

@@ -46,6 +46,7 @@ struct TplLayout {
   int o_q;            // [np]
   int o_sigma;        // [np]
   int o_mass;         // [np]
+  int o_beta0;        // [nbend] rest bend angle per bending edge (0 = no rest angle)
   int n_float;
   int nspecies;
   int lj_att_bits[kMaxSpecies];  // bit js of row is: (species is -> js) attractive

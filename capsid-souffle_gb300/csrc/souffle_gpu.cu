@@ -48,6 +48,30 @@ namespace {
       return fail(SOUFFLE_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));     \
   } while (0)
 
+// Signed bend angle of the quad (a0, b0, b1, a1) in positions x [.][3]: the dihedral about b0 -> b1
+// shifted so that a flat quad is 0, beta = atan2(-|v2| v1 . n, -m . n) with v1 = x_b0 - x_a0,
+// v2 = x_b1 - x_b0, v3 = x_a1 - x_b1, m = v1 x v2, n = v2 x v3.
+double bend_angle(const double* x, int b0, int b1, int a0, int a1) {
+  double v1[3], v2[3], v3[3], m[3], n[3];
+  for (int k = 0; k < 3; k++) {
+    v1[k] = x[3 * b0 + k] - x[3 * a0 + k];
+    v2[k] = x[3 * b1 + k] - x[3 * b0 + k];
+    v3[k] = x[3 * a1 + k] - x[3 * b1 + k];
+  }
+  auto cross = [](const double* a, const double* b, double* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  cross(v1, v2, m);
+  cross(v2, v3, n);
+  const double l2 = std::sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  const double y = l2 * (v1[0] * n[0] + v1[1] * n[1] + v1[2] * n[2]);
+  const double xx = m[0] * n[0] + m[1] * n[1] + m[2] * n[2];
+  const double b = std::atan2(-y, -xx);
+  return std::fabs(b) < 1e-12 ? 0.0 : b;
+}
+
 souffle_status derive_template(const souffle_template* t, HostTemplate& h) {
   if (!t || t->np <= 0 || t->np > kMaxNp || t->ne < 0 || t->nf < 0 || t->n_lj < 0)
     return fail(SOUFFLE_ERR_BAD_INPUT, "template sizes out of range (np must be 1..256)");
@@ -113,6 +137,7 @@ souffle_status derive_template(const souffle_template* t, HostTemplate& h) {
     h.bend_edge.push_back(e);
     h.bend.insert(h.bend.end(), {b0, b1, r2, r3});
     h.bendf.insert(h.bendf.end(), {h.edge_f0[e], h.edge_f1[e]});
+    h.beta0.push_back(t->bend_rest_pos ? bend_angle(t->bend_rest_pos, b0, b1, r2, r3) : 0.0);
   }
   // BEAD::itsE order = template edge order (src/initialize.cpp:328-329)
   std::vector<std::vector<int>> be(h.np), br(h.np);
@@ -193,6 +218,8 @@ souffle_status upload(souffle_gpu_system* h) {
   for (double v : T.sigma) tf.push_back((float)v);
   L.o_mass = (int)tf.size();
   for (double v : T.mass) tf.push_back((float)v);
+  L.o_beta0 = (int)tf.size();
+  for (double v : T.beta0) tf.push_back((float)v);
   while (tf.size() % 4) tf.push_back(0.f);
   L.n_float = (int)tf.size();
   L.nspecies = T.nspecies;
@@ -820,6 +847,7 @@ souffle_status souffle_gpu_energies(souffle_gpu_system* h, int32_t system, souff
   EnergyArgs a{};
   a.L = h->L;
   a.tpl_i = h->tpl_i.p;
+  a.tpl_f = h->tpl_f.p;
   a.sys = h->d_sys.p;
   a.state = h->d_state.p;
   const int64_t N = h->N;

@@ -30,6 +30,7 @@ struct HostTemplate {
   std::vector<int> sp_type;
   int maxdeg = 1, maxrole = 1;
   std::vector<int> bead_edges, bead_roles;
+  std::vector<double> beta0;           // [nb] rest bend angle (0: the reference's bending)
 };
 
 }  // namespace souffle

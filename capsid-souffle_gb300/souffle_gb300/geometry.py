@@ -23,13 +23,16 @@ rim beads -0.5 e.  Interior in-layer edges (shared by two faces of the same
 layer) are bending edges (type 1), all others type 0.  The reference bending
 energy has no rest angle (src/edge.cpp:51-67), so a curvature radius only
 shapes the initial template: beads are lifted onto a sphere of that radius and
-every edge's rest length is its template chord length.
+every edge's rest length is its template chord length.  ``with_rest_dihedral``
+makes that curved shape the bending rest shape as well (every bending edge then
+relaxes to its dihedral there): an option of this package, which the reference
+does not have.
 """
 from __future__ import annotations
 
 import dataclasses
 import math
-from typing import List, Sequence, Tuple
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -49,6 +52,7 @@ class Template:
     faces: np.ndarray          # (nf, 3) int
     lj_attract: List[Tuple[int, int]]  # directed (type_i, type_j) rows
     name: str = "template"
+    bend_rest: Optional[np.ndarray] = None  # (np, 3) bending rest shape; None = no rest angle
 
     @property
     def n_beads(self) -> int:
@@ -164,6 +168,11 @@ def bilayer_n5(curvature_radius: float = 6.0, gap: float = 0.5) -> Template:
     return Template(allpts, types, charge, np.ones(n), np.ones(n), e,
                     np.array(etype, dtype=np.int64), len0,
                     np.array(flist, dtype=np.int64), [(2, 2)], name="bilayer_n5")
+
+
+def with_rest_dihedral(t: Template) -> Template:
+    """A copy of ``t`` whose bending edges relax to the dihedrals of its own (curved) shape."""
+    return dataclasses.replace(t, bend_rest=t.pos.copy(), name=t.name + "_rest")
 
 
 def template_by_name(name: str, curvature_radius: float = 6.0) -> Template:

@@ -58,7 +58,7 @@ class Template_(C.Structure):
                 ("bead_sigma", C.POINTER(C.c_double)), ("bead_mass", C.POINTER(C.c_double)),
                 ("edge_beads", C.POINTER(C.c_int32)), ("edge_type", C.POINTER(C.c_int32)),
                 ("edge_len0", C.POINTER(C.c_double)), ("face_beads", C.POINTER(C.c_int32)),
-                ("lj_types", C.POINTER(C.c_int32))]
+                ("lj_types", C.POINTER(C.c_int32)), ("bend_rest_pos", C.POINTER(C.c_double))]
 
 
 class Params_(C.Structure):
@@ -196,10 +196,13 @@ class GpuSystem:
             lj=np.ascontiguousarray(np.array(t.lj_attract, dtype=np.int32).reshape(-1)),
         )
         a = self._arrs
+        if t.bend_rest is not None:
+            a["rest"] = np.ascontiguousarray(t.bend_rest, dtype=np.float64).reshape(-1)
         tpl = Template_(t.n_beads, len(t.edges), len(t.faces), len(t.lj_attract), _ip(a["type"]),
                         _dp(a["q"]), _dp(a["sig"]), _dp(a["m"]), _ip(a["eb"]), _ip(a["et"]),
                         _dp(a["l0"]), _ip(a["fb"]),
-                        _ip(a["lj"]) if a["lj"].size else None)
+                        _ip(a["lj"]) if a["lj"].size else None,
+                        _dp(a["rest"]) if t.bend_rest is not None else None)
         self.params = list(params)
         arr = (Params_ * len(self.params))(*self.params)
         opts = Options_(inter_capacity, cand_capacity, 1 if quirks else -1, device, threads_per_cta,

@@ -55,6 +55,11 @@ typedef struct souffle_template {
   const double* edge_len0;    /* [ne] */
   const int32_t* face_beads;  /* [3*nf] */
   const int32_t* lj_types;    /* [2*n_lj] (type of bead i, type of neighbour j) */
+  /* Optional, no reference counterpart (the reference's bending has no rest angle,
+   * src/edge.cpp:51-67): a rest shape [np][3].  When given, every bending edge relaxes to its
+   * signed bend angle beta0 in that shape, E = kb (1 - cos(beta - beta0)); NULL (or a flat
+   * shape) gives the reference's kb (1 - |n0 . n1|) exactly. */
+  const double* bend_rest_pos;
 } souffle_template;
 
 /* Per-system parameters in reduced units, as run_simulation derives them

@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   const long long* kick_c = a.kick_c + (size_t)w.sys * np;
   long long ke_acc = 0, px_acc = 0, py_acc = 0, pz_acc = 0;
   const int h = threadIdx.x & 1;
+  const bool bd = P.brownian && a.mode == 1;  // Brownian MD step
   const unsigned int parity = h ? 0xAAAAAAAAu : 0x55555555u;
   const int half = blockDim.x >> 1;
 
@@ -315,6 +316,14 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     Fx += __shfl_xor_sync(0xffffffffu, Fx, 1);
     Fy += __shfl_xor_sync(0xffffffffu, Fy, 1);
     Fz += __shfl_xor_sync(0xffffffffu, Fz, 1);
+    if (act && h == 0 && bd) {
+      // Brownian: tforce + (fran - mean fran over the system) + fdrag (src/md.cpp:468-494,
+      // src/bead.h:147-149)
+      const long long N = a.n_beads_total;
+      Fx += a.fran[g] - __double2ll_rn((double)st.fran_sum[0] * st.inv_n) + a.fdrag[g];
+      Fy += a.fran[N + g] - __double2ll_rn((double)st.fran_sum[1] * st.inv_n) + a.fdrag[N + g];
+      Fz += a.fran[2 * N + g] - __double2ll_rn((double)st.fran_sum[2] * st.inv_n) + a.fdrag[2 * N + g];
+    }
     if (act && h == 0) {
       a.fx[g] = Fx;
       a.fy[g] = Fy;
@@ -420,6 +429,10 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       S.done = 0;
       S.ke = df_from_fixed(k, 2.3283064365386963e-10f);  // 2^-32
       if (a.mode == 1) S.steps += 1;
+      if (P.brownian && a.mode == 1) {  // this step's draws are used: next step's generator state
+        S.fran_sum[0] = S.fran_sum[1] = S.fran_sum[2] = 0;
+        S.lcg = lcg_mul(S.lcg, P.lcg_step);
+      }
     }
     __syncwarp();
     if (a.mode == 1) nhc_forward_warp(S, lane);
@@ -454,6 +467,29 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   }
 }
 
+// Half-kick and drift of one bead (src/md.cpp:409-414, src/bead.h:72-81,113-117), with the
+// pending centre-of-mass velocity subtracted first; integer arithmetic only (x += v dt is an
+// exact multiply into the fixed-point box).
+__device__ __forceinline__ void drift_bead(int g, int l, long long c, long long delta_fx, long long vcx, long long vcy,
+                                           long long vcz, long long dx_fx, const long long* fx, const long long* fy,
+                                           const long long* fz, long long* vxp, long long* vyp, long long* vzp,
+                                           long long* px, long long* py, long long* pz, int4* pos32) {
+  long long vx = vxp[g] - vcx, vy = vyp[g] - vcy, vz = vzp[g] - vcz;
+  vx = vx - mul_shr(vx, delta_fx, 62) + mul_shr(fx[g], c, 56);
+  vy = vy - mul_shr(vy, delta_fx, 62) + mul_shr(fy[g], c, 56);
+  vz = vz - mul_shr(vz, delta_fx, 62) + mul_shr(fz[g], c, 56);
+  vxp[g] = vx;
+  vyp[g] = vy;
+  vzp[g] = vz;
+  const long long X = (long long)((unsigned long long)px[g] + (unsigned long long)mul_shr(vx, dx_fx, 40));
+  const long long Y = (long long)((unsigned long long)py[g] + (unsigned long long)mul_shr(vy, dx_fx, 40));
+  const long long Z = (long long)((unsigned long long)pz[g] + (unsigned long long)mul_shr(vz, dx_fx, 40));
+  px[g] = X;
+  py[g] = Y;
+  pz[g] = Z;
+  pos32[g] = make_int4(hi_word(X), hi_word(Y), hi_word(Z), l);
+}
+
 __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
@@ -464,7 +500,7 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
 __global__ void __launch_bounds__(256) k_drift(DriftArgs a) {
   const WorkItem w = a.work[blockIdx.x];
   const SysParams& P = a.sys[w.sys];
-  const SysState& S = a.state[w.sys];
+  SysState& S = a.state[w.sys];
   const long long delta_fx = S.delta_fx;
   const long long vcx = S.vcom_fx[0], vcy = S.vcom_fx[1], vcz = S.vcom_fx[2];
   const long long dx_fx = P.drift_fx;
@@ -472,6 +508,47 @@ __global__ void __launch_bounds__(256) k_drift(DriftArgs a) {
   const int n = w.nsub * a.np;
   const int bead0 = w.sub_begin * a.np;
   const int half = blockDim.x >> 1;
+  if (P.brownian) {
+    // Brownian step, first half (src/md.cpp:415-421): drag -m v / damp from the velocity after
+    // the last centre-of-mass removal, half-kick with the stored total force, drift; then this
+    // step's random forces (src/md.cpp:461-467): bead k of the system takes draws 6k+1 .. 6k+6
+    // of the generator after the previous steps' draws (x, y, z: two draws each)
+    const long long N = a.n_total;
+    long long sx = 0, sy = 0, sz = 0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      const int g = bead0 + t, l = t % a.np;
+      const long long dc = a.bd_drag[(size_t)w.sys * a.np + l];
+      const long long vx = a.vx[g] - vcx, vy = a.vy[g] - vcy, vz = a.vz[g] - vcz;
+      a.fdrag[g] = -mul_shr(vx, dc, 48);
+      a.fdrag[N + g] = -mul_shr(vy, dc, 48);
+      a.fdrag[2 * N + g] = -mul_shr(vz, dc, 48);
+      drift_bead(g, l, kick_c[l], 0, vcx, vcy, vcz, dx_fx, a.fx, a.fy, a.fz, a.vx, a.vy, a.vz, a.px, a.py, a.pz,
+                 a.pos32);
+      unsigned int x = lcg_mul(S.lcg, a.lcg_table[g - P.bead0]);
+      unsigned int d[6];
+#pragma unroll
+      for (int k = 0; k < 6; k++) d[k] = x = lcg_mul(x, 16807u);
+      const double sc = a.bd_noise[(size_t)w.sys * a.np + l];
+      const long long rx = __double2ll_rn(__dmul_rn(sc, lcg_uniform_half(d[0], d[1])) * 4294967296.0);
+      const long long ry = __double2ll_rn(__dmul_rn(sc, lcg_uniform_half(d[2], d[3])) * 4294967296.0);
+      const long long rz = __double2ll_rn(__dmul_rn(sc, lcg_uniform_half(d[4], d[5])) * 4294967296.0);
+      a.fran[g] = rx;
+      a.fran[N + g] = ry;
+      a.fran[2 * N + g] = rz;
+      sx += rx;
+      sy += ry;
+      sz += rz;
+    }
+    sx = warp_sum_ll(sx);
+    sy = warp_sum_ll(sy);
+    sz = warp_sum_ll(sz);
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(reinterpret_cast<unsigned long long*>(&S.fran_sum[0]), (unsigned long long)sx);
+      atomicAdd(reinterpret_cast<unsigned long long*>(&S.fran_sum[1]), (unsigned long long)sy);
+      atomicAdd(reinterpret_cast<unsigned long long*>(&S.fran_sum[2]), (unsigned long long)sz);
+    }
+    return;
+  }
   if (a.inter_ids && n <= half && (int)threadIdx.x >= half) {
     // Idle half of the CTA: bring into L2 what k_forces of this work item reads next step, the
     // used part of each bead's inter-subunit row and the subunits' intra-pair masks (cold after
@@ -488,23 +565,9 @@ __global__ void __launch_bounds__(256) k_drift(DriftArgs a) {
     return;
   }
   for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const int g = bead0 + t;
     const int l = t % a.np;
-    const long long c = kick_c[l];
-    long long vx = a.vx[g] - vcx, vy = a.vy[g] - vcy, vz = a.vz[g] - vcz;
-    vx = vx - mul_shr(vx, delta_fx, 62) + mul_shr(a.fx[g], c, 56);
-    vy = vy - mul_shr(vy, delta_fx, 62) + mul_shr(a.fy[g], c, 56);
-    vz = vz - mul_shr(vz, delta_fx, 62) + mul_shr(a.fz[g], c, 56);
-    a.vx[g] = vx;
-    a.vy[g] = vy;
-    a.vz[g] = vz;
-    const long long X = (long long)((unsigned long long)a.px[g] + (unsigned long long)mul_shr(vx, dx_fx, 40));
-    const long long Y = (long long)((unsigned long long)a.py[g] + (unsigned long long)mul_shr(vy, dx_fx, 40));
-    const long long Z = (long long)((unsigned long long)a.pz[g] + (unsigned long long)mul_shr(vz, dx_fx, 40));
-    a.px[g] = X;
-    a.py[g] = Y;
-    a.pz[g] = Z;
-    a.pos32[g] = make_int4(hi_word(X), hi_word(Y), hi_word(Z), l);
+    drift_bead(bead0 + t, l, kick_c[l], delta_fx, vcx, vcy, vcz, dx_fx, a.fx, a.fy, a.fz, a.vx, a.vy, a.vz, a.px, a.py,
+               a.pz, a.pos32);
   }
 }
 

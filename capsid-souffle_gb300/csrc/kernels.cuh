@@ -65,6 +65,8 @@ struct ForceArgs {
   const unsigned int* intra_mask;
   const int* inter_ids;      // [N][inter_cap] row-major, ascending
   const float4* surr_f = nullptr;  // [N] far-field forces from the surrogate, or null
+  const long long* fdrag = nullptr;  // Brownian: [3][N] drag and random force of the step
+  const long long* fran = nullptr;
   const int* inter_count;
   int inter_cap;
   const float* dh_w;         // [n_sys * np] q * exp(kappa sigma/2)/(1 + kappa sigma/2) * sqrt(lb)
@@ -84,7 +86,7 @@ struct ForceArgs {
 
 struct DriftArgs {
   const SysParams* sys;
-  const SysState* state;
+  SysState* state;
   const WorkItem* work;
   const long long* kick_c;
   int np;
@@ -99,6 +101,15 @@ struct DriftArgs {
   int inter_cap = 0;
   const unsigned int* intra_mask = nullptr;
   int words = 0;
+  // Brownian systems (src/md.cpp:415-431, 461-501): drag m/damp (2^40 units) and noise scale
+  // sqrt(24 m / (damp dt)) per system and template bead, the minstd_rand0 skip-ahead table
+  // 16807^(6k) mod (2^31 - 1) by system-local bead k, and the step's drag and noise (2^-32)
+  const long long* bd_drag = nullptr;
+  const double* bd_noise = nullptr;
+  const unsigned int* lcg_table = nullptr;
+  long long* fdrag = nullptr;  // [3][N]
+  long long* fran = nullptr;   // [3][N]
+  long long n_total = 0;
 };
 
 struct StateArgs {

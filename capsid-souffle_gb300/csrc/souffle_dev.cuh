@@ -74,6 +74,8 @@ struct SysParams {
   double dt;
   double ks_d, kb_d;        // double copies for the FP64 energy pass
   long long drift_fx;       // dt 2^32 / L in 2^-40 units: x_fixed += v_fixed * drift_fx >> 40
+  int brownian;             // Brownian dynamics (src/md.cpp:415-431, 461-501) instead of the NHC
+  unsigned int lcg_step;    // Brownian noise: 16807^(6 n_beads) mod (2^31 - 1), one step of draws
 };
 
 // Thermostat chain and step scalars of one system, updated on the device.
@@ -102,6 +104,8 @@ struct __align__(16) SysState {
   double vcom_mag;       // |mean velocity| removed at the last step (src/md.cpp:623)
   unsigned int done;     // arrival counter for the last-block reduction
   unsigned int steps;    // MD steps completed since md_begin
+  long long fran_sum[3]; // Brownian: sum of this step's random forces (2^-32 units)
+  unsigned int lcg;      // Brownian: minstd_rand0 state before this step's draws
 };
 
 // Work item: a run of subunits of one system handled by one CTA.
@@ -254,6 +258,34 @@ __host__ __device__ inline double expm1_small(double x) {
   if (x >= -0.0625 && x <= 0.0625) return x * expm1_over_x_series(x);
   if (x >= -0.34657359027997264 && x <= 0.34657359027997264) return x * expm1_over_r_s13(x);
   return exp_reduced(x) - 1.0;
+}
+
+// ---- the reference's Brownian noise: std::default_random_engine = minstd_rand0 -------------
+constexpr unsigned long long kLcgMod = 2147483647ull;  // 2^31 - 1
+constexpr unsigned int kLcgSeed = 69521u;              // src/md.cpp:382
+
+__host__ __device__ inline unsigned int lcg_mul(unsigned int x, unsigned int m) {
+  return (unsigned int)(((unsigned long long)x * m) % kLcgMod);
+}
+
+// std::uniform_real_distribution<double>(-0.5, 0.5) on minstd_rand0 as libstdc++ evaluates it:
+// generate_canonical<double, 53> takes two draws g1, g2 and returns
+// ((g1 - 1) + (g2 - 1) r) / r^2 with r = 2^31 - 2, every operation rounded in double (r^2 is
+// exact before its rounding), a result >= 1 replaced by the largest double below 1; then
+// u * (0.5 - -0.5) + -0.5.
+__host__ __device__ inline double lcg_uniform_half(unsigned int g1, unsigned int g2) {
+  const double r = 2147483646.0;
+#ifdef __CUDA_ARCH__
+  const double sum = __dadd_rn((double)(g1 - 1u), __dmul_rn((double)(g2 - 1u), r));
+  double u = __ddiv_rn(sum, __dmul_rn(r, r));
+#else
+  volatile double prod = (double)(g2 - 1u) * r;
+  volatile double sum = (double)(g1 - 1u) + prod;
+  volatile double r2 = r * r;
+  double u = sum / r2;
+#endif
+  if (u >= 1.0) u = 0.99999999999999988898;  // nextafter(1, 0)
+  return u - 0.5;
 }
 
 // Velocities are int64 in units of 2^-40 (resolution 9.1e-13, range +-8.4e6 in LJ units).

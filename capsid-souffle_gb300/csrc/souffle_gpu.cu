@@ -402,6 +402,8 @@ ForceArgs force_args(souffle_gpu_system* h, int mode, bool want_parts) {
   a.partial = h->partial.p;
   a.err = h->err.p;
   a.n_beads_total = (int)N;
+  a.fdrag = h->bd_fdrag.p;
+  a.fran = h->bd_fran.p;
   a.max_sub = h->subs_per_cta;
   a.mode = mode;
   return a;
@@ -430,6 +432,12 @@ DriftArgs drift_args(souffle_gpu_system* h) {
   a.inter_cap = h->inter_cap;
   a.intra_mask = h->intra_mask.p;
   a.words = h->L.words;
+  a.bd_drag = h->bd_drag.p;
+  a.bd_noise = h->bd_noise.p;
+  a.lcg_table = h->lcg_table.p;
+  a.fdrag = h->bd_fdrag.p;
+  a.fran = h->bd_fran.p;
+  a.n_total = N;
   return a;
 }
 
@@ -588,6 +596,8 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
     if (!(dx < 8388608.0))
       return fail(SOUFFLE_ERR_BAD_INPUT, "time step too large for the box (dt 2^24 / L >= 2^23)");
     q.drift_fx = (long long)std::llrint(dx * 1099511627776.0);
+    q.brownian = p.brownian ? 1 : 0;
+    if (p.brownian && !(p.damp > 0)) return fail(SOUFFLE_ERR_BAD_INPUT, "Brownian dynamics needs damp > 0");
     for (int i = 0; i < np; i++)
       if (!(0.5 * p.dt * 1.5 / tpl->bead_mass[i] < 0.45))  // kick coefficient below 0.49 * 2^64
         return fail(SOUFFLE_ERR_BAD_INPUT, "dt / (2 m) too large for the fixed-point kick");
@@ -633,6 +643,42 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(h->cell_subs.alloc(h->S));
   CUDA_TRY(h->err.alloc(1));
   CUDA_TRY(cudaMemset(h->err.p, 0, sizeof(unsigned int)));
+  // Brownian systems (src/md.cpp:415-431, 461-501): drag m / damp and noise scale
+  // sqrt(24 m / (damp dt)) per template bead, and minstd_rand0 skip-ahead multipliers
+  for (int k = 0; k < n_systems; k++) h->any_brownian = h->any_brownian || params[k].brownian;
+  if (h->any_brownian) {
+    std::vector<long long> drag((size_t)n_systems * np, 0);
+    std::vector<double> noise((size_t)n_systems * np, 0.0);
+    int max_n = 0;
+    for (int k = 0; k < n_systems; k++) {
+      const souffle_params& p = params[k];
+      max_n = std::max(max_n, p.n_subunits * np);
+      if (!p.brownian) continue;
+      for (int l = 0; l < np; l++) {
+        const double m = tpl->bead_mass[l];
+        drag[(size_t)k * np + l] = std::llrint(m / p.damp * 1099511627776.0);  // 2^40
+        noise[(size_t)k * np + l] = std::sqrt((m * 24.0) / (p.damp * p.dt));
+      }
+    }
+    // table[k] = 16807^(6k) mod (2^31 - 1); one step of a system of n beads advances by table[n]
+    std::vector<unsigned int> table(max_n + 1);
+    unsigned int m6 = 1;
+    for (int k = 0; k < 6; k++) m6 = lcg_mul(m6, 16807u);
+    table[0] = 1;
+    for (int k = 1; k <= max_n; k++) table[k] = lcg_mul(table[k - 1], m6);
+    for (int k = 0; k < n_systems; k++) h->sp[k].lcg_step = table[params[k].n_subunits * np];
+    CUDA_TRY(cudaMemcpy(h->d_sys.p, h->sp.data(), sizeof(SysParams) * n_systems, cudaMemcpyHostToDevice));
+    CUDA_TRY(h->bd_drag.alloc(drag.size()));
+    CUDA_TRY(cudaMemcpy(h->bd_drag.p, drag.data(), drag.size() * sizeof(long long), cudaMemcpyHostToDevice));
+    CUDA_TRY(h->bd_noise.alloc(noise.size()));
+    CUDA_TRY(cudaMemcpy(h->bd_noise.p, noise.data(), noise.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(h->lcg_table.alloc(table.size()));
+    CUDA_TRY(cudaMemcpy(h->lcg_table.p, table.data(), table.size() * sizeof(unsigned int), cudaMemcpyHostToDevice));
+    CUDA_TRY(h->bd_fdrag.alloc(3 * N));
+    CUDA_TRY(h->bd_fran.alloc(3 * N));
+    CUDA_TRY(cudaMemset(h->bd_fdrag.p, 0, sizeof(long long) * 3 * N));
+    CUDA_TRY(cudaMemset(h->bd_fran.p, 0, sizeof(long long) * 3 * N));
+  }
   CUDA_TRY(h->e_tot.alloc(8));
   CUDA_TRY(cudaMemset(h->intra_mask.p, 0, sizeof(unsigned int) * (size_t)h->S * np * L.words));
   CUDA_TRY(cudaMemset(h->inter_count.p, 0, sizeof(int) * N));
@@ -953,6 +999,10 @@ souffle_status souffle_gpu_md_begin(souffle_gpu_system* h) {
       S.t[m] = p.temperature;
       S.dof[m++] = n3;
       S.m = m;
+    }
+    if (p.brownian) {  // no thermostat (src/md.cpp:187 sets one up for -D m only); the noise
+      S.m = 0;         // generator restarts from its seed every run (src/md.cpp:382-385)
+      S.lcg = kLcgSeed;
     }
     nhc_set_constants(S, p.dt);
     S.inv_n = 1.0 / S.n_beads;

@@ -79,6 +79,12 @@ struct souffle_gpu_system {
   DevBuf<int> type_d, lj_d;
   DevBuf<double> e_bead, e_tot;
   DevBuf<unsigned int> err;
+  // Brownian systems: per system and template bead drag (2^40 units) and noise scale, the
+  // generator skip-ahead table, the step's drag and random forces
+  bool any_brownian = false;
+  DevBuf<long long> bd_drag, bd_fdrag, bd_fran;
+  DevBuf<double> bd_noise;
+  DevBuf<unsigned int> lcg_table;
   // graphs keyed by (2 window length + rebuild-first, mask of steps in the window that end with
   // a surrogate judgement)
   std::map<std::pair<int, unsigned long long>, cudaGraphExec_t> graphs;

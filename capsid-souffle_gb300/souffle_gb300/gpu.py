@@ -67,7 +67,8 @@ class Params_(C.Structure):
                 ("kappa", C.c_double), ("ecut", C.c_double), ("ecut_el", C.c_double),
                 ("nlist_cutoff", C.c_double), ("nlist_capacity", C.c_int32),
                 ("center_local", C.c_int32), ("dt", C.c_double), ("chain_length", C.c_int32),
-                ("nhc_mass", C.c_double), ("temperature", C.c_double), ("build_freq", C.c_int32)]
+                ("nhc_mass", C.c_double), ("temperature", C.c_double), ("build_freq", C.c_int32),
+                ("brownian", C.c_int32), ("damp", C.c_double)]
 
 
 class Options_(C.Structure):
@@ -173,7 +174,7 @@ def system_params(opt: CliOptions, d: Derived, n_sub: int, center_local: int) ->
     """Reduced-unit parameters of one system, as run_simulation derives them."""
     return Params_(int(n_sub), d.box, opt.s, opt.b, opt.E, d.lb, d.kappa, d.ecut, d.ecut_el,
                    d.nlist_cutoff, d.nlist_capacity, int(center_local), opt.t, int(opt.q), opt.Q,
-                   d.T_reduced, int(opt.B))
+                   d.T_reduced, int(opt.B), 1 if opt.D == "b" else 0, float(opt.d))
 
 
 class GpuSystem:

@@ -83,6 +83,9 @@ typedef struct souffle_params {
   double nhc_mass;        /* -Q */
   double temperature;     /* reduced temperature T = K/298 (src/md.cpp:138) */
   int32_t build_freq;     /* -B: rebuild the pair list when step % B == 0 */
+  int32_t brownian;       /* -D b: 1 = the reference's Brownian dynamics (src/md.cpp:415-431,
+                             461-501), 0 = molecular dynamics with the Nose-Hoover chain */
+  double damp;            /* -d: damping time of the Brownian integrator (drag m / damp) */
 } souffle_params;
 
 typedef struct souffle_options {

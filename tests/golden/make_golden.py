@@ -33,6 +33,7 @@ CASES = [
     ("patch_crowded", "patch_n3", 60, 20000.0, 4242, -1.0),
 ]
 MD_STEPS = 20
+BD_DAMP = 100.0   # -d, the reference's default
 
 
 def cli(name, S, C):
@@ -79,6 +80,18 @@ def main():
             rows = np.loadtxt(f"{md}/outfiles/energy.out", skiprows=1, usecols=range(11))
             energy_text = open(f"{md}/outfiles/energy.out").read()
             restart_text = open(f"{md}/outfiles/restart_{MD_STEPS}.out").read()
+            # Brownian dynamics (-D b): the same state and steps
+            bd = f"{wd}/bd"
+            os.makedirs(f"{bd}/outfiles")
+            shutil.copytree(f"{wd}/infiles", f"{bd}/infiles")
+            for f in ("restart_0.out", "rb_0.out"):
+                shutil.copy(f"{wd}/outfiles/{f}", f"{bd}/outfiles/{f}")
+            bd_args = cli(tname, S, C) + ["-D", "b", "-d", repr(BD_DAMP), "-B", str(o.B), "-t", repr(o.t),
+                                          "-K", repr(o.K), "-T", str(MD_STEPS), "-W", "1", "-M", "1000000",
+                                          "-w", str(MD_STEPS)]
+            subprocess.run([refdump.REF_RUN] + bd_args, cwd=bd, check=True, capture_output=True)
+            _, vbd, pbd = state.read_restart(f"{bd}/outfiles/restart_{MD_STEPS}.out")
+            bd_rows = np.loadtxt(f"{bd}/outfiles/energy.out", skiprows=1, usecols=range(11))
             np.savez_compressed(
                 os.path.join(HERE, f"{name}.npz"),
                 template=np.array(tname), n_sub=S, conc=C, seed=seed, gap=gap,
@@ -92,6 +105,7 @@ def main():
                 md_steps=MD_STEPS, md_pos=pmd, md_vel=vmd, md_energy_rows=rows,
                 md_energy_text=np.array(energy_text), md_restart_text=np.array(restart_text),
                 md_args=np.array(args),
+                bd_pos=pbd, bd_vel=vbd, bd_energy_rows=bd_rows, bd_args=np.array(bd_args), bd_damp=BD_DAMP,
             )
             print(name, n, "beads; mean list", counts.mean(), "max", counts.max(), "cap", cap)
 

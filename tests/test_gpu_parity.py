@@ -238,3 +238,28 @@ def test_bad_cta_shape_is_rejected():
     with pytest.raises(gpu.SouffleError) as e:
         _gpu(g, threads_per_cta=100)
     assert e.value.code == 1
+
+
+@pytest.mark.parametrize("name", ["plain_small", "bilayer_dense"])
+def test_brownian_steps_match_reference_run(name):
+    """-D b: the reference's Brownian dynamics, including its noise sequence (minstd_rand0 seeded
+    69521, uniform in [-0.5, 0.5) through libstdc++'s generate_canonical), against the
+    reference's own 20-step run from the same state."""
+    import dataclasses
+    from souffle_gb300 import gpu
+    g = load_golden(name)
+    t, opt, d = golden_workload(g)
+    opt = dataclasses.replace(opt, D="b", d=float(g["bd_damp"]))
+    s = gpu.GpuSystem(t, [gpu.system_params(opt, d, int(g["n_sub"]), int(g["center"]))])
+    s.set_state(g["pos"], g["vel"])
+    s.md_begin()
+    s.md_steps(0, int(g["md_steps"]) + 1)      # T+1 iterations (src/md.cpp:387)
+    pos, vel = s.get_state()
+    L = float(g["box"])
+    dp = pos - g["bd_pos"]
+    dp -= L * np.round(dp / L)
+    assert np.abs(dp).max() < 1e-6
+    assert np.abs(vel - g["bd_vel"]).max() < 1e-5 * max(1.0, np.abs(g["bd_vel"]).max())
+    e = s.energies()
+    assert e["temperature"] == pytest.approx(g["bd_energy_rows"][-1, 8], rel=2e-5)
+    assert e["thermo_pe"] == 0 and e["thermo_ke"] == 0      # no thermostat in Brownian runs

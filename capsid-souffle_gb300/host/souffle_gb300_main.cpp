@@ -8,8 +8,9 @@
 //   outfiles/restart_<a>.out     src/md.cpp:526-546 (12 significant digits)
 //   outfiles/model.parameters.out  src/md.cpp:111-180,233-235
 // The MD loop (src/md.cpp:387-688, molecular-dynamics branch) runs on the GPU through the C ABI
-// in include/souffle_gpu.h; the host only steps between output points.  Brownian dynamics
-// (-D b) and encapsulation (-p) are not part of the GPU path and are rejected.
+// in include/souffle_gpu.h; the host only steps between output points.  -D b runs the Brownian
+// branch (src/md.cpp:400-470) on the same path; as in src/md.cpp:109-116 any -D other than 'm'
+// selects Brownian dynamics.  Encapsulation (-p) is not part of the GPU path and is rejected.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -215,10 +216,6 @@ void progress(double frac) {  // the bar of src/functions.cpp:24-30
 
 int main(int argc, char** argv) {
   Options o = parse(argc, argv);
-  if (o.D != 'm') {
-    fprintf(stderr, "souffle_gb300: only molecular dynamics (-D m) runs on the GPU path\n");
-    return 1;
-  }
   if (o.p) {
     fprintf(stderr, "souffle_gb300: encapsulation (-p true) is not part of the GPU path\n");
     return 1;
@@ -234,7 +231,9 @@ int main(int argc, char** argv) {
        << "LJ" << setw(15) << "electrostatics" << setw(15) << "total" << setw(15) << "potential" << setw(15)
        << "temperature" << setw(20) << "thermo_potential" << setw(15) << "thermo_kinetic" << setw(15)
        << "system_velocity_magnitude" << endl;
-  sysdata << "Running molecular dynamics with Nose Hoover thermostat." << endl;
+  const bool brownian = o.D != 'm';  // src/md.cpp:31,109-116
+  if (o.D == 'b') sysdata << "Running brownian dynamics." << endl;
+  else if (o.D == 'm') sysdata << "Running molecular dynamics with Nose Hoover thermostat." << endl;
 
   Infile in;
   if (!read_infile("infiles/" + o.f, in)) {
@@ -392,6 +391,8 @@ int main(int argc, char** argv) {
   p.nhc_mass = o.Q;
   p.temperature = Tred;
   p.build_freq = o.B;
+  p.brownian = brownian ? 1 : 0;
+  p.damp = o.d;
   souffle_gpu_system* h = nullptr;
   check(souffle_gpu_create(&t, &p, 1, nullptr, &h), "souffle_gpu_create");
   // the reference wraps lattice positions only when they move; the fixed-point state wraps now

@@ -17,14 +17,14 @@ pytestmark = pytest.mark.gpu
 DRIVER = os.path.join(REPO, "capsid-souffle_gb300", "_build", "souffle_gb300")
 
 
-def _run_driver(tmp_path, g):
+def _run_driver(tmp_path, g, key="md_args"):
     from souffle_gb300 import geometry, state
     t = geometry.template_by_name(str(g["template"]))
     os.makedirs(tmp_path / "infiles")
     os.makedirs(tmp_path / "outfiles")
     geometry.write_infile(t, str(tmp_path / "infiles" / t.name))
     state.write_restart(state.State(g["pos"], g["vel"], float(g["box"])), str(tmp_path / "outfiles"))
-    args = [str(x) for x in g["md_args"]]
+    args = [str(x) for x in g[key]]
     r = subprocess.run([DRIVER] + args, cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     return args
@@ -62,6 +62,31 @@ def test_driver_outfiles_match_reference_run(tmp_path, name):
     b = np.array([[float(x) for x in ln.split()] for ln in ref_lines[1:]])
     assert np.array_equal(a[:, 0], b[:, 0])
     np.testing.assert_allclose(a[:, 1:], b[:, 1:], rtol=0, atol=2e-6 * max(1.0, np.abs(b).max()))
+
+
+@pytest.mark.parametrize("name", ["plain_small", "bilayer_dense"])
+def test_driver_brownian_run_matches_reference_run(tmp_path, name):
+    """-D b through the driver: energy.out rows and the final restart file against the
+    reference's own Brownian run from the same state (noise sequence included)."""
+    g = load_golden(name)
+    _run_driver(tmp_path, g, "bd_args")
+    params = open(tmp_path / "outfiles" / "model.parameters.out").read()
+    assert params.splitlines()[0] == "Running brownian dynamics."
+    rows_r = np.asarray(g["bd_energy_rows"])
+    _, rows_g = _rows(open(tmp_path / "outfiles" / "energy.out").read())
+    rows_g = np.array([r[:11] for r in rows_g])
+    assert rows_g.shape == rows_r.shape
+    assert np.array_equal(rows_g[:, 0], rows_r[:, 0])
+    np.testing.assert_allclose(rows_g[:, 1:], rows_r[:, 1:], rtol=5e-5, atol=5e-6)
+    assert np.all(rows_g[:, 9:11] == 0)             # no thermostat in Brownian runs
+    from souffle_gb300 import state
+    T = int(g["md_steps"])
+    _, vel, pos = state.read_restart(str(tmp_path / "outfiles" / f"restart_{T}.out"))
+    L = float(g["box"])
+    dp = pos - g["bd_pos"]
+    dp -= L * np.round(dp / L)
+    assert np.abs(dp).max() < 1e-6
+    assert np.abs(vel - g["bd_vel"]).max() < 1e-5 * max(1.0, np.abs(g["bd_vel"]).max())
 
 
 def test_driver_restart_resume_continues_the_run(tmp_path):

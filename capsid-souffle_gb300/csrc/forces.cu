@@ -19,6 +19,8 @@
 // FP64 is used only for the per-system thermostat scalars.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "thermostat.cuh"
 
@@ -43,6 +45,24 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
   return v;
 }
 
+// A bead's force component in 2^-32 fixed point kept as three 21-bit limbs in 32-bit words
+// (v = l2 2^42 + l1 2^21 + l0, l0 and l1 in [0, 2^21), l2 signed), so that pair forces can be
+// added with native 32-bit shared-memory atomics: the limb sums stay exact for up to 2^11 adds.
+__device__ __forceinline__ void limbs_set(unsigned int* L, long long v) {
+  L[0] = (unsigned int)(v & 0x1FFFFF);
+  L[1] = (unsigned int)((v >> 21) & 0x1FFFFF);
+  L[2] = (unsigned int)(int)(v >> 42);
+}
+__device__ __forceinline__ void limbs_add(unsigned int* L, long long v) {
+  atomicAdd(L, (unsigned int)(v & 0x1FFFFF));
+  atomicAdd(L + 1, (unsigned int)((v >> 21) & 0x1FFFFF));
+  atomicAdd(L + 2, (unsigned int)(int)(v >> 42));
+}
+__device__ __forceinline__ long long limbs_value(const unsigned int* L) {
+  const unsigned long long hi = (unsigned long long)(long long)(int)L[2] << 42;
+  return (long long)(hi + ((unsigned long long)L[1] << 21) + (unsigned long long)L[0]);
+}
+
 // 5 CTAs of 256 threads per SM (<= 51 registers) so 3-subunit work items fit one wave of
 // 152 x 5 CTAs at the 2000-subunit workload.
 __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
@@ -58,19 +78,22 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   float4* s_edge = reinterpret_cast<float4*>(smem);                 // [max_sub * ne]
   float4* s_face = s_edge + a.max_sub * ne;                         // [max_sub * nf]
   float4* s_bend = s_face + a.max_sub * nf;                         // [max_sub * nb * 4]
-  int4* s_pos = reinterpret_cast<int4*>(s_bend + a.max_sub * nb * 4);  // [max_sub * np]
+  // (the tail of the system's last CTA reuses this first region for the system state)
+  int4* s_pos = reinterpret_cast<int4*>(smem + force_tile_bytes(a.max_sub, ne, nf, nb));  // [max_sub * np]
   float4* s_rel = reinterpret_cast<float4*>(s_pos + a.max_sub * np);   // [max_sub * np]
-  long long* s_red = reinterpret_cast<long long*>(s_rel + a.max_sub * np);  // [4 * 32]
-  float* s_tf = reinterpret_cast<float*>(s_red + 4 * 32);           // [n_float], n_float % 4 == 0
-  int* s_ti = reinterpret_cast<int*>(s_tf + L.n_float);             // [n_int], n_int % 4 == 0
-  float* s_w = reinterpret_cast<float*>(s_ti + L.n_int);            // [np]
+  long long* s_red = reinterpret_cast<long long*>(s_rel + a.max_sub * np);  // [4 * warps]
+  unsigned int* s_F = reinterpret_cast<unsigned int*>(s_red + 4 * (blockDim.x >> 5));  // [force_slot_len(max_sub * np)]
+  int* s_pref = reinterpret_cast<int*>(s_F + force_slot_len(a.max_sub * np));  // [force_pref_len(...)]
+  float* tpl_f = reinterpret_cast<float*>(s_pref + force_pref_len(a.max_sub * np));  // [n_float], n_float % 4 == 0
+  int* tpl_i = reinterpret_cast<int*>(tpl_f + L.n_float);                    // [n_int], n_int % 4 == 0
+  float* s_w = reinterpret_cast<float*>(tpl_i + L.n_int);                    // [np]
 
-  {
+  {  // the template tables, one copy per CTA
     const int4* gi = reinterpret_cast<const int4*>(a.tpl_i);
-    int4* si = reinterpret_cast<int4*>(s_ti);
+    int4* si = reinterpret_cast<int4*>(tpl_i);
     for (int t = threadIdx.x; t < (L.n_int >> 2); t += blockDim.x) si[t] = __ldg(gi + t);
     const float4* gf = reinterpret_cast<const float4*>(a.tpl_f);
-    float4* sf = reinterpret_cast<float4*>(s_tf);
+    float4* sf = reinterpret_cast<float4*>(tpl_f);
     for (int t = threadIdx.x; t < (L.n_float >> 2); t += blockDim.x) sf[t] = __ldg(gf + t);
   }
   for (int t = threadIdx.x; t < np; t += blockDim.x) s_w[t] = a.dh_w[w.sys * np + t];
@@ -86,13 +109,42 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     s_rel[t] = make_float4(hi_diff(p.x, c.x, unit), hi_diff(p.y, c.y, unit), hi_diff(p.z, c.z, unit),
                            __ldg(&a.dh_w[w.sys * np + l]));
   }
+  // exclusive prefix sums of the beads' inter-subunit list lengths (s_pref[nbead] = total): each
+  // thread a run of `per` beads, a warp scan, then the warp totals (s_red is free until the end)
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int per = (nbead + blockDim.x - 1) / blockDim.x;
+  int my_cnt = 0;
+  for (int i = 0; i < per; i++) {
+    const int b = threadIdx.x * per + i;
+    if (b < nbead) my_cnt += __ldg(a.inter_count + bead0 + b);
+  }
+  int incl = my_cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  int* s_wtot = reinterpret_cast<int*>(s_red);
+  if (lane == 31) s_wtot[wid] = incl;
   __syncthreads();
+  {
+    int off = incl - my_cnt;
+    for (int q = 0; q < wid; q++) off += s_wtot[q];
+    for (int i = 0; i < per; i++) {
+      const int b = threadIdx.x * per + i;
+      if (b < nbead) {
+        s_pref[b] = off;
+        off += __ldg(a.inter_count + bead0 + b);
+      }
+    }
+    if (threadIdx.x == blockDim.x - 1) s_pref[nbead] = off;
+  }
 
-  const int* e_pack = s_ti + L.o_edge;
-  const int* f_b = s_ti + L.o_face;
-  const int* bq = s_ti + L.o_bend;
-  const int* bf = s_ti + L.o_bendf;
-  const float* len0 = s_tf + L.o_len0;
+  const int* e_pack = tpl_i + L.o_edge;
+  const int* f_b = tpl_i + L.o_face;
+  const int* bq = tpl_i + L.o_bend;
+  const int* bf = tpl_i + L.o_bendf;
+  const float* len0 = tpl_f + L.o_len0;
 
   // edges: length vector and stretching coefficient (len0 - l) ks / l
   for (int t = threadIdx.x; t < w.nsub * ne; t += blockDim.x) {
@@ -119,7 +171,7 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     const int s = t / nb, k = t - s * nb;
     const int4* sp = s_pos + s * np;
     const int b0 = bq[4 * k], b1 = bq[4 * k + 1], r2 = bq[4 * k + 2], r3 = bq[4 * k + 3];
-    const float beta0 = s_tf[L.o_beta0 + k];
+    const float beta0 = tpl_f[L.o_beta0 + k];
     if (beta0 != 0.f) {
       // rest-angle option (no reference counterpart): E = kb (1 - cos(beta - beta0)) with beta
       // the signed bend angle of (across0, b0, b1, across1); -dE/dx = -kb sin(beta - beta0)
@@ -186,10 +238,10 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   }
   __syncthreads();
 
-  const int* bead_edges = s_ti + L.o_bead_edges;
-  const int* bead_roles = s_ti + L.o_bead_roles;
-  const int* species = s_ti + L.o_species;
-  const float* s_mass = s_tf + L.o_mass;
+  const int* bead_edges = tpl_i + L.o_bead_edges;
+  const int* bead_roles = tpl_i + L.o_bead_roles;
+  const int* species = tpl_i + L.o_species;
+  const float* s_mass = tpl_f + L.o_mass;
   const float kappa = P.kappa;
   const float ecut_el2 = P.ecut_el2;
   const int words = L.words;
@@ -203,18 +255,18 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   const unsigned int parity = h ? 0xAAAAAAAAu : 0x55555555u;
   const int half = blockDim.x >> 1;
 
-  // uniform trip count so the pair shuffle always has both lanes
+  // Phase 1: bonded forces and intra-subunit Debye-Hueckel pairs, two threads per bead: thread
+  // h = 0 the stretching terms, h = 1 the bending terms, and each its parity of the bead's
+  // intra-subunit row.  The pair's sum goes to the bead's fixed-point limbs in s_F.
+  // (uniform trip count so the pair shuffle always has both lanes)
   for (int base = 0; base < nbead; base += half) {
     const int t = base + (threadIdx.x >> 1);
     const bool act = t < nbead;
     long long Fx = 0, Fy = 0, Fz = 0;
-    int g = 0, l = 0;
     if (act) {
       const int s = t / np;
-      l = t - s * np;
-      g = bead0 + t;
-      const int4* sp = s_pos + s * np;
-      const int4 pi = sp[l];
+      const int l = t - s * np;
+      const int g = bead0 + t;
       float3 fown = f3(0.f, 0.f, 0.f);
       if (h == 0) {  // stretching, in the bead's edge order
         for (int k = 0; k < L.maxdeg; k++) {
@@ -237,7 +289,6 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       // intra-subunit pairs (Debye-Hueckel only: same subunit, src/forces.cpp:79-80), this
       // thread's parity of the row
       float3 fe = f3(0.f, 0.f, 0.f);
-      const float wi = s_w[l];
       const float4* sr = s_rel + s * np;
       const float4 ri = sr[l];
       const unsigned int* mrow = a.intra_mask + ((size_t)(w.sub_begin + s) * np + l) * words;
@@ -257,66 +308,87 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
           }
         }
       }
-      // inter-subunit pairs: DH + LJ/WCA.  The bead's list is one contiguous row; thread h takes
-      // one half of it, in batches of four with every id load, then every position load, in
-      // flight before any use (the gathers are L2 round trips).
-      float3 fp = f3(0.f, 0.f, 0.f);
-      const int si = species[l];
-      const int nint = a.inter_count[g];
-      const int att_row = L.lj_att_bits[si];
-      const int* row = a.inter_ids + (size_t)g * a.inter_cap;
-      const int khalf = (nint + 1) >> 1;
-      const int k0 = h ? khalf : 0, k1 = h ? nint : khalf;
-      for (int k = k0; k < k1; k += 4) {
-        int jn[4];
-        int4 pn[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) jn[u] = (k + u < k1) ? __ldg(row + k + u) : -1;
-#pragma unroll
-        for (int u = 0; u < 4; u++) pn[u] = (jn[u] >= 0) ? __ldg(&a.pos32[jn[u]]) : pi;
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          if (jn[u] < 0) continue;
-          const int4 pj = pn[u];
-          const int lj = pj.w;
-          const float3 d = dvec(pi, pj, unit);
-          const float r2 = dot3(d, d);
-          float c = 0.f;
-          const float wj = s_w[lj];
-          if (wi * wj != 0.f && r2 < ecut_el2) {
-            const float ir = rsqrtf(r2);
-            const float r = r2 * ir;
-            c = wi * wj * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
-          }
-          const int sj = species[lj];
-          const int pidx = si * kMaxSpecies + sj;
-          if (r2 < pt.cut2[pidx]) {
-            const bool att = (att_row >> sj) & 1;
-            const float eps = att ? (((L.type7_bits >> sj) & 1) ? 50.0f : P.elj_att) : 1.0f;
-            const float ir2 = 1.0f / r2;
-            const float s6 = pt.sig6[pidx] * ir2 * ir2 * ir2;
-            c += 48.0f * eps * s6 * (s6 - 0.5f) * ir2;
-          }
-          fp = fp + d * c;
-        }
-      }
+      float3 fs = f3(0.f, 0.f, 0.f);
       if (a.surr_f && h == 0) {  // far-field subunit pairs from the learned surrogate
         const float4 sv = a.surr_f[g];
-        fp = fp + f3(sv.x, sv.y, sv.z);
+        fs = f3(sv.x, sv.y, sv.z);
       }
-      const float tx = fown.x + fe.x + fp.x, ty = fown.y + fe.y + fp.y, tz = fown.z + fe.z + fp.z;
+      const float tx = fown.x + fe.x + fs.x, ty = fown.y + fe.y + fs.y, tz = fown.z + fe.z + fs.z;
       if (!(isfinite(tx) && isfinite(ty) && isfinite(tz)) ||
           fmaxf(fmaxf(fabsf(tx), fabsf(ty)), fabsf(tz)) > 1.0e9f)
         atomicOr(a.err, kErrNonFinite);
-      Fx = f32_to_fx32(fown.x) + f32_to_fx32(fe.x) + f32_to_fx32(fp.x);
-      Fy = f32_to_fx32(fown.y) + f32_to_fx32(fe.y) + f32_to_fx32(fp.y);
-      Fz = f32_to_fx32(fown.z) + f32_to_fx32(fe.z) + f32_to_fx32(fp.z);
+      Fx = f32_to_fx32(fown.x) + f32_to_fx32(fe.x) + f32_to_fx32(fs.x);
+      Fy = f32_to_fx32(fown.y) + f32_to_fx32(fe.y) + f32_to_fx32(fs.y);
+      Fz = f32_to_fx32(fown.z) + f32_to_fx32(fe.z) + f32_to_fx32(fs.z);
     }
     // the pair's total, exact in fixed point
     Fx += __shfl_xor_sync(0xffffffffu, Fx, 1);
     Fy += __shfl_xor_sync(0xffffffffu, Fy, 1);
     Fz += __shfl_xor_sync(0xffffffffu, Fz, 1);
-    if (act && h == 0 && bd) {
+    if (act && h == 0) {
+      limbs_set(s_F + 9 * t, Fx);
+      limbs_set(s_F + 9 * t + 3, Fy);
+      limbs_set(s_F + 9 * t + 6, Fz);
+    }
+  }
+  __syncthreads();
+
+  // Phase 2: inter-subunit pairs (DH + LJ/WCA, src/forces.cpp:81-138).  The CTA's beads' lists
+  // are one flat sequence (s_pref: exclusive prefix sums of their lengths) dealt out evenly over
+  // all threads, so a bead with a long list does not hold up its CTA; each pair force is added
+  // to the bead's limbs exactly in fixed point (order-independent, deterministic).
+  {
+    const int n_inter = s_pref[nbead];
+    for (int p = threadIdx.x; p < n_inter; p += blockDim.x) {
+      int lo = 0, hi = nbead;  // s_pref[lo] <= p < s_pref[hi]: the pair belongs to bead lo
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (s_pref[mid] <= p) lo = mid;
+        else hi = mid;
+      }
+      const int b = lo, g = bead0 + b, l = b % np;
+      const int j = __ldg(a.inter_ids + (size_t)g * a.inter_cap + (p - s_pref[b]));
+      const int4 pj = __ldg(&a.pos32[j]);
+      const int4 pi = s_pos[b];
+      const int si = species[l];
+      const int lj = pj.w;
+      const float3 d = dvec(pi, pj, unit);
+      const float r2 = dot3(d, d);
+      float c = 0.f;
+      const float wi = s_w[l], wj = s_w[lj];
+      if (wi * wj != 0.f && r2 < ecut_el2) {
+        const float ir = rsqrtf(r2);
+        const float r = r2 * ir;
+        c = wi * wj * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
+      }
+      const int sj = species[lj];
+      const int pidx = si * kMaxSpecies + sj;
+      if (r2 < pt.cut2[pidx]) {
+        const bool att = (L.lj_att_bits[si] >> sj) & 1;
+        const float eps = att ? (((L.type7_bits >> sj) & 1) ? 50.0f : P.elj_att) : 1.0f;
+        const float ir2 = 1.0f / r2;
+        const float s6 = pt.sig6[pidx] * ir2 * ir2 * ir2;
+        c += 48.0f * eps * s6 * (s6 - 0.5f) * ir2;
+      }
+      const float3 f = d * c;
+      if (!(isfinite(f.x) && isfinite(f.y) && isfinite(f.z)) ||
+          fmaxf(fmaxf(fabsf(f.x), fabsf(f.y)), fabsf(f.z)) > 1.0e9f) {
+        atomicOr(a.err, kErrNonFinite);
+        continue;
+      }
+      limbs_add(s_F + 9 * b, f32_to_fx32(f.x));
+      limbs_add(s_F + 9 * b + 3, f32_to_fx32(f.y));
+      limbs_add(s_F + 9 * b + 6, f32_to_fx32(f.z));
+    }
+  }
+  __syncthreads();
+
+  // Phase 3: the bead's total force, the second half kick and the kinetic-energy and momentum
+  // sums, one thread per bead
+  for (int t = threadIdx.x; t < nbead; t += blockDim.x) {
+    const int l = t % np, g = bead0 + t;
+    long long Fx = limbs_value(s_F + 9 * t), Fy = limbs_value(s_F + 9 * t + 3), Fz = limbs_value(s_F + 9 * t + 6);
+    if (bd) {
       // Brownian: tforce + (fran - mean fran over the system) + fdrag (src/md.cpp:468-494,
       // src/bead.h:147-149)
       const long long N = a.n_beads_total;
@@ -324,35 +396,32 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       Fy += a.fran[N + g] - __double2ll_rn((double)st.fran_sum[1] * st.inv_n) + a.fdrag[N + g];
       Fz += a.fran[2 * N + g] - __double2ll_rn((double)st.fran_sum[2] * st.inv_n) + a.fdrag[2 * N + g];
     }
-    if (act && h == 0) {
-      a.fx[g] = Fx;
-      a.fy[g] = Fy;
-      a.fz[g] = Fz;
-      if (a.mode == 1 || a.mode == 2) {
-        long long vx = a.vx[g], vy = a.vy[g], vz = a.vz[g];
-        if (a.mode == 1) {  // v <- v exp(-dt xi/2) + F dt sqrt(expfac)/(2m)  (src/bead.h:113-117)
-          const long long c = kick_c[l];
-          vx = vx - mul_shr(vx, delta_fx, 62) + mul_shr(Fx, c, 56);
-          vy = vy - mul_shr(vy, delta_fx, 62) + mul_shr(Fy, c, 56);
-          vz = vz - mul_shr(vz, delta_fx, 62) + mul_shr(Fz, c, 56);
-          a.vx[g] = vx;
-          a.vy[g] = vy;
-          a.vz[g] = vz;
-          px_acc += vx;
-          py_acc += vy;
-          pz_acc += vz;
-        }
-        const float ux = vel_to_f32(vx), uy = vel_to_f32(vy), uz = vel_to_f32(vz);
-        const float v2 = ux * ux + uy * uy + uz * uz;
-        if (!(v2 < 1.0e12f)) atomicOr(a.err, kErrNonFinite);  // |v| beyond 1e6: a blown-up run
-        ke_acc += f32_to_fx32(0.5f * s_mass[l] * v2);
+    a.fx[g] = Fx;
+    a.fy[g] = Fy;
+    a.fz[g] = Fz;
+    if (a.mode == 1 || a.mode == 2) {
+      long long vx = a.vx[g], vy = a.vy[g], vz = a.vz[g];
+      if (a.mode == 1) {  // v <- v exp(-dt xi/2) + F dt sqrt(expfac)/(2m)  (src/bead.h:113-117)
+        const long long c = kick_c[l];
+        vx = vx - mul_shr(vx, delta_fx, 62) + mul_shr(Fx, c, 56);
+        vy = vy - mul_shr(vy, delta_fx, 62) + mul_shr(Fy, c, 56);
+        vz = vz - mul_shr(vz, delta_fx, 62) + mul_shr(Fz, c, 56);
+        a.vx[g] = vx;
+        a.vy[g] = vy;
+        a.vz[g] = vz;
+        px_acc += vx;
+        py_acc += vy;
+        pz_acc += vz;
       }
+      const float ux = vel_to_f32(vx), uy = vel_to_f32(vy), uz = vel_to_f32(vz);
+      const float v2 = ux * ux + uy * uy + uz * uz;
+      if (!(v2 < 1.0e12f)) atomicOr(a.err, kErrNonFinite);  // |v| beyond 1e6: a blown-up run
+      ke_acc += f32_to_fx32(0.5f * s_mass[l] * v2);
     }
   }
   if (a.mode == 0) return;
 
   // exact CTA reduction in int64
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   ke_acc = warp_sum_ll(ke_acc);
   px_acc = warp_sum_ll(px_acc);
   py_acc = warp_sum_ll(py_acc);
@@ -365,6 +434,9 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   }
   __syncthreads();
   __shared__ bool last;
+  // the system's running sums (kinetic energy, momentum) for this launch: exact int64 adds,
+  // order-independent; the last CTA reads them and clears them for the next launch
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(a.partial) + 4 * (size_t)w.sys;
   if (threadIdx.x == 0) {
     long long k = 0, x = 0, y = 0, z = 0;
     for (int q = 0; q < nw; q++) {
@@ -373,9 +445,10 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       y += s_red[q * 4 + 2];
       z += s_red[q * 4 + 3];
     }
-    longlong2* dst = reinterpret_cast<longlong2*>(a.partial) + 2 * (size_t)w.slot;
-    dst[0] = make_longlong2(k, x);
-    dst[1] = make_longlong2(y, z);
+    atomicAdd(acc + 0, (unsigned long long)k);
+    atomicAdd(acc + 1, (unsigned long long)x);
+    atomicAdd(acc + 2, (unsigned long long)y);
+    atomicAdd(acc + 3, (unsigned long long)z);
     __threadfence();
     const int2 sl = a.sys_slots[w.sys];
     unsigned int prev = atomicAdd(&a.state[w.sys].done, 1u);
@@ -384,50 +457,29 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   __syncthreads();
   if (!last) return;
 
-  // Last CTA of this system: all threads sum the slots (exact int64) while the system's state
-  // is copied into shared memory; then warp 0 runs the thermostat chain (one lane per link) and
-  // warp 1 the centre-of-mass velocity.
+  // Last CTA of this system: the running sums and the system's state come into shared memory
+  // (the tile area, free by now) in one round of loads; then warp 0 runs the thermostat chain
+  // and warp 1 the centre-of-mass velocity.
   __threadfence();
-  __shared__ SysState s_state;
   static_assert(sizeof(SysState) % 16 == 0, "SysState is copied as int4");
   constexpr int kStateVecs = (int)(sizeof(SysState) / 16);
+  SysState& S = *reinterpret_cast<SysState*>(smem);
+  dfloat* chain_scratch = reinterpret_cast<dfloat*>(smem + sizeof(SysState));  // 3 kMaxChain
   const int4* st_src = reinterpret_cast<const int4*>(a.state + w.sys);
-  int4* st_dst = reinterpret_cast<int4*>(&s_state);
-  int4 st_reg = make_int4(0, 0, 0, 0);  // in flight together with the slot loads below
-  if (threadIdx.x < kStateVecs) st_reg = __ldcg(st_src + threadIdx.x);
-  const int2 sl = a.sys_slots[w.sys];
-  ke_acc = px_acc = py_acc = pz_acc = 0;
-#pragma unroll 4
-  for (int q = threadIdx.x; q < sl.y; q += blockDim.x) {
-    const longlong2* src = reinterpret_cast<const longlong2*>(a.partial) + 2 * (size_t)(sl.x + q);
-    const longlong2 v0 = __ldcg(src), v1 = __ldcg(src + 1);  // L2 (coherent), not L1
-    ke_acc += v0.x;
-    px_acc += v0.y;
-    py_acc += v1.x;
-    pz_acc += v1.y;
+  int4* st_dst = reinterpret_cast<int4*>(&S);
+  long long sum = 0;
+  if (threadIdx.x < 4) {
+    sum = (long long)__ldcg(acc + threadIdx.x);  // L2 (coherent), not L1
+    acc[threadIdx.x] = 0;
   }
-  if (threadIdx.x < kStateVecs) st_dst[threadIdx.x] = st_reg;
-  for (int q = threadIdx.x + blockDim.x; q < kStateVecs; q += blockDim.x) st_dst[q] = __ldcg(st_src + q);
-  ke_acc = warp_sum_ll(ke_acc);
-  px_acc = warp_sum_ll(px_acc);
-  py_acc = warp_sum_ll(py_acc);
-  pz_acc = warp_sum_ll(pz_acc);
+  for (int q = threadIdx.x; q < kStateVecs; q += blockDim.x) st_dst[q] = __ldcg(st_src + q);
+  if (threadIdx.x < 4) s_red[threadIdx.x] = sum;
   __syncthreads();
-  if (lane == 0) {
-    s_red[wid * 4 + 0] = ke_acc;
-    s_red[wid * 4 + 1] = px_acc;
-    s_red[wid * 4 + 2] = py_acc;
-    s_red[wid * 4 + 3] = pz_acc;
-  }
-  __syncthreads();
-  SysState& S = s_state;
   const int vcom_warp = nw > 1 ? 1 : 0;
   if (wid == 0) {
     if (lane == 0) {
-      long long k = 0;
-      for (int q = 0; q < nw; q++) k += s_red[q * 4];
       S.done = 0;
-      S.ke = df_from_fixed(k, 2.3283064365386963e-10f);  // 2^-32
+      S.ke = df_from_fixed(s_red[0], 2.3283064365386963e-10f);  // 2^-32
       if (a.mode == 1) S.steps += 1;
       if (P.brownian && a.mode == 1) {  // this step's draws are used: next step's generator state
         S.fran_sum[0] = S.fran_sum[1] = S.fran_sum[2] = 0;
@@ -435,16 +487,11 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       }
     }
     __syncwarp();
-    if (a.mode == 1) nhc_forward_warp(S, lane);
-    if (!nhc_backward_warp(S, lane)) atomicOr(a.err, kErrNonFinite);
+    if (a.mode == 1) nhc_forward_warp(S, lane, chain_scratch);
+    if (!nhc_backward_warp(S, lane, chain_scratch + 2 * kMaxChain)) atomicOr(a.err, kErrNonFinite);
   }
   if (wid == vcom_warp && lane == 0) {
-    long long x = 0, y = 0, z = 0;
-    for (int q = 0; q < nw; q++) {
-      x += s_red[q * 4 + 1];
-      y += s_red[q * 4 + 2];
-      z += s_red[q * 4 + 3];
-    }
+    const long long x = s_red[1], y = s_red[2], z = s_red[3];
     if (a.mode == 1) {
       // mean velocity, removed from every bead before the next kick (src/md.cpp:505-514)
       const double vx = (double)x * S.inv_n, vy = (double)y * S.inv_n, vz = (double)z * S.inv_n;
@@ -636,9 +683,33 @@ void launch_state_in(const StateArgs& a, int grid, int block, cudaStream_t s) {
 void launch_state_out(const StateArgs& a, int grid, int block, cudaStream_t s) {
   k_state_out<<<grid, block, 0, s>>>(a);
 }
-cudaError_t set_kernel_smem(size_t force_smem, size_t pair_smem) {
+cudaError_t set_kernel_smem(size_t force_smem, int force_threads, size_t pair_smem) {
   cudaError_t e = cudaFuncSetAttribute(k_forces, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_smem);
   if (e != cudaSuccess) return e;
+  // Ask for a shared-memory carveout that holds as many force CTAs as the registers allow (the
+  // default may be smaller, which splits a one-wave grid into two waves).
+  cudaFuncAttributes fa{};
+  if ((e = cudaFuncGetAttributes(&fa, k_forces)) != cudaSuccess) return e;
+  int dev = 0, regs_sm = 0, smem_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+  const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;
+  const int ctas = regs_sm / (warp_regs * ((force_threads + 31) / 32));
+  const size_t need = (size_t)ctas * (force_smem + fa.sharedSizeBytes + 1024);
+  const int percent = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / (size_t)smem_sm);
+  if ((e = cudaFuncSetAttribute(k_forces, cudaFuncAttributePreferredSharedMemoryCarveout, percent)) != cudaSuccess)
+    return e;
   return set_pairs_smem(pair_smem);
+}
+
+cudaError_t force_wave_ctas(int threads, size_t smem, int* ctas) {
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces, threads, smem);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  *ctas = per_sm * sms;
+  return cudaSuccess;
 }
 }  // namespace souffle

@@ -60,7 +60,7 @@ struct ForceArgs {
   const SysParams* sys;
   SysState* state;
   const WorkItem* work;
-  const int2* sys_slots;     // per system: first partial slot, slot count
+  const int2* sys_slots;     // per system: first work item, work-item (CTA) count
   const int4* pos32;
   const unsigned int* intra_mask;
   const int* inter_ids;      // [N][inter_cap] row-major, ascending
@@ -77,7 +77,7 @@ struct ForceArgs {
   long long* vx; long long* vy; long long* vz;   // velocity, 2^-32 units
   float* sfx; float* sfy; float* sfz;   // optional stretching force out
   float* bfx; float* bfy; float* bfz;   // optional bending force out
-  long long* partial;        // [slots * 4] KE (2^-32), momentum (2^-32)
+  long long* partial;        // [systems * 4] running KE and momentum sums (2^-32), zero between launches
   unsigned int* err;
   int n_beads_total;
   int max_sub;               // subunits per CTA (shared-memory sizing)
@@ -164,7 +164,9 @@ void launch_drift(const DriftArgs& a, int grid, int block, cudaStream_t s);
 void launch_state_in(const StateArgs& a, int grid, int block, cudaStream_t s);
 void launch_state_out(const StateArgs& a, int grid, int block, cudaStream_t s);
 void launch_energies(const EnergyArgs& a, int n, cudaStream_t s);
-cudaError_t set_kernel_smem(size_t force_smem, size_t pair_smem);
+cudaError_t set_kernel_smem(size_t force_smem, int force_threads, size_t pair_smem);
+// force-kernel CTAs of the given shape resident on the device at once (one wave)
+cudaError_t force_wave_ctas(int threads, size_t smem, int* ctas);
 cudaError_t set_pairs_smem(size_t smem);
 
 }  // namespace souffle

@@ -21,6 +21,7 @@ namespace souffle {
 
 constexpr int kMaxNp = 256;        // beads per subunit
 constexpr int kMaxChain = 16;      // Nose-Hoover chain links
+constexpr int kMaxInterPerBead = 2048;  // inter-subunit pairs of one bead (force-kernel limb sums)
 constexpr int kMaxSpecies = 16;
 constexpr double kTwo32 = 4294967296.0;
 
@@ -107,6 +108,21 @@ struct __align__(16) SysState {
   long long fran_sum[3]; // Brownian: sum of this step's random forces (2^-32 units)
   unsigned int lcg;      // Brownian: minstd_rand0 state before this step's draws
 };
+
+// Lengths of the force kernel's per-bead fixed-point force limbs (3 components x 3 32-bit limbs
+// per bead, padded to keep 16-byte alignment) and of its prefix-sum array (nbead + 1 ints,
+// padded to a multiple of 4).
+__host__ __device__ inline int force_slot_len(int nbead_max) { return 9 * ((nbead_max + 3) & ~3); }
+__host__ __device__ inline int force_pref_len(int nbead_max) { return (nbead_max + 4) & ~3; }
+
+// Bytes of the force kernel's first shared-memory region: the bonded tile (edge, face and
+// bending terms of max_sub subunits), and at least the system state plus the thermostat scratch
+// (3 kMaxChain dfloats) that the tail of a system's last CTA keeps there.
+__host__ __device__ inline size_t force_tile_bytes(int max_sub, int ne, int nf, int nb) {
+  const size_t tile = 16 * (size_t)max_sub * (size_t)(ne + nf + 4 * nb);
+  const size_t tail = (sizeof(SysState) + 3 * kMaxChain * sizeof(dfloat) + 15) / 16 * 16;
+  return tile > tail ? tile : tail;
+}
 
 // Work item: a run of subunits of one system handled by one CTA.
 struct WorkItem {

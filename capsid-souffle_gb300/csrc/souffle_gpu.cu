@@ -284,9 +284,9 @@ souffle_status upload(souffle_gpu_system* h) {
 }
 
 souffle_status check_err(souffle_gpu_system* h) {
-  unsigned int e = 0;
-  CUDA_TRY(cudaMemcpyAsync(&e, h->err.p, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->err_host, h->err.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const unsigned int e = *h->err_host;
   if (e) {
     CUDA_TRY(cudaMemsetAsync(h->err.p, 0, sizeof(unsigned int), h->stream));
     if (e & kErrNonFinite) return fail(SOUFFLE_ERR_NONFINITE, "non-finite force or kinetic energy");
@@ -458,36 +458,57 @@ void launch_step(souffle_gpu_system* h, bool rebuild, bool judge) {
 }
 
 
-size_t force_smem_for(const souffle_gpu_system* h, int subs) {
+size_t force_smem_for(const souffle_gpu_system* h, int subs, int threads) {
   const TplLayout& L = h->L;
   const int np = h->tpl.np;
-  return sizeof(float4) * subs * (L.ne + L.nf + 4 * L.nbend) + (sizeof(int4) + sizeof(float4)) * subs * np +
-         sizeof(long long) * 4 * 32 + sizeof(float) * (np + L.n_float) + sizeof(int) * L.n_int;
+  return force_tile_bytes(subs, L.ne, L.nf, L.nbend) + (sizeof(int4) + sizeof(float4)) * subs * np +
+         sizeof(long long) * 4 * (threads / 32) + sizeof(unsigned int) * force_slot_len(subs * np) +
+         sizeof(int) * force_pref_len(subs * np) + sizeof(float) * (np + L.n_float) + sizeof(int) * L.n_int;
 }
 
 // Work items of up to `subs` subunits of one system each (one force-kernel CTA per item, in
 // system order), their partial-sum slots, the force kernel's shared memory, and `threads` threads
 // per CTA.  Cached graphs are dropped (their launch shapes change).
+//
+// A single system whose items leave part of one wave of CTAs empty is cut into exactly as many
+// items as the wave holds (or one per subunit), of floor or ceil(S / items) subunits with the
+// larger ones first.  The block scheduler deals a one-wave grid out round-robin over the SMs, so
+// every SM then holds the same number of larger items within one, and the per-SM work is even;
+// equal items of `subs` subunits would leave some SMs with one CTA more than others (2000
+// subunits in 3-subunit items: 667 CTAs on 152 SMs, 4 or 5 per SM).
 souffle_status plan_work(souffle_gpu_system* h, int subs, int threads) {
-  const size_t smem = force_smem_for(h, subs);
+  const size_t smem = force_smem_for(h, subs, threads);
   if (smem > 200 * 1024) return fail(SOUFFLE_ERR_BAD_INPUT, "template too large for shared memory");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(set_kernel_smem(smem, threads, h->pair_smem));
+  int wave = 0;
+  CUDA_TRY(force_wave_ctas(threads, smem, &wave));
   std::vector<WorkItem> work;
   std::vector<int2> slots;
   int sub0 = 0;
   for (int k = 0; k < h->n_sys; k++) {
     const int n = h->prm[k].n_subunits;
     const int first = (int)work.size();
-    for (int b = 0; b < n; b += subs) work.push_back(WorkItem{k, sub0 + b, std::min(subs, n - b), (int)work.size()});
+    const int w0 = (n + subs - 1) / subs;
+    if (h->n_sys == 1 && wave > w0) {
+      const int items = std::min(wave, n), q = n / items, r = n % items;
+      for (int i = 0, b = 0; i < items; i++) {
+        const int len = q + (i < r ? 1 : 0);
+        work.push_back(WorkItem{k, sub0 + b, len, (int)work.size()});
+        b += len;
+      }
+    } else {
+      for (int b = 0; b < n; b += subs) work.push_back(WorkItem{k, sub0 + b, std::min(subs, n - b), (int)work.size()});
+    }
     slots.push_back(make_int2(first, (int)work.size() - first));
     sub0 += n;
   }
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
   CUDA_TRY(h->d_work.alloc(work.size()));
   CUDA_TRY(cudaMemcpy(h->d_work.p, work.data(), sizeof(WorkItem) * work.size(), cudaMemcpyHostToDevice));
   CUDA_TRY(h->d_slots.alloc(slots.size()));
   CUDA_TRY(cudaMemcpy(h->d_slots.p, slots.data(), sizeof(int2) * slots.size(), cudaMemcpyHostToDevice));
-  CUDA_TRY(h->partial.alloc(4 * work.size()));
-  CUDA_TRY(set_kernel_smem(smem, h->pair_smem));
+  CUDA_TRY(h->partial.alloc(4 * work.size()));  // the force kernel's per-system running sums
+  CUDA_TRY(cudaMemset(h->partial.p, 0, sizeof(long long) * h->partial.n));
   h->work.swap(work);
   h->slots.swap(slots);
   h->subs_per_cta = subs;
@@ -548,7 +569,9 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   // which bounds the inter part of any list the reference can hold
   int ref_cap = 64;
   for (int k = 0; k < n_systems; k++) ref_cap = std::max<int>(ref_cap, params[k].nlist_capacity);
-  h->inter_cap = h->opt.inter_capacity > 0 ? h->opt.inter_capacity : ref_cap;
+  // (at most kMaxInterPerBead: the force kernel's exact per-bead limb sums hold 2^11 pair forces,
+  // and no bead can have more neighbours within a list radius at close packing)
+  h->inter_cap = std::min(kMaxInterPerBead, h->opt.inter_capacity > 0 ? h->opt.inter_capacity : ref_cap);
   h->cand_cap = h->opt.cand_capacity > 0 ? h->opt.cand_capacity : 128;
   if (h->opt.threads_per_cta != 0 &&
       (h->opt.threads_per_cta < 64 || h->opt.threads_per_cta > 256 || h->opt.threads_per_cta % 32))
@@ -643,6 +666,7 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(h->cell_subs.alloc(h->S));
   CUDA_TRY(h->err.alloc(1));
   CUDA_TRY(cudaMemset(h->err.p, 0, sizeof(unsigned int)));
+  CUDA_TRY(cudaMallocHost(&h->err_host, sizeof(unsigned int)));
   // Brownian systems (src/md.cpp:415-431, 461-501): drag m / damp and noise scale
   // sqrt(24 m / (damp dt)) per template bead, and minstd_rand0 skip-ahead multipliers
   for (int k = 0; k < n_systems; k++) h->any_brownian = h->any_brownian || params[k].brownian;
@@ -809,7 +833,8 @@ souffle_status souffle_gpu_forces(souffle_gpu_system* h, int32_t rebuild, double
       h->cand_cap *= 2;
       CUDA_TRY(h->cand.alloc((size_t)h->cand_cap * h->S));
     } else {
-      h->inter_cap *= 2;
+      if (h->inter_cap >= kMaxInterPerBead) break;
+      h->inter_cap = std::min(kMaxInterPerBead, 2 * h->inter_cap);
       CUDA_TRY(h->inter_ids.alloc((size_t)h->inter_cap * h->N));
     }
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);
@@ -1020,6 +1045,12 @@ souffle_status souffle_gpu_md_begin(souffle_gpu_system* h) {
 }
 
 souffle_status souffle_gpu_md_steps(souffle_gpu_system* h, int64_t first_step, int32_t n_steps) {
+  const souffle_status s = souffle_gpu_md_enqueue(h, first_step, n_steps);
+  if (s != SOUFFLE_OK) return s;
+  return check_err(h);
+}
+
+souffle_status souffle_gpu_md_enqueue(souffle_gpu_system* h, int64_t first_step, int32_t n_steps) {
   if (!h || n_steps < 0 || first_step < 0) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
   if (!h->began) return fail(SOUFFLE_ERR_STATE, "md_begin has not been called");
   CUDA_TRY(cudaSetDevice(h->opt.device));
@@ -1060,7 +1091,7 @@ souffle_status souffle_gpu_md_steps(souffle_gpu_system* h, int64_t first_step, i
     if (s != SOUFFLE_OK) return s;
   }
   CUDA_TRY(cudaGetLastError());
-  return check_err(h);
+  return SOUFFLE_OK;
 }
 
 void* souffle_gpu_stream(souffle_gpu_system* h) { return h ? (void*)h->stream : nullptr; }
@@ -1129,8 +1160,8 @@ souffle_status souffle_gpu_autotune(souffle_gpu_system* h, int32_t trials, souff
   // any bead count; at most 256 threads)
   std::vector<std::pair<int, int>> cand;
   for (int subs : {1, 2, 3, 4, 6, 8})
-    for (int thr : {128, 192, 256}) {
-      if (force_smem_for(h, subs) > 200 * 1024) continue;
+    for (int thr : {96, 128, 192, 256}) {
+      if (force_smem_for(h, subs, thr) > 200 * 1024) continue;
       if (subs * np * 2 > 4 * thr) continue;  // more than two passes per thread pair
       if (subs * np * 2 < thr / 2) continue;   // most of the CTA idle
       cand.emplace_back(subs, thr);
@@ -1182,8 +1213,8 @@ souffle_status souffle_gpu_autotune(souffle_gpu_system* h, int32_t trials, souff
 
 souffle_status souffle_gpu_synchronize(souffle_gpu_system* h) {
   if (!h) return fail(SOUFFLE_ERR_BAD_INPUT, "null handle");
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
-  return SOUFFLE_OK;
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  return check_err(h);
 }
 
 }  // extern "C"

@@ -79,6 +79,7 @@ struct souffle_gpu_system {
   DevBuf<int> type_d, lj_d;
   DevBuf<double> e_bead, e_tot;
   DevBuf<unsigned int> err;
+  unsigned int* err_host = nullptr;  // pinned landing word for the error flag's read-back
   // Brownian systems: per system and template bead drag (2^40 units) and noise scale, the
   // generator skip-ahead table, the step's drag and random forces
   bool any_brownian = false;
@@ -93,6 +94,7 @@ struct souffle_gpu_system {
   ~souffle_gpu_system() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
     souffle::surrogate_free(sur);
+    if (err_host) cudaFreeHost(err_host);
     if (stream) cudaStreamDestroy(stream);
   }
 };

@@ -9,8 +9,8 @@
 //
 // Two forms with the same operations in the same order, so they give bitwise equal results:
 // serial functions (host-callable; the CPU checks against FP64 use them) and warp functions for
-// the device, where lane j holds link j: exponentials, G terms and eta updates run on all lanes
-// at once and only the link recurrence passes from lane to lane.
+// the device, where lane j evaluates link j's exponentials, G terms and eta updates at once and
+// every lane then runs the short link recurrence from shared operands.
 #pragma once
 #include "souffle_dev.cuh"
 
@@ -95,48 +95,54 @@ __host__ __device__ inline bool nhc_backward(SysState& s) {
 #ifdef __CUDACC__
 static_assert(kMaxChain <= 32, "one lane per chain link");
 
-__device__ inline dfloat df_shfl(dfloat v, int src) {
-  return {__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
-}
-
-// nhc_forward with lane j holding link j; all 32 lanes of one warp call it together (m <= 32).
-__device__ inline void nhc_forward_warp(SysState& s, int lane) {
+// Forward half on one warp: lane j evaluates link j's exponential, p_j and eta_j at once; then
+// every lane runs the link recurrence itself from those shared operands (no lane-to-lane
+// hand-off in the dependent chain) and lane j stores xi_j.  scratch: 2 kMaxChain dfloats of
+// shared memory.
+__device__ inline void nhc_forward_warp(SysState& s, int lane, dfloat* scratch) {
   const int m = s.m;
-  const bool mine = lane < m;
-  const bool on = mine && nhc_active(s, lane);
-  const dfloat xb = mine ? s.xi_b[lane] : dfloat{0.0f, 0.0f};
-  dfloat e4 = {1.0f, 0.0f}, p = {0.0f, 0.0f};
-  if (mine) s.eta[lane] = on ? nhc_eta(s, s.eta_b[lane], xb) : s.eta_b[lane];
-  if (on) {
-    e4 = nhc_e4(s, s.xi_b[lane + 1]);
-    p = df_mul(xb, e4);
+  dfloat* e4s = scratch;
+  dfloat* ps = scratch + kMaxChain;
+  if (lane < m) {
+    const bool on = nhc_active(s, lane);
+    const dfloat xb = s.xi_b[lane];
+    s.eta[lane] = on ? nhc_eta(s, s.eta_b[lane], xb) : s.eta_b[lane];
+    if (on) {
+      const dfloat e4 = nhc_e4(s, s.xi_b[lane + 1]);
+      e4s[lane] = e4;
+      ps[lane] = df_mul(xb, e4);
+    }
   }
-  dfloat x = xb, prev = {0.0f, 0.0f};
+  __syncwarp();
+  dfloat prev = {0.0f, 0.0f};
   for (int j = 0; j < m; j++) {
-    if (lane == j && on) x = df_mul(e4, df_add(p, df_mul(s.c_hdt_inv_q[j], nhc_g(s, prev, j))));
-    prev = df_shfl(x, j);
+    dfloat x = s.xi_b[j];
+    if (nhc_active(s, j)) x = df_mul(e4s[j], df_add(ps[j], df_mul(s.c_hdt_inv_q[j], nhc_g(s, prev, j))));
+    if (lane == j) s.xi[j] = x;
+    prev = x;
   }
-  if (mine) s.xi[lane] = x;
+  __syncwarp();
 }
 
-// nhc_backward with lane j holding link j; the kick factors are set by lane 0, whose return
-// value is the one that counts.
-__device__ inline bool nhc_backward_warp(SysState& s, int lane) {
+// Backward half on one warp: lane j evaluates c_j G_j (reads xi_{j-1} before it changes); then
+// every lane runs the recurrence j = M-1 .. 0 and lane j stores xi_j; lane 0 sets the kick
+// factors (its return value is the one that counts).  scratch: kMaxChain dfloats.
+__device__ inline bool nhc_backward_warp(SysState& s, int lane, dfloat* scratch) {
   __syncwarp();  // xi / eta written by other lanes (the forward half) are visible from here on
   const int m = s.m;
-  const bool mine = lane < m;
-  const bool on = mine && nhc_active(s, lane);
-  dfloat x = mine ? s.xi[lane] : dfloat{0.0f, 0.0f}, cg = {0.0f, 0.0f};
-  if (on) cg = df_mul(s.c_hdt_inv_q[lane], nhc_g(s, lane > 0 ? s.xi[lane - 1] : dfloat{0.0f, 0.0f}, lane));
+  dfloat* cgs = scratch;
+  if (lane < m && nhc_active(s, lane))
+    cgs[lane] = df_mul(s.c_hdt_inv_q[lane], nhc_g(s, lane > 0 ? s.xi[lane - 1] : dfloat{0.0f, 0.0f}, lane));
+  __syncwarp();
   dfloat next = {0.0f, 0.0f};
   for (int j = m - 1; j > -1; j--) {
-    if (lane == j && on) x = nhc_link(x, nhc_e4(s, next), cg);
-    next = df_shfl(x, j);
+    dfloat x = s.xi[j];
+    if (nhc_active(s, j)) x = nhc_link(x, nhc_e4(s, next), cgs[j]);
+    if (lane == j) s.xi_b[j] = x;
+    next = x;
   }
-  if (mine) {
-    s.xi_b[lane] = x;
-    s.eta_b[lane] = on ? nhc_eta(s, s.eta[lane], x) : s.eta[lane];
-  }
+  __syncwarp();
+  if (lane < m) s.eta_b[lane] = nhc_active(s, lane) ? nhc_eta(s, s.eta[lane], s.xi_b[lane]) : s.eta[lane];
   return lane == 0 ? nhc_kick_factors(s, next) : true;
 }
 #endif

@@ -25,7 +25,7 @@ EXPORTED = [
     "souffle_gpu_create", "souffle_gpu_destroy", "souffle_gpu_num_beads", "souffle_gpu_set_state",
     "souffle_gpu_get_state", "souffle_gpu_forces", "souffle_gpu_get_pairlist",
     "souffle_gpu_pairlist_stats", "souffle_gpu_energies", "souffle_gpu_kinetic_energy",
-    "souffle_gpu_md_begin", "souffle_gpu_md_steps", "souffle_gpu_md_scalars",
+    "souffle_gpu_md_begin", "souffle_gpu_md_steps", "souffle_gpu_md_enqueue", "souffle_gpu_md_scalars",
     "souffle_gpu_synchronize", "souffle_gpu_last_error", "souffle_gpu_stream",
     "souffle_gpu_md_profile", "souffle_gpu_kinetic_energy_noalloc", "souffle_gpu_autotune",
     # include/souffle_surrogate.h
@@ -123,6 +123,7 @@ def load() -> C.CDLL:
     lib.souffle_gpu_kinetic_energy.argtypes = [vp, C.c_int32, dp]
     lib.souffle_gpu_md_begin.argtypes = [vp]
     lib.souffle_gpu_md_steps.argtypes = [vp, C.c_int64, C.c_int32]
+    lib.souffle_gpu_md_enqueue.argtypes = [vp, C.c_int64, C.c_int32]
     lib.souffle_gpu_md_scalars.argtypes = [vp, C.c_int32, dp, dp, dp]
     lib.souffle_gpu_synchronize.argtypes = [vp]
     lib.souffle_gpu_last_error.restype = C.c_char_p
@@ -278,6 +279,10 @@ class GpuSystem:
 
     def md_steps(self, first_step: int, n_steps: int):
         _check(self.lib.souffle_gpu_md_steps(self.h, int(first_step), int(n_steps)))
+
+    def md_enqueue(self, first_step: int, n_steps: int):
+        """md_steps without waiting; errors surface at the next md_steps or synchronize."""
+        _check(self.lib.souffle_gpu_md_enqueue(self.h, int(first_step), int(n_steps)))
 
     def md_scalars(self, system: int = 0):
         ke, xi0, vc = C.c_double(), C.c_double(), C.c_double()

@@ -162,11 +162,19 @@ souffle_status souffle_gpu_md_begin(souffle_gpu_system* h);
  * system (src/md.cpp:387-514).  Uses CUDA graphs for whole rebuild windows. */
 souffle_status souffle_gpu_md_steps(souffle_gpu_system* h, int64_t first_step, int32_t n_steps);
 
+/* souffle_gpu_md_steps without the wait: queues the same iterations on the handle's stream and
+ * returns.  Device-side errors of queued steps (pair-list overflow, non-finite forces) are
+ * reported by the next souffle_gpu_md_steps or souffle_gpu_synchronize.  No reference
+ * counterpart: lets a caller queue many windows, or time steps with events, without a host
+ * round trip per call. */
+souffle_status souffle_gpu_md_enqueue(souffle_gpu_system* h, int64_t first_step, int32_t n_steps);
+
 /* Per-system scalars after the last step: particle_ke, xi[0], |v_com|. */
 souffle_status souffle_gpu_md_scalars(souffle_gpu_system* h, int32_t system, double* ke,
                                       double* xi0, double* vcom);
 
-/* Block until all queued GPU work of the handle has finished. */
+/* Block until all queued GPU work of the handle has finished; reports the device-side errors
+ * of queued steps like souffle_gpu_md_steps. */
 souffle_status souffle_gpu_synchronize(souffle_gpu_system* h);
 
 /* The CUDA stream (cudaStream_t) all work of the handle is queued on, so a caller can

@@ -294,18 +294,22 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       const unsigned int* mrow = a.intra_mask + ((size_t)(w.sub_begin + s) * np + l) * words;
       for (int wd = 0; wd < words; wd++) {
         unsigned int m = __ldg(mrow + wd) & parity;
+        // two pairs per iteration (independent chains for the scheduler), added in bit order
         while (m) {
-          const int jj = (wd << 5) + __ffs(m) - 1;
+          const int j1 = (wd << 5) + __ffs(m) - 1;
           m &= m - 1;
-          const float4 rj = sr[jj];
-          const float3 d = f3(ri.x - rj.x, ri.y - rj.y, ri.z - rj.z);
-          const float r2 = dot3(d, d);
-          if (r2 < ecut_el2) {
-            const float ir = rsqrtf(r2);
-            const float r = r2 * ir;
-            const float c = ri.w * rj.w * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
-            fe = fe + d * c;
-          }
+          const bool two = m != 0;
+          const int j2 = two ? (wd << 5) + __ffs(m) - 1 : j1;
+          m &= m - 1;
+          const float4 rj1 = sr[j1], rj2 = sr[j2];
+          const float3 d1 = f3(ri.x - rj1.x, ri.y - rj1.y, ri.z - rj1.z);
+          const float3 d2 = f3(ri.x - rj2.x, ri.y - rj2.y, ri.z - rj2.z);
+          const float r21 = dot3(d1, d1), r22 = dot3(d2, d2);
+          const float ir1 = rsqrtf(r21), ir2 = rsqrtf(r22);
+          const float c1 = ri.w * rj1.w * __expf(-kappa * (r21 * ir1)) * (ir1 * ir1) * (kappa + ir1);
+          const float c2 = ri.w * rj2.w * __expf(-kappa * (r22 * ir2)) * (ir2 * ir2) * (kappa + ir2);
+          if (r21 < ecut_el2) fe = fe + d1 * c1;
+          if (two && r22 < ecut_el2) fe = fe + d2 * c2;
         }
       }
       float3 fs = f3(0.f, 0.f, 0.f);

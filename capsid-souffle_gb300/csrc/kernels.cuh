@@ -25,6 +25,7 @@ struct CellArgs {
 
 struct CandArgs {
   CellArgs c;
+  const int4* pos32;  // [N] high words of the positions (float pre-test)
   int cap;
   int* cand;        // [S_total * cap] candidate subunits (global ids), ascending
   int* cand_count;  // [S_total]

@@ -13,6 +13,8 @@
 // fixed-point differences, matching the reference up to long double vs double ties.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace souffle {
@@ -37,8 +39,10 @@ __global__ void k_cells_count(CellArgs a) {
 
 // Exclusive scan of cell counts, one CTA per system: a system's cells hold only its own
 // subunits, which are contiguous, so its scan starts at the system's first subunit and the
-// segments line up into one global cell_start array.
-__global__ void k_cells_scan(CellArgs a) {
+// segments line up into one global cell_start array.  Each thread takes a run of kScanPer cells
+// (their loads in flight together) and the runs' sums are scanned across the CTA.
+constexpr int kScanPer = 8;
+__global__ void __launch_bounds__(1024) k_cells_scan(CellArgs a) {
   __shared__ int warp_sums[32];
   __shared__ int carry;
   const SysParams& P = a.sys[blockIdx.x];
@@ -46,10 +50,16 @@ __global__ void k_cells_scan(CellArgs a) {
   if (threadIdx.x == 0) carry = P.sub0;
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int base = 0; base < nc; base += blockDim.x) {
-    int i = base + threadIdx.x;
-    int v = (i < nc) ? a.cell_count[c0 + i] : 0;
-    int x = v;
+  for (int base = 0; base < nc; base += blockDim.x * kScanPer) {
+    const int i0 = base + threadIdx.x * kScanPer;
+    int v[kScanPer];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      v[k] = (i0 + k < nc) ? a.cell_count[c0 + i0 + k] : 0;
+      sum += v[k];
+    }
+    int x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -67,10 +77,14 @@ __global__ void k_cells_scan(CellArgs a) {
       warp_sums[lane] = w;  // inclusive
     }
     __syncthreads();
-    int excl = x - v + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
-    if (i < nc) a.cell_start[c0 + i] = excl;
+    int excl = x - sum + (wid > 0 ? warp_sums[wid - 1] : 0) + carry;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      if (i0 + k < nc) a.cell_start[c0 + i0 + k] = excl;
+      excl += v[k];
+    }
     __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    if (threadIdx.x == blockDim.x - 1) carry = excl;  // the pass's end: carry + all its counts
     __syncthreads();
   }
   // the end sentinel of the last system (other systems' ends are the next system's first start)
@@ -84,10 +98,15 @@ __global__ void k_cells_scatter(CellArgs a) {
 }
 
 
+// Margin (in length^2) within which the float test defers to the exact double test.
+__device__ __forceinline__ float pair_margin(float nl2) { return 1e-4f * (1.0f + nl2); }
+
 // One warp per subunit i: lane k scans stencil cell k (27 cells; with fewer than 3 cells per side
 // every cell of the system is a neighbour and is scanned once), testing centre distances
-// (src/functions.cpp:80-91) exactly in double.  Hits are compacted with a warp scan into shared
-// memory and put in ascending order by rank.  blockDim must be 128 (4 warps).
+// (src/functions.cpp:80-91): in float on the high words, and exactly in double from the 64-bit
+// fixed-point differences when the float value lies within a safety margin of the cut-off.  Hits
+// are compacted with a warp scan into shared memory and put in ascending order by rank.
+// blockDim must be 128 (4 warps).
 __global__ void __launch_bounds__(128) k_candidates(CandArgs a) {
   extern __shared__ int s_cand[];  // [4 warps][cap]
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -112,9 +131,16 @@ __global__ void __launch_bounds__(128) k_candidates(CandArgs a) {
     s0 = a.c.cell_start[cell];
     s1 = a.c.cell_start[cell + 1];
   }
+  const int4 pci = a.pos32[ci];
+  const float pre2f = (float)p.pre2, marg = pair_margin(pre2f);
   auto take = [&](int j) {
     if (j == i) return true;  // r2 = 0 for i == j (src/functions.cpp:90)
     const int cj = j * np + cl;
+    const int4 pcj = a.pos32[cj];
+    const float fx = hi_diff(pci.x, pcj.x, p.unit32), fy = hi_diff(pci.y, pcj.y, p.unit32),
+                fz = hi_diff(pci.z, pcj.z, p.unit32);
+    const float r2f = fx * fx + fy * fy + fz * fz;
+    if (fabsf(r2f - pre2f) > marg) return r2f < pre2f;
     const double ddx = fixed_diff(xi, a.c.px[cj], p.fx_to_len);
     const double ddy = fixed_diff(yi, a.c.py[cj], p.fx_to_len);
     const double ddz = fixed_diff(zi, a.c.pz[cj], p.fx_to_len);
@@ -150,12 +176,11 @@ __global__ void __launch_bounds__(128) k_candidates(CandArgs a) {
 }
 
 
-// Margin (in length^2) within which the float test defers to the exact double test.
-__device__ __forceinline__ float pair_margin(float nl2) { return 1e-4f * (1.0f + nl2); }
 
-// One CTA per subunit i; thread t owns bead rows t, t + blockDim, ...  Candidate subunit j's
-// positions are staged in shared memory, in ascending j, so each row's entries come out in
-// ascending global id.
+// One CTA per subunit i; thread t owns bead rows t, t + blockDim, ... (at most two: blockDim is
+// np rounded up to whole warps, at most 128, so that a one-wave grid holds every subunit).
+// Candidate subunit j's positions are staged in shared memory, in ascending j, so each row's
+// entries come out in ascending global id.
 __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int4* s32 = reinterpret_cast<int4*>(smem_raw);                   // [np] 16-byte entries first
@@ -165,6 +190,7 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
   double* row_last = reinterpret_cast<double*>(sz + a.np);         // [np] quirk pass
   int* row_has = reinterpret_cast<int*>(row_last + a.np);          // [np]
   float* sq = reinterpret_cast<float*>(row_has + a.np);           // [np]
+  unsigned int* s_imask = reinterpret_cast<unsigned int*>(sq + a.np);  // [np * words] intra bits
 
   const int i = blockIdx.x;
   const int sysid = a.sub_sys[i];
@@ -187,11 +213,19 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
   const int ci_global = i * np + p.center_local;
   const long long cxi = a.px[ci_global], cyi = a.py[ci_global], czi = a.pz[ci_global];
 
+  // Exact shortcut by the triangle inequality, from candidate j's radius about its centre bead
+  // (float on the high words, padded by eps far beyond their rounding): a row farther than
+  // R_j + r_list from j's centre has no pair with j.  Cases touched by the stale-r2 quirk skip it.
+  __shared__ float s_Rj;
+  const float r_list = sqrtf(nl2f), eps = 1e-3f * (1.0f + r_list);
+  for (int t = threadIdx.x; t < np * a.words; t += blockDim.x) s_imask[t] = 0u;
+
   const bool skip_far = a.cand_far && *a.far_ok;
   for (int c = 0; c < ncand; c++) {
     const int j = cand[c];
     if (skip_far && a.cand_far[(size_t)i * a.cand_cap + c]) continue;  // uniform over the CTA
     __syncthreads();
+    if (threadIdx.x == 0) s_Rj = 0.0f;
     for (int t = threadIdx.x; t < np; t += blockDim.x) {
       int g = j * np + t;
       sx[t] = a.px[g];
@@ -226,6 +260,16 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
     // later rows) and the computed pair just before the stale column.
     const bool quirk = p.quirks && (i_local == 0 || j_local == 0);
     const int cl = p.center_local;
+    if (!same && !quirk) {  // radius of candidate j about its centre bead
+      const int4 pc = s32[cl];
+      for (int t = threadIdx.x; t < np; t += blockDim.x) {
+        const int4 pt = s32[t];
+        const float dx = hi_diff(pt.x, pc.x, unit), dy = hi_diff(pt.y, pc.y, unit), dz = hi_diff(pt.z, pc.z, unit);
+        atomicMax(reinterpret_cast<int*>(&s_Rj), __float_as_int(sqrtf(dx * dx + dy * dy + dz * dz)));
+      }
+      __syncthreads();
+    }
+    const float reach_j = s_Rj + r_list + eps;
     const bool i0 = quirk && (i_local == 0), j0 = quirk && (j_local == 0);
     double init_r2 = 0.0;
     if (quirk) {
@@ -266,28 +310,61 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
             carried = row_last[k];
             break;
           }
+      if (same && !quirk) {
+        // each unordered pair once: row ii takes partners ii + d (mod np), d = 1 .. (np - 1) / 2,
+        // and d = np / 2 for ii < np / 2 when np is even (21 tests per row at np = 42).  The
+        // decision is symmetric in (ii, jj) in both the float and the exact test, so both rows
+        // get the bit the reference computes for each.
+        if (!qi) continue;
+        const int dmax = (np - 1) >> 1;
+        const int dlast = ((np & 1) == 0 && ii < (np >> 1)) ? (np >> 1) : dmax;
+        for (int dd = 1; dd <= dlast; dd++) {
+          int jj = ii + dd;
+          if (jj >= np) jj -= np;
+          if (sq[jj] == 0.0f || !inside(gi, pi, jj)) continue;
+          atomicOr(&s_imask[ii * a.words + (jj >> 5)], 1u << (jj & 31));
+          atomicOr(&s_imask[jj * a.words + (ii >> 5)], 1u << (ii & 31));
+        }
+        continue;
+      }
+      if (!same && !quirk) {  // a row out of reach of subunit j has no pair with it
+        const int4 pc = s32[cl];
+        const float dx = hi_diff(pi.x, pc.x, unit), dy = hi_diff(pi.y, pc.y, unit), dz = hi_diff(pi.z, pc.z, unit);
+        if (dx * dx + dy * dy + dz * dz > reach_j * reach_j) continue;
+      }
       const bool row_stale = i0 && ii == cl;
       int prev_jj = -1;  // last computed pair of this row
-      for (int jj = 0; jj < np; jj++) {
-        if (same && !(jj != ii && qi && sq[jj] != 0.0f)) continue;  // electrostatic only (:94-96)
-        bool in;
-        if (row_stale) {
-          in = carried < p.nl2;
-        } else if (j0 && jj == cl) {
-          in = (prev_jj >= 0 ? d2_exact(gi, prev_jj) : carried) < p.nl2;
-        } else {
-          in = inside(gi, pi, jj);
-          prev_jj = jj;
+      for (int w0 = 0; w0 < np; w0 += 32) {
+        unsigned int bits = 0;  // the row's intra-subunit mask word, stored once
+        const int w1 = min(np, w0 + 32);
+        for (int jj = w0; jj < w1; jj++) {
+          if (same && !(jj != ii && qi && sq[jj] != 0.0f)) continue;  // electrostatic only (:94-96)
+          bool in;
+          if (row_stale) {
+            in = carried < p.nl2;
+          } else if (j0 && jj == cl) {
+            in = (prev_jj >= 0 ? d2_exact(gi, prev_jj) : carried) < p.nl2;
+          } else {
+            in = inside(gi, pi, jj);
+            prev_jj = jj;
+          }
+          if (!in) continue;
+          if (same) {
+            bits |= 1u << (jj - w0);
+          } else {
+            int k = inter_n[r];
+            if (k < a.inter_cap) a.inter_ids[(size_t)gi * a.inter_cap + k] = j * np + jj;
+            inter_n[r] = k + 1;
+          }
         }
-        if (!in) continue;
-        if (same) {
-          mask_rows[ii * a.words + (jj >> 5)] |= 1u << (jj & 31);
-        } else {
-          int k = inter_n[r];
-          if (k < a.inter_cap) a.inter_ids[(size_t)gi * a.inter_cap + k] = j * np + jj;
-          inter_n[r] = k + 1;
-        }
+        // the subunit's own block is the only one that sets intra bits (its candidate list holds
+        // it once), so the word is written whole
+        if (same) mask_rows[ii * a.words + (w0 >> 5)] = bits;
       }
+    }
+    if (same && !quirk) {  // the symmetric block's bits, complete once every row is done
+      __syncthreads();
+      for (int t = threadIdx.x; t < np * a.words; t += blockDim.x) mask_rows[t] = s_imask[t];
     }
   }
   __syncthreads();
@@ -310,7 +387,7 @@ namespace souffle {
 void launch_cells_count(const CellArgs& a, int grid, int block, cudaStream_t s) {
   k_cells_count<<<grid, block, 0, s>>>(a);
 }
-void launch_cells_scan(const CellArgs& a, cudaStream_t s) { k_cells_scan<<<a.n_sys, 512, 0, s>>>(a); }
+void launch_cells_scan(const CellArgs& a, cudaStream_t s) { k_cells_scan<<<a.n_sys, 1024, 0, s>>>(a); }
 void launch_cells_scatter(const CellArgs& a, int grid, int block, cudaStream_t s) {
   k_cells_scatter<<<grid, block, 0, s>>>(a);
 }
@@ -322,7 +399,8 @@ void launch_candidates(const CandArgs& a, int grid, int block, cudaStream_t s) {
   k_candidates<<<g, 32 * warps_per_block, sizeof(int) * warps_per_block * a.cap, s>>>(a);
 }
 void launch_pairs(const PairArgs& a, int n_sub, size_t smem, cudaStream_t s) {
-  k_pairs<<<n_sub, 128, smem, s>>>(a);
+  const int block = std::min(128, 32 * ((a.np + 31) / 32));
+  k_pairs<<<n_sub, block, smem, s>>>(a);
 }
 cudaError_t set_pairs_smem(size_t smem) {
   return cudaFuncSetAttribute(k_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -329,6 +329,7 @@ void launch_candidates_all(souffle_gpu_system* h) {
   launch_cells_scatter(c, gb, tb, st);
   CandArgs ca{};
   ca.c = c;
+  ca.pos32 = h->pos32.p;
   ca.cap = h->cand_cap;
   ca.cand = h->cand.p;
   ca.cand_count = h->cand_count.p;
@@ -708,7 +709,8 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(cudaMemset(h->inter_count.p, 0, sizeof(int) * N));
   CUDA_TRY(cudaMemset(h->force.p, 0, sizeof(long long) * 3 * N));
 
-  h->pair_smem = np * (3 * sizeof(long long) + sizeof(int4) + sizeof(double) + sizeof(int) + sizeof(float));
+  h->pair_smem = np * (3 * sizeof(long long) + sizeof(int4) + sizeof(double) + sizeof(int) + sizeof(float)) +
+                 sizeof(unsigned int) * np * ((np + 31) / 32);
   s = plan_work(h.get(), h->subs_per_cta, h->threads);
   if (s != SOUFFLE_OK) return s;
   *out = h.release();

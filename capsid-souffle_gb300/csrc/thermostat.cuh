@@ -54,20 +54,37 @@ __host__ __device__ inline bool nhc_kick_factors(SysState& s, dfloat xb0) {
 // Forward half at the end of a step (src/md.cpp:457-460), from (xi_b, eta_b) into (xi, eta):
 // links j = 0 .. M-1, each reading xi_{j+1} before it changes (so all exponentials come first)
 // and G_j from the freshly updated xi_{j-1}.
+// The forward link update e4 (xi_j e4 + c_j G_j) rearranged so that only one square, one product
+// and one sum depend on the freshly updated xi_{j-1}: x_j = A_j + B_j xi_{j-1}^2 with
+// A_j = e4 (xi_j e4 - c_j dof_j T_j) and B_j = e4 c_j Q_{j-1}; link 0 (G_0 = 2 KE - dof_0 T)
+// depends on no other link and is A_0 itself.
+__host__ __device__ inline void nhc_forward_terms(const SysState& s, int j, dfloat& A, dfloat& B) {
+  const dfloat e4 = nhc_e4(s, s.xi_b[j + 1]);
+  const dfloat p = df_mul(s.xi_b[j], e4);
+  if (j == 0) {
+    A = df_mul(e4, df_add(p, df_mul(s.c_hdt_inv_q[0], nhc_g(s, dfloat{0.0f, 0.0f}, 0))));
+    B = dfloat{0.0f, 0.0f};
+  } else {
+    A = df_mul(e4, df_add(p, df_neg(df_mul(s.c_hdt_inv_q[j], s.c_dof_t[j]))));
+    B = df_mul(df_mul(e4, s.c_hdt_inv_q[j]), s.c_q[j - 1]);
+  }
+}
+
+__host__ __device__ inline dfloat nhc_forward_link(int j, dfloat A, dfloat B, dfloat prev) {
+  return j == 0 ? A : df_add(A, df_mul(B, df_mul(prev, prev)));
+}
+
 __host__ __device__ inline void nhc_forward(SysState& s) {
-  dfloat e4[kMaxChain], p[kMaxChain];
+  dfloat A[kMaxChain], B[kMaxChain];
   for (int j = 0; j < s.m; j++) {
     const bool on = nhc_active(s, j);
     s.eta[j] = on ? nhc_eta(s, s.eta_b[j], s.xi_b[j]) : s.eta_b[j];
-    if (on) {
-      e4[j] = nhc_e4(s, s.xi_b[j + 1]);
-      p[j] = df_mul(s.xi_b[j], e4[j]);
-    }
+    if (on) nhc_forward_terms(s, j, A[j], B[j]);
   }
   dfloat prev = {0.0f, 0.0f};
   for (int j = 0; j < s.m; j++) {
     dfloat x = s.xi_b[j];
-    if (nhc_active(s, j)) x = df_mul(e4[j], df_add(p[j], df_mul(s.c_hdt_inv_q[j], nhc_g(s, prev, j))));
+    if (nhc_active(s, j)) x = nhc_forward_link(j, A[j], B[j], prev);
     s.xi[j] = x;
     prev = x;
   }
@@ -95,29 +112,24 @@ __host__ __device__ inline bool nhc_backward(SysState& s) {
 #ifdef __CUDACC__
 static_assert(kMaxChain <= 32, "one lane per chain link");
 
-// Forward half on one warp: lane j evaluates link j's exponential, p_j and eta_j at once; then
-// every lane runs the link recurrence itself from those shared operands (no lane-to-lane
+// Forward half on one warp: lane j evaluates link j's exponential, A_j, B_j and eta_j at once;
+// then every lane runs the link recurrence itself from those shared operands (no lane-to-lane
 // hand-off in the dependent chain) and lane j stores xi_j.  scratch: 2 kMaxChain dfloats of
 // shared memory.
 __device__ inline void nhc_forward_warp(SysState& s, int lane, dfloat* scratch) {
   const int m = s.m;
-  dfloat* e4s = scratch;
-  dfloat* ps = scratch + kMaxChain;
+  dfloat* As = scratch;
+  dfloat* Bs = scratch + kMaxChain;
   if (lane < m) {
     const bool on = nhc_active(s, lane);
-    const dfloat xb = s.xi_b[lane];
-    s.eta[lane] = on ? nhc_eta(s, s.eta_b[lane], xb) : s.eta_b[lane];
-    if (on) {
-      const dfloat e4 = nhc_e4(s, s.xi_b[lane + 1]);
-      e4s[lane] = e4;
-      ps[lane] = df_mul(xb, e4);
-    }
+    s.eta[lane] = on ? nhc_eta(s, s.eta_b[lane], s.xi_b[lane]) : s.eta_b[lane];
+    if (on) nhc_forward_terms(s, lane, As[lane], Bs[lane]);
   }
   __syncwarp();
   dfloat prev = {0.0f, 0.0f};
   for (int j = 0; j < m; j++) {
     dfloat x = s.xi_b[j];
-    if (nhc_active(s, j)) x = df_mul(e4s[j], df_add(ps[j], df_mul(s.c_hdt_inv_q[j], nhc_g(s, prev, j))));
+    if (nhc_active(s, j)) x = nhc_forward_link(j, As[j], Bs[j], prev);
     if (lane == j) s.xi[j] = x;
     prev = x;
   }

@@ -48,11 +48,6 @@ __device__ __forceinline__ long long warp_sum_ll(long long v) {
 // A bead's force component in 2^-32 fixed point kept as three 21-bit limbs in 32-bit words
 // (v = l2 2^42 + l1 2^21 + l0, l0 and l1 in [0, 2^21), l2 signed), so that pair forces can be
 // added with native 32-bit shared-memory atomics: the limb sums stay exact for up to 2^11 adds.
-__device__ __forceinline__ void limbs_set(unsigned int* L, long long v) {
-  L[0] = (unsigned int)(v & 0x1FFFFF);
-  L[1] = (unsigned int)((v >> 21) & 0x1FFFFF);
-  L[2] = (unsigned int)(int)(v >> 42);
-}
 __device__ __forceinline__ void limbs_add(unsigned int* L, long long v) {
   atomicAdd(L, (unsigned int)(v & 0x1FFFFF));
   atomicAdd(L + 1, (unsigned int)((v >> 21) & 0x1FFFFF));
@@ -70,16 +65,15 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   const TplLayout& L = a.L;
   const WorkItem w = a.work[blockIdx.x];
   const SysParams& P = a.sys[w.sys];
-  const int np = L.np, ne = L.ne, nf = L.nf, nb = L.nbend;
+  const int np = L.np, ne = L.ne, nb = L.nbend;
   const int nbead = w.nsub * np;
   const int bead0 = w.sub_begin * np;  // global index of the first bead
 
   // shared-memory carve-up (16-byte aligned pieces first)
   float4* s_edge = reinterpret_cast<float4*>(smem);                 // [max_sub * ne]
-  float4* s_face = s_edge + a.max_sub * ne;                         // [max_sub * nf]
-  float4* s_bend = s_face + a.max_sub * nf;                         // [max_sub * nb * 4]
+  float4* s_bend = s_edge + a.max_sub * ne;                         // [max_sub * nb * 4]
   // (the tail of the system's last CTA reuses this first region for the system state)
-  int4* s_pos = reinterpret_cast<int4*>(smem + force_tile_bytes(a.max_sub, ne, nf, nb));  // [max_sub * np]
+  int4* s_pos = reinterpret_cast<int4*>(smem + force_tile_bytes(a.max_sub, ne, nb));  // [max_sub * np]
   float4* s_rel = reinterpret_cast<float4*>(s_pos + a.max_sub * np);   // [max_sub * np]
   long long* s_red = reinterpret_cast<long long*>(s_rel + a.max_sub * np);  // [4 * warps]
   unsigned int* s_F = reinterpret_cast<unsigned int*>(s_red + 4 * (blockDim.x >> 5));  // [force_slot_len(max_sub * np)]
@@ -109,6 +103,7 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     s_rel[t] = make_float4(hi_diff(p.x, c.x, unit), hi_diff(p.y, c.y, unit), hi_diff(p.z, c.z, unit),
                            __ldg(&a.dh_w[w.sys * np + l]));
   }
+  for (int t = threadIdx.x; t < 9 * nbead; t += blockDim.x) s_F[t] = 0u;  // the beads' force limbs
   // exclusive prefix sums of the beads' inter-subunit list lengths (s_pref[nbead] = total): each
   // thread a run of `per` beads, a warp scan, then the warp totals (s_red is free until the end)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -156,15 +151,6 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     float coef = (len0[e] - l) * P.ks / l;
     s_edge[t] = make_float4(lv.x, lv.y, lv.z, coef);
   }
-  // faces: area vector 1/2 (b1 - b0) x (b2 - b1) and its magnitude
-  for (int t = threadIdx.x; t < w.nsub * nf; t += blockDim.x) {
-    const int s = t / nf, f = t - s * nf;
-    const int4* sp = s_pos + s * np;
-    int4 p0 = sp[f_b[3 * f]], p1 = sp[f_b[3 * f + 1]], p2 = sp[f_b[3 * f + 2]];
-    float3 A = cross3(dvec(p1, p0, unit), dvec(p2, p1, unit)) * 0.5f;
-    s_face[t] = make_float4(A.x, A.y, A.z, sqrtf(dot3(A, A)));
-  }
-  __syncthreads();
   // bending edges: the four bead contributions of EDGE::update_bending_forces.
   // The in-place normal flip (src/edge.cpp:78-81) makes S = 4 |A0 . A1| whatever the flip history.
   for (int t = threadIdx.x; t < w.nsub * nb; t += blockDim.x) {
@@ -192,7 +178,13 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       o[3] = make_float4(ga1.x * c, ga1.y * c, ga1.z * c, 0.f);
       continue;
     }
-    const float4 F0 = s_face[s * nf + bf[2 * k]], F1 = s_face[s * nf + bf[2 * k + 1]];
+    // the edge's two faces: area vector 1/2 (b1 - b0) x (b2 - b1) and its magnitude
+    auto face = [&](int f) {
+      const int4 p0 = sp[f_b[3 * f]], p1 = sp[f_b[3 * f + 1]], p2 = sp[f_b[3 * f + 2]];
+      const float3 A = cross3(dvec(p1, p0, unit), dvec(p2, p1, unit)) * 0.5f;
+      return make_float4(A.x, A.y, A.z, sqrtf(dot3(A, A)));
+    };
+    const float4 F0 = face(bf[2 * k]), F1 = face(bf[2 * k + 1]);
     const float a0 = F0.w, a1 = F1.w;
     const float S = 4.0f * fabsf(F0.x * F1.x + F0.y * F1.y + F0.z * F1.z);
     const int4 P0 = sp[b0], P1 = sp[b1], P2 = sp[r2], P3 = sp[r3];
@@ -257,7 +249,7 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
 
   // Phase 1: bonded forces and intra-subunit Debye-Hueckel pairs, two threads per bead: thread
   // h = 0 the stretching terms, h = 1 the bending terms, and each its parity of the bead's
-  // intra-subunit row.  The pair's sum goes to the bead's fixed-point limbs in s_F.
+  // intra-subunit row.  The pair's sum is added to the bead's fixed-point limbs in s_F.
   // (uniform trip count so the pair shuffle always has both lanes)
   for (int base = 0; base < nbead; base += half) {
     const int t = base + (threadIdx.x >> 1);
@@ -330,12 +322,12 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     Fy += __shfl_xor_sync(0xffffffffu, Fy, 1);
     Fz += __shfl_xor_sync(0xffffffffu, Fz, 1);
     if (act && h == 0) {
-      limbs_set(s_F + 9 * t, Fx);
-      limbs_set(s_F + 9 * t + 3, Fy);
-      limbs_set(s_F + 9 * t + 6, Fz);
+      limbs_add(s_F + 9 * t, Fx);
+      limbs_add(s_F + 9 * t + 3, Fy);
+      limbs_add(s_F + 9 * t + 6, Fz);
     }
   }
-  __syncthreads();
+  // (no barrier: phase 2 adds into the same zeroed limbs, in any order)
 
   // Phase 2: inter-subunit pairs (DH + LJ/WCA, src/forces.cpp:81-138).  The CTA's beads' lists
   // are one flat sequence (s_pref: exclusive prefix sums of their lengths) dealt out evenly over

@@ -21,7 +21,8 @@ namespace souffle {
 
 constexpr int kMaxNp = 256;        // beads per subunit
 constexpr int kMaxChain = 16;      // Nose-Hoover chain links
-constexpr int kMaxInterPerBead = 2048;  // inter-subunit pairs of one bead (force-kernel limb sums)
+constexpr int kMaxInterPerBead = 2047;  // inter-subunit pairs of one bead (force-kernel limb sums
+                                        // hold 2^11 adds: these plus the bead's own terms)
 constexpr int kMaxSpecies = 16;
 constexpr double kTwo32 = 4294967296.0;
 
@@ -115,11 +116,11 @@ struct __align__(16) SysState {
 __host__ __device__ inline int force_slot_len(int nbead_max) { return 9 * ((nbead_max + 3) & ~3); }
 __host__ __device__ inline int force_pref_len(int nbead_max) { return (nbead_max + 4) & ~3; }
 
-// Bytes of the force kernel's first shared-memory region: the bonded tile (edge, face and
-// bending terms of max_sub subunits), and at least the system state plus the thermostat scratch
+// Bytes of the force kernel's first shared-memory region: the bonded tile (edge and bending
+// terms of max_sub subunits), and at least the system state plus the thermostat scratch
 // (3 kMaxChain dfloats) that the tail of a system's last CTA keeps there.
-__host__ __device__ inline size_t force_tile_bytes(int max_sub, int ne, int nf, int nb) {
-  const size_t tile = 16 * (size_t)max_sub * (size_t)(ne + nf + 4 * nb);
+__host__ __device__ inline size_t force_tile_bytes(int max_sub, int ne, int nb) {
+  const size_t tile = 16 * (size_t)max_sub * (size_t)(ne + 4 * nb);
   const size_t tail = (sizeof(SysState) + 3 * kMaxChain * sizeof(dfloat) + 15) / 16 * 16;
   return tile > tail ? tile : tail;
 }

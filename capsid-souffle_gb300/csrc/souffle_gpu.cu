@@ -462,7 +462,7 @@ void launch_step(souffle_gpu_system* h, bool rebuild, bool judge) {
 size_t force_smem_for(const souffle_gpu_system* h, int subs, int threads) {
   const TplLayout& L = h->L;
   const int np = h->tpl.np;
-  return force_tile_bytes(subs, L.ne, L.nf, L.nbend) + (sizeof(int4) + sizeof(float4)) * subs * np +
+  return force_tile_bytes(subs, L.ne, L.nbend) + (sizeof(int4) + sizeof(float4)) * subs * np +
          sizeof(long long) * 4 * (threads / 32) + sizeof(unsigned int) * force_slot_len(subs * np) +
          sizeof(int) * force_pref_len(subs * np) + sizeof(float) * (np + L.n_float) + sizeof(int) * L.n_int;
 }

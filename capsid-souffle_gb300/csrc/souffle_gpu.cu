@@ -1199,6 +1199,12 @@ souffle_status souffle_gpu_autotune(souffle_gpu_system* h, int32_t trials, souff
       best_shape = c;
     }
   }
+  // The default shape stays unless another is clearly faster: the search times forces-only
+  // launches, and differences of a few percent there are within run-to-run noise.
+  if (def_us > 0 && best > 0.97 * def_us) {
+    best = def_us;
+    best_shape = std::make_pair(def_subs, def_threads);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (s != SOUFFLE_OK) return s;

@@ -21,7 +21,8 @@ OUT = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(REPO, "include")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["pairlist.cu", "forces.cu", "energies.cu", "souffle_gpu.cu", "noalloc.cu", "gemm.cu", "mlp.cu", "surrogate.cu"]
+CU_SOURCES = ["pairlist.cu", "forces.cu", "energies.cu", "souffle_gpu.cu", "noalloc.cu", "gemm.cu", "mlp.cu", "surrogate.cu",
+              "analysis.cu"]
 LIB = os.path.join(OUT, "libsouffle_gb300.so")
 DRIVER = os.path.join(OUT, "souffle_gb300")
 
@@ -43,7 +44,7 @@ def _newer(target, deps):
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
-    headers.append(os.path.join(INCLUDE, "souffle_gpu.h"))
+    headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE,
                      "-I", CSRC, "--expt-relaxed-constexpr"]
     if verbose:

@@ -25,6 +25,8 @@
 #include <string>
 #include <vector>
 
+#include "analysis_host.h"
+#include "souffle_analysis.h"
 #include "souffle_gpu.h"
 
 using namespace std;
@@ -45,6 +47,12 @@ struct Options {
   double a = 3.0, G = -78.0;
   int m = 1;
   double H = 3.5;
+  // not in the reference: what runs (r = MD then analysis, as src/main.cpp:15-16; o = analysis
+  // only; n = MD only), beads per subunit for the analysis (0 = the reference's 41/43/78 rule),
+  // and the analysis image rule (r = as the reference's analysis computes it, m = minimum image)
+  char A = 'r';
+  int Y = 0;
+  char I = 'r';
 };
 
 bool parse_bool(const string& v) {
@@ -58,7 +66,10 @@ void usage() {
   printf("Usage:\nsouffle_gb300 <options>  (letters as the reference driver)\n"
          "  -D b|m  -f infile  -C uM  -c mM  -S subunits  -s ks  -b kb  -T steps  -t dt\n"
          "  -q chain  -Q mass  -K kelvin  -e ecut_c  -R bool  -E eps  -B rebuild  -L skin\n"
-         "  -M movie  -W energy  -w restart  (-r -d -X -V -N -p -a -G -m -H accepted)\n");
+         "  -M movie  -W energy  -w restart  (-r -d -X -V -N -p -a -G -m -H accepted)\n"
+         "  -A r|o|n  MD then analysis (default) | analysis only | MD only\n"
+         "  -Y np     beads per subunit for the analysis (default: 41, 43 or 78 from the bead count)\n"
+         "  -I r|m    analysis image rule: as the reference's analysis (default) | minimum image\n");
 }
 
 // Short options "-X value" or "-Xvalue" (src/md.cpp:53-90).
@@ -115,6 +126,9 @@ Options parse(int argc, char** argv) {
       case 'G': o.G = atof(v.c_str()); break;
       case 'm': o.m = atoi(v.c_str()); break;
       case 'H': o.H = atof(v.c_str()); break;
+      case 'A': o.A = v[0]; break;
+      case 'Y': o.Y = atoi(v.c_str()); break;
+      case 'I': o.I = v[0]; break;
       default:
         fprintf(stderr, "unrecognised option -%c\n", k);
         exit(2);
@@ -212,10 +226,29 @@ void progress(double frac) {  // the bar of src/functions.cpp:24-30
   fflush(stdout);
 }
 
+int run_simulation(const Options& o);
+
 }  // namespace
 
 int main(int argc, char** argv) {
   Options o = parse(argc, argv);
+  if (o.A != 'r' && o.A != 'o' && o.A != 'n') {
+    fprintf(stderr, "souffle_gb300: -A takes r, o or n\n");
+    return 2;
+  }
+  if (o.A != 'o') {
+    const int rc = run_simulation(o);
+    if (rc != 0 || o.A == 'n') return rc;
+  }
+  souffle_host::AnalysisCli cli;
+  cli.beads_per_subunit = o.Y;
+  cli.image = o.I == 'm' ? SOUFFLE_IMAGE_MINIMUM : SOUFFLE_IMAGE_REFERENCE;
+  return souffle_host::analyze_output(cli);
+}
+
+namespace {
+
+int run_simulation(const Options& o) {
   if (o.p) {
     fprintf(stderr, "souffle_gb300: encapsulation (-p true) is not part of the GPU path\n");
     return 1;
@@ -455,3 +488,5 @@ int main(int argc, char** argv) {
   souffle_gpu_destroy(h);
   return 0;
 }
+
+}  // namespace

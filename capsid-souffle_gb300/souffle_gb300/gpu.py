@@ -33,6 +33,10 @@ EXPORTED = [
     "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_gradients", "souffle_mlp_train_step",
     "souffle_gemm_bf16", "souffle_surrogate_attach", "souffle_surrogate_collect", "souffle_surrogate_fit",
     "souffle_surrogate_enable", "souffle_surrogate_get_stats",
+    # include/souffle_analysis.h
+    "souffle_analysis_default_options", "souffle_analysis_create", "souffle_analysis_destroy",
+    "souffle_analysis_frames", "souffle_analysis_enqueue", "souffle_analysis_synchronize",
+    "souffle_analysis_stream", "souffle_analysis_last_counts",
 ]
 
 

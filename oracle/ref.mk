@@ -3,6 +3,7 @@
 # oracle/_ref/ (git-ignored).  Two programs come out:
 #   oracle/_ref/ref_run    run_simulation only (the reference MD driver)
 #   oracle/_ref/ref_dump   forces, pair lists and energies for one state
+#   oracle/_ref/ref_analyze  analyze_output only (the reference post-run analysis)
 # Usage: make -f oracle/ref.mk REF=/path/to/capsid-souffle -j8
 # The reference's own build (src/Makefile) needs mpicxx, Boost and GSL, none of
 # which exist here, so this recipe compiles the same files with g++ instead,
@@ -18,7 +19,7 @@ INC := -I$(HERE)shim -I$(REF)/src
 LIBSRC := bead edge face subunit functions forces energies initialize analysis
 LIBOBJ := $(addprefix $(OUT)/obj/,$(addsuffix .o,$(LIBSRC)))
 
-all: $(OUT)/ref_run $(OUT)/ref_dump
+all: $(OUT)/ref_run $(OUT)/ref_dump $(OUT)/ref_analyze
 
 $(OUT)/obj/%.o: $(REF)/src/%.cpp
 	@mkdir -p $(OUT)/obj
@@ -32,6 +33,9 @@ $(OUT)/ref_run: $(HERE)harness/ref_run_main.cpp $(LIBOBJ) $(OUT)/obj/md.o
 	$(CXX) $(CXXFLAGS) $(INC) $^ -o $@
 
 $(OUT)/ref_dump: $(HERE)harness/ref_dump_main.cpp $(LIBOBJ)
+	$(CXX) $(CXXFLAGS) $(INC) $^ -o $@
+
+$(OUT)/ref_analyze: $(HERE)harness/ref_analyze_main.cpp $(LIBOBJ)
 	$(CXX) $(CXXFLAGS) $(INC) $^ -o $@
 
 # Link-substitution check of the drop-in binding: the reference driver with src/forces.cpp

@@ -14,7 +14,7 @@ def _header_symbols():
     for name in sorted(os.listdir(os.path.join(REPO, "include"))):
         if name.endswith(".h"):
             text = open(os.path.join(REPO, "include", name)).read()
-            syms |= set(re.findall(r"\b(souffle_(?:gpu|mlp|gemm|surrogate)_\w+)\s*\(", text))
+            syms |= set(re.findall(r"\b(souffle_(?:gpu|mlp|gemm|surrogate|analysis)_\w+)\s*\(", text))
     return sorted(syms)
 
 

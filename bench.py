@@ -17,7 +17,9 @@ Verlet, the pair-list rebuild every 10th step, forces, centre-of-mass velocity r
          OpenMP over subunits, all host cores) on a bounded sample of the same workload.
 
 --surrogate: the learned far-field surrogate (include/souffle_surrogate.h) against the plain
-path on the same workload and protocol; --replicas N: a batch of N uneven systems in one handle.
+path on the same workload and protocol; --replicas N: a batch of N uneven systems in one handle;
+--analysis: the post-run trajectory analysis (include/souffle_analysis.h), frames/s on frames of
+2000 43-bead capsomeres (86,000 beads).
 
 Multi-GPU (torchrun): every rank runs an independent replica of the workload (replicas only;
 the path has no exchange step), value = total bead-steps / max rank time.
@@ -278,6 +280,143 @@ def bench_surrogate(args):
                      "final_loss_normalised": loss, "generation_s": gen_s, "fit_s": fit_s}}))
 
 
+def cpu_analysis_port(n_sub: int, seconds: float = 10.0):
+    """Time the C restatement of the reference's analysis loops (oracle/analysis_port.c, long
+    double, one thread, as the reference's analyze_output) on frames of the same generator at two
+    smaller sizes, and extrapolate to n_sub subunits with the fitted a*S^2 + b*S cost."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import analysis_oracle as ao
+    from souffle_gb300 import workloads
+    sizes, times = [], []
+    S = 50
+    while True:
+        ty, fr, L, np_ = workloads.analysis_frames(S, 1)
+        t0 = time.perf_counter()
+        ao.port_frame(ty, fr[0], L, np_)
+        dt = time.perf_counter() - t0
+        sizes.append(S)
+        times.append(dt)
+        if sum(times) > seconds / 3 or S * 2 > n_sub:
+            break
+        S *= 2
+    A = np.array([[s * s, s] for s in sizes], dtype=float)
+    coef = np.linalg.lstsq(A, np.array(times), rcond=None)[0]
+    t_full = float(coef[0] * n_sub * n_sub + coef[1] * n_sub)
+    if n_sub in sizes:
+        t_full = times[sizes.index(n_sub)]
+    import platform
+    return {"value": 1.0 / t_full, "unit": "frames/s", "cores": 1, "kind": "port",
+            "sample": f"one frame each at {sizes} subunits ({[round(t, 3) for t in times]} s); "
+                      f"full size {n_sub} extrapolated by a*S^2+b*S; long double = "
+                      f"{'x87 80-bit' if platform.machine() in ('x86_64', 'AMD64') else 'IEEE binary128 (software)'}"
+                      f" on {platform.machine()}"}
+
+
+def bench_analysis(args):
+    """Post-run analysis: frames/s of souffle_analysis on 86,000-bead frames."""
+    import numpy as np
+    from souffle_gb300 import workloads
+    S = args.subunits
+    types, frames, box, np_ = workloads.analysis_frames(S, 4)
+    N = S * np_
+    config = {"workload": f"analysis_large: {S} capsomeres x {np_} beads = {N} beads per frame, "
+                          f"800 uM (box {box:.4g}), 60% in chains of 2-8, pcf type 5 (4 per subunit), "
+                          f"sub-oligomer type 0 (6 per subunit), 100 bins, contact 2",
+              "image": "reference rule (as analyze_output computes dist())",
+              "l2": "flushed (256 MB write) before every timed frame",
+              "parallelism": "replicas x1"}
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        cb = cpu_analysis_port(S, args.cpu_seconds)
+        print(json.dumps({
+            "impl": "reference", "metric": "frames/s", "value": cb["value"], "unit": "frames/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "long double",
+            "data": "synthetic (seeded capsomere frames)", "config": config, "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    from souffle_gb300.analysis import Analysis, IMAGE_MINIMUM, IMAGE_REFERENCE
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda:0")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    pos_d = torch.tensor(frames, dtype=torch.float64, device=dev)
+    typ_d = torch.tensor(types, dtype=torch.int32, device=dev)
+    out = {}
+    for image, key in ((IMAGE_REFERENCE, "reference"), (IMAGE_MINIMUM, "minimum")):
+        a = Analysis(N, np_, box, image=image)
+        gr = torch.zeros(100, dtype=torch.int64, device=dev)
+        ol = torch.zeros(S, dtype=torch.int64, device=dev)
+        so = torch.zeros(2 * S, dtype=torch.int64, device=dev)
+        ext = torch.cuda.ExternalStream(a.stream())
+        for k in range(max(3, args.warmup)):
+            a.enqueue(pos_d[k % 4].data_ptr(), typ_d.data_ptr(), gr.data_ptr(), ol.data_ptr(), so.data_ptr())
+        a.synchronize()
+        torch.cuda.synchronize()
+        samples, stop, th = _clock_sampler()
+        th.start()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        for k in range(args.steps):
+            with torch.cuda.stream(ext):
+                flush.zero_()
+            evs[k][0].record(ext)
+            a.enqueue(pos_d[k % 4].data_ptr(), typ_d.data_ptr(), gr.data_ptr(), ol.data_ptr(), so.data_ptr())
+            evs[k][1].record(ext)
+        a.synchronize()
+        torch.cuda.synchronize()
+        stop.set()
+        th.join()
+        ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+        cand, fp64 = a.last_counts()
+        olig = ol.cpu().numpy()
+        # e2e: frames from host memory through souffle_analysis_frames (H2D of positions and
+        # types, results back to the host every frame)
+        host = np.ascontiguousarray(np.stack([frames[k % 4] for k in range(args.steps)]))
+        host_t = np.ascontiguousarray(np.broadcast_to(types, (args.steps, N)))
+        t0 = time.perf_counter()
+        a.frames(host, host_t)
+        e2e_s = time.perf_counter() - t0
+        out[key] = {"ms": float(np.mean(ms)), "value": args.steps / (sum(ms) / 1e3), "e2e": args.steps / e2e_s,
+                    "candidate_pairs": cand, "fp64_pairs": fp64, "clocks": _summarize_clocks(samples),
+                    "oligomers_gt1": int(olig[1:].sum()), "launches_per_frame": 7}
+        a.close()
+    r = out["reference"]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    frame_bytes = (24 + 4) * N  # positions and types read once: the data a frame must move
+    n5 = 4 * S
+    res = {
+        "metric": "frames/s", "value": r["value"], "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 with f64 tie-breaks", "data": "synthetic (seeded capsomere frames)",
+        "config": config,
+        "e2e": {"value": r["e2e"], "unit": "frames/s", "h2d_bytes_per_step": frame_bytes,
+                "d2h_bytes_per_step": 8 * (100 + 3 * S) + 4 * S,
+                "note": "souffle_analysis_frames from host arrays: upload, 7 kernels, results back, per frame"},
+        "gpu_launches": 7 * args.steps,
+        "minimum_image": out["minimum"],
+        "work_per_frame": {"pcf_pairs": n5 * (n5 - 1) // 2, "candidate_subunit_pairs": r["candidate_pairs"],
+                           "bead_pair_tests_contacts": r["candidate_pairs"] * np_ * np_,
+                           "fp64_decisions": r["fp64_pairs"]},
+        "roofline": {"bound": "hbm", "kernel": "whole frame (7 kernels)", "achieved": frame_bytes / (r["ms"] / 1e3) / 1e9,
+                     "peak": peak, "unit": "GB/s", "frac": frame_bytes / (r["ms"] / 1e3) / 1e9 / peak,
+                     "traffic": None,
+                     "note": "the frame's data is 2.4 MB; the work is FP32 pair tests, so the HBM "
+                             "fraction is small by construction"},
+        "clocks": r["clocks"],
+    }
+    if not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_analysis_port(S, args.cpu_seconds)
+    print(json.dumps(res))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -294,6 +433,8 @@ def main():
                          "per-replica epsilon, Debye length and concentration) instead")
     ap.add_argument("--surrogate", action="store_true",
                     help="learned far-field surrogate vs the plain path on the same workload")
+    ap.add_argument("--analysis", action="store_true",
+                    help="post-run trajectory analysis (pcf, oligomers, sub-oligomers), frames/s")
     ap.add_argument("--train-rows", type=int, default=2_000_000)
     ap.add_argument("--max-frames", type=int, default=6000)
     ap.add_argument("--epochs", type=int, default=20)
@@ -303,6 +444,8 @@ def main():
         return bench_replicas(args)
     if args.surrogate:
         return bench_surrogate(args)
+    if args.analysis:
+        return bench_analysis(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -88,3 +88,42 @@ def replicas(n: int = 256, seed: int = 2024, sub_range=(20, 500)) -> List[Worklo
         salt = state.salt_for_debye_length(lam)
         out.append(make(t, S, seed=seed * 1000 + k, name=f"replica{k}", E=eps, c=salt, C=conc))
     return out
+
+
+def analysis_frames(n_sub: int = 2000, n_frames: int = 4, seed: int = 4242, conc_um: float = 800.0,
+                    cluster_frac: float = 0.6, sigma_si: float = 1e-9):
+    """Frames for the post-run analysis: 43-bead capsomeres (the bilayer patch plus a centre
+    bead; the reference's analysis only sizes 41-, 43- and 78-bead subunits), 6 beads of type 0
+    (sub-oligomer beads) and 4 of type 5 (pair-correlation beads) per subunit, in the box of
+    n_sub subunits at conc_um micromolar (src/md.cpp:159).  A fraction of the subunits sits in
+    chains of 2-8 with neighbours 3-5 sigma apart, so that oligomers and sub-oligomers form; later
+    frames move every subunit by up to 0.3 sigma.
+
+    Returns (types (N,) int32, frames (F, N, 3) float64, box, beads per subunit)."""
+    t = geometry.bilayer_n5()
+    local = t.pos - t.pos.mean(axis=0)
+    local = np.vstack([local, np.zeros((1, 3))])
+    np_ = local.shape[0]
+    types = np.ones(np_, dtype=np.int32)
+    types[0:6] = 0
+    types[6:10] = 5
+    box = (n_sub * 1000 / (conc_um * sigma_si ** 3 * 6.022e23)) ** (1.0 / 3.0)
+    rng = np.random.default_rng(seed)
+    n_cl = int(n_sub * cluster_frac)
+    centres = []
+    while len(centres) < n_cl:
+        c = rng.uniform(-box / 2, box / 2, 3)
+        for _ in range(min(int(rng.integers(2, 9)), n_cl - len(centres))):
+            centres.append(c.copy())
+            d = rng.normal(size=3)
+            c = c + d / np.linalg.norm(d) * rng.uniform(3.0, 5.0)
+    centres = np.vstack([np.array(centres).reshape(-1, 3), rng.uniform(-box / 2, box / 2, (n_sub - n_cl, 3))])
+    rots = state._random_rotations(rng, n_sub)
+    frames = []
+    for f in range(n_frames):
+        shift = rng.uniform(-0.3, 0.3, (n_sub, 3)) if f else np.zeros((n_sub, 3))
+        pos = (np.einsum("sij,bj->sbi", rots, local) + (centres + shift)[:, None, :]).reshape(-1, 3)
+        pos = pos - box * np.floor(pos / box + 0.5)
+        pos = np.where(pos >= box / 2, pos - box, pos)
+        frames.append(pos)
+    return np.tile(types, n_sub), np.stack(frames), box, np_

@@ -27,7 +27,9 @@ the same decimal inputs.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
+import os
 import re
 
 import numpy as np
@@ -304,3 +306,35 @@ def analyze(energy_text: str, trajectory_text: str, np_: int | None = None, imag
     return {"analysis.rdat": tf["rdat"], "analysis.gr": gr_s.text(), "analysis.so": so_s.text(),
             "analysis.ms": ms_s.text(), "info.gr": info.text(), "trust": tf,
             "frames_analysed": len(ms_frames)}
+
+
+_PORT = None
+
+
+def port_frame(types, pos, L, np_, image=IMAGE_REFERENCE, pcf_type=5, pcf_bins=100, so_type=0,
+               contact=2.0):
+    """One frame through the C restatement of the reference's loops (oracle/analysis_port.c, long
+    double, single thread): (gr (bins,), oligomer size histogram (S,), sub-oligomer bins (2S,))."""
+    global _PORT
+    if _PORT is None:
+        lib = C.CDLL(os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "liboracle.so"))
+        lp = C.POINTER(C.c_longlong)
+        lib.oracle_analysis_frame.argtypes = [C.c_long, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                              C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                              lp, lp, lp]
+        _PORT = lib
+    t = np.ascontiguousarray(types, dtype=np.int32)
+    p = np.ascontiguousarray(pos, dtype=np.float64)
+    n = len(t)
+    S = n // np_
+    gr = np.zeros(pcf_bins, dtype=np.int64)
+    ms = np.zeros(S, dtype=np.int64)
+    so = np.zeros(2 * S, dtype=np.int64)
+    lp = C.POINTER(C.c_longlong)
+    rc = _PORT.oracle_analysis_frame(n, np_, t.ctypes.data_as(C.POINTER(C.c_int)),
+                                     p.ctypes.data_as(C.POINTER(C.c_double)), L, image, pcf_type, pcf_bins,
+                                     so_type, contact, gr.ctypes.data_as(lp), ms.ctypes.data_as(lp),
+                                     so.ctypes.data_as(lp))
+    if rc:
+        raise ValueError("a sub-oligomer lies past the histogram")
+    return gr, ms, so

@@ -81,3 +81,18 @@ def test_subunit_size_rule():
     assert ao.subunit_size(41 * 43) == 43   # the last matching size wins (src/analysis.cpp:81-83)
     assert ao.subunit_size(78 * 2) == 78
     assert ao.subunit_size(42 * 2000) == 0  # the reference divides by zero next
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_c_port_agrees_with_the_oracle(name):
+    """oracle/analysis_port.c (the reference's loop structure in long double, used as the CPU
+    baseline) gives the oracle's integers on the reference fixtures, both image rules."""
+    g = load_golden(f"analysis_{name}")
+    for _s, half, types, pos in ao.read_trajectory(str(g["trajectory"])):
+        for image in (ao.IMAGE_REFERENCE, ao.IMAGE_MINIMUM):
+            gr, olig, so = ao.frame_analysis(types, pos, 2 * half, int(g["np_"]), image)
+            S = len(pos) // int(g["np_"])
+            pg, pm, ps = ao.port_frame(types, pos, 2 * half, int(g["np_"]), image)
+            np.testing.assert_array_equal(pg, gr)
+            np.testing.assert_array_equal(pm, np.bincount(olig - 1, minlength=S))
+            np.testing.assert_array_equal(ps, np.bincount((so - 1) // 3, minlength=2 * S))

@@ -381,7 +381,7 @@ def bench_analysis(args):
         e2e_s = time.perf_counter() - t0
         out[key] = {"ms": float(np.mean(ms)), "value": args.steps / (sum(ms) / 1e3), "e2e": args.steps / e2e_s,
                     "candidate_pairs": cand, "fp64_pairs": fp64, "clocks": _summarize_clocks(samples),
-                    "oligomers_gt1": int(olig[1:].sum()), "launches_per_frame": 7}
+                    "oligomers_gt1": int(olig[1:].sum()), "launches_per_frame": 6}
         a.close()
     r = out["reference"]
     peaks = {}
@@ -399,13 +399,13 @@ def bench_analysis(args):
         "config": config,
         "e2e": {"value": r["e2e"], "unit": "frames/s", "h2d_bytes_per_step": frame_bytes,
                 "d2h_bytes_per_step": 8 * (100 + 3 * S) + 4 * S,
-                "note": "souffle_analysis_frames from host arrays: upload, 7 kernels, results back, per frame"},
-        "gpu_launches": 7 * args.steps,
+                "note": "souffle_analysis_frames from host arrays: upload, 6 kernels, results back, per frame"},
+        "gpu_launches": 6 * args.steps,
         "minimum_image": out["minimum"],
         "work_per_frame": {"pcf_pairs": n5 * (n5 - 1) // 2, "candidate_subunit_pairs": r["candidate_pairs"],
                            "bead_pair_tests_contacts": r["candidate_pairs"] * np_ * np_,
                            "fp64_decisions": r["fp64_pairs"]},
-        "roofline": {"bound": "hbm", "kernel": "whole frame (7 kernels)", "achieved": frame_bytes / (r["ms"] / 1e3) / 1e9,
+        "roofline": {"bound": "hbm", "kernel": "whole frame (6 kernels)", "achieved": frame_bytes / (r["ms"] / 1e3) / 1e9,
                      "peak": peak, "unit": "GB/s", "frac": frame_bytes / (r["ms"] / 1e3) / 1e9 / peak,
                      "traffic": None,
                      "note": "the frame's data is 2.4 MB; the work is FP32 pair tests, so the HBM "

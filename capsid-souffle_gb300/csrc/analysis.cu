@@ -5,18 +5,21 @@
 // The reference grows each oligomer by testing every bead of every unassigned subunit against
 // every bead of the oligomer (O(S^2 np^2) per frame, src/analysis.cpp:140-178) and the pair
 // correlation over all pairs of beads (:117-131).  Here:
-//   k_an_prep        FP32 copies of the positions, union-find roots reset, pcf beads listed
-//   k_an_spheres     per subunit an anchor bead and the radius of the sphere about it that holds
-//                    every bead (minimum image)
-//   k_an_candidates  subunit pairs whose spheres come within the contact distance (all pairs, in
-//                    FP32 with a margin); every separation rule used here is at least the minimum
-//                    image separation, so no contact lies outside these pairs
-//   k_an_contacts    one warp per candidate pair (and per subunit, for pairs inside it): every bead
-//                    pair tested; a contact joins the two subunits, a contact between two so-type
-//                    beads joins the two beads (lock-free union-find, larger root linked under
-//                    smaller, so every component ends with its smallest index as root)
-//   k_an_pcf         all pairs of pcf beads in 256 x 256 tiles, binned into warp-private shared
-//                    histograms
+//   k_an_prep        warp per subunit: FP32 copies of the positions, union-find roots reset, the
+//                    subunit's bounding sphere about its first bead (minimum image), pcf beads
+//                    listed, the output histograms cleared
+//   k_an_candidates  subunit pairs whose spheres come within the contact distance (all pairs, a
+//                    warp per folded pair of rows, FP32 with a margin); every separation rule used
+//                    here is at least the minimum image separation, so no contact lies outside
+//                    these pairs
+//   k_an_contacts    one warp per candidate pair (and per subunit, for pairs inside it), both
+//                    subunits staged in shared memory, each side cut to the beads within reach of
+//                    the other's sphere: bead pairs 32 at a time until a contact joins the
+//                    subunits, then the so-type pairs, each contact joining two beads (lock-free
+//                    union-find, larger root linked under smaller, so every component ends with
+//                    its smallest index as root)
+//   k_an_pcf         all pairs of pcf beads in 128 x 128 tiles of the upper triangle, rejected
+//                    on the squared separation first, binned into warp-private shared histograms
 //   k_an_finish/k_an_hist  roots, component sizes, the two size histograms
 // Comparisons with the contact distance, the pcf cut-off and the bin edges are made in FP32 with
 // an error bound; a pair inside the bound is decided by the FP64 evaluation the reference's
@@ -41,7 +44,13 @@ using souffle::DevBuf;
 
 constexpr int kMaxBeadsPerSubunit = 256;
 constexpr int kContactWarps = 8;           // warps per CTA in k_an_contacts
-constexpr int kTile = 256;                 // tile edge of k_an_candidates and k_an_pcf
+constexpr int kCandWarps = 8;              // warps per CTA in k_an_candidates (two rows each)
+constexpr int kCandBuf = 2048;             // candidate hits gathered per CTA in shared memory
+constexpr int kCandSeg = 256;              // values of k per block in k_an_candidates
+constexpr int kPcfTile = 128;              // tile edge of k_an_pcf
+constexpr int kPrivBins = 128;             // k_an_pcf: per-thread 16-bit histograms up to this many bins
+constexpr int kPrivFlushTiles = 500;       // ... flushed after this many tiles (500 x 128 < 65536)
+constexpr int kHistLocal = 256;            // k_an_hist: size bins counted in shared memory first
 constexpr int kUnionIterLimit = 1 << 22;   // bound on retries of one union (never reached in practice)
 
 // Counter slots.
@@ -78,11 +87,12 @@ __device__ __noinline__ double exact_sep(const double* __restrict__ pos, int a, 
 
 // FP32 squared separation; `unsure` is set when a coordinate difference is too close to zero for
 // FP32 to tell whether the reference rule shifts it.
-__device__ __forceinline__ float sep2_f(float4 p, float4 q, const AnParams& P, bool& unsure) {
+template <int IMAGE>
+__device__ __forceinline__ float sep2_f_t(float4 p, float4 q, const AnParams& P, bool& unsure) {
   const float dx = fabsf(p.x - q.x), dy = fabsf(p.y - q.y), dz = fabsf(p.z - q.z);
   float gx, gy, gz;
-  if (P.image == SOUFFLE_IMAGE_REFERENCE) {
-    unsure |= (dx <= P.tolz) | (dy <= P.tolz) | (dz <= P.tolz);
+  if (IMAGE == SOUFFLE_IMAGE_REFERENCE) {
+    unsure |= fminf(fminf(dx, dy), dz) <= P.tolz;
     gx = P.Lf - dx;
     gy = P.Lf - dy;
     gz = P.Lf - dz;
@@ -92,6 +102,11 @@ __device__ __forceinline__ float sep2_f(float4 p, float4 q, const AnParams& P, b
     gz = dz > P.halff ? P.Lf - dz : dz;
   }
   return gx * gx + gy * gy + gz * gz;
+}
+
+__device__ __forceinline__ float sep2_f(float4 p, float4 q, const AnParams& P, bool& unsure) {
+  return P.image == SOUFFLE_IMAGE_REFERENCE ? sep2_f_t<SOUFFLE_IMAGE_REFERENCE>(p, q, P, unsure)
+                                            : sep2_f_t<SOUFFLE_IMAGE_MINIMUM>(p, q, P, unsure);
 }
 
 // Minimum-image separation squared in FP32 (sphere tests only).
@@ -132,96 +147,185 @@ __device__ void uf_union(int* parent, int a, int b, unsigned int* flags) {
   atomicOr(flags, F_UNION_LIMIT);
 }
 
+// Warp per subunit: FP32 copies of the positions, union-find roots reset, the subunit's bounding
+// sphere (anchor = its first bead, radius = largest minimum-image distance from the anchor to a
+// bead of the subunit, FP32 plus a margin that covers the FP32 rounding), pcf beads appended to
+// their list.
 __global__ void k_an_prep(const double* __restrict__ pos, const int* __restrict__ types, const AnParams P,
-                          float4* __restrict__ posf, int* __restrict__ parent_bead, int* __restrict__ size_bead,
-                          int* __restrict__ parent_sub, int* __restrict__ size_sub, int* __restrict__ pcf_idx,
+                          float4* __restrict__ posf, float4* __restrict__ sph, int* __restrict__ parent_bead,
+                          int* __restrict__ size_bead, int* __restrict__ parent_sub, int* __restrict__ size_sub,
+                          int* __restrict__ pcf_idx, unsigned long long* __restrict__ gr,
+                          unsigned long long* __restrict__ olig, unsigned long long* __restrict__ so,
                           unsigned int* __restrict__ cnt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < P.N) {
-    const int t = types[i];
-    const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-    // the FP32 error bounds and the sphere test assume coordinates inside the box (the MD writes
-    // them wrapped into [-box/2, box/2]); far outside it, report instead of guessing
-    if (!(fabs(x) <= 0.75 * P.L && fabs(y) <= 0.75 * P.L && fabs(z) <= 0.75 * P.L)) atomicOr(cnt + C_FLAGS, F_POS_RANGE);
-    posf[i] = make_float4((float)x, (float)y, (float)z, __int_as_float(t));
-    parent_bead[i] = i;
-    size_bead[i] = 0;
-    // warp-aggregated append of the pcf beads (their order does not matter: the histogram is a
-    // sum over unordered pairs)
-    const bool is_pcf = t == P.pcf_type;
-    const unsigned am = __activemask();
-    const unsigned m = __ballot_sync(am, is_pcf);
-    if (m) {
-      const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-      unsigned base = 0;
-      if (lane == leader) base = atomicAdd(cnt + C_NPCF, __popc(m));
-      base = __shfl_sync(am, base, leader);
-      if (is_pcf) pcf_idx[base + __popc(m & ((1u << lane) - 1))] = i;
-    }
-  }
-  if (i < P.S) {
-    parent_sub[i] = i;
-    size_sub[i] = 0;
-  }
-}
-
-// Warp per subunit: anchor = its first bead; radius = largest minimum-image distance from the
-// anchor to a bead of the subunit, rounded up.
-__global__ void k_an_spheres(const double* __restrict__ pos, const AnParams P, float4* __restrict__ sph) {
   const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (s >= P.S) return;
-  const long a0 = (long)s * P.np;
-  const double ax = pos[3 * a0], ay = pos[3 * a0 + 1], az = pos[3 * a0 + 2];
-  double r2 = 0;
-  for (int b = lane; b < P.np; b += 32) {
-    double d[3] = {pos[3 * (a0 + b)] - ax, pos[3 * (a0 + b) + 1] - ay, pos[3 * (a0 + b) + 2] - az};
-    for (int c = 0; c < 3; c++) {
-      if (d[c] > P.half) d[c] -= P.L;
-      else if (d[c] < -P.half) d[c] += P.L;
-    }
-    r2 = fmax(r2, d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  // the frame's output histograms start at zero (every later kernel runs after this one)
+  if (lane == 0) {
+    olig[s] = 0;
+    so[2 * s] = 0;
+    so[2 * s + 1] = 0;
   }
-  for (int o = 16; o; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
-  if (lane == 0) sph[s] = make_float4((float)ax, (float)ay, (float)az, (float)sqrt(r2) * 1.0001f + P.sph_margin);
+  for (int k = s + lane * P.S; k < P.bins; k += 32 * P.S) gr[k] = 0;
+  const int b0 = s * P.np;
+  float4 anchor = make_float4(0.f, 0.f, 0.f, 0.f);
+  float r2max = 0.f;
+  bool out_of_box = false;
+  for (int base = 0; base < P.np; base += 32) {
+    const int l = base + lane, i = b0 + l;
+    const bool valid = l < P.np;
+    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    int t = 0;
+    if (valid) {
+      t = types[i];
+      const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+      // the FP32 error bounds and the sphere test assume coordinates inside the box (the MD
+      // writes them wrapped into [-box/2, box/2]); far outside it, report instead of guessing
+      out_of_box |= !(fabs(x) <= 0.75 * P.L && fabs(y) <= 0.75 * P.L && fabs(z) <= 0.75 * P.L);
+      f = make_float4((float)x, (float)y, (float)z, __int_as_float(t));
+      posf[i] = f;
+      parent_bead[i] = i;
+      size_bead[i] = 0;
+    }
+    if (base == 0) {
+      anchor.x = __shfl_sync(0xffffffffu, f.x, 0);
+      anchor.y = __shfl_sync(0xffffffffu, f.y, 0);
+      anchor.z = __shfl_sync(0xffffffffu, f.z, 0);
+    }
+    if (valid) r2max = fmaxf(r2max, min_image2_f(f, anchor, P.Lf, P.halff));
+    // warp-aggregated append of the pcf beads (their order does not matter: the histogram is a
+    // sum over unordered pairs)
+    const bool is_pcf = valid && t == P.pcf_type;
+    const unsigned m = __ballot_sync(0xffffffffu, is_pcf);
+    if (m) {
+      unsigned slot = 0;
+      if (lane == 0) slot = atomicAdd(cnt + C_NPCF, __popc(m));
+      slot = __shfl_sync(0xffffffffu, slot, 0);
+      if (is_pcf) pcf_idx[slot + __popc(m & ((1u << lane) - 1))] = i;
+    }
+  }
+  for (int o = 16; o; o >>= 1) r2max = fmaxf(r2max, __shfl_xor_sync(0xffffffffu, r2max, o));
+  if (__any_sync(0xffffffffu, out_of_box) && lane == 0) atomicOr(cnt + C_FLAGS, F_POS_RANGE);
+  if (lane == 0) {
+    sph[s] = make_float4(anchor.x, anchor.y, anchor.z, sqrtf(r2max) * 1.0001f + P.sph_margin);
+    parent_sub[s] = s;
+    size_sub[s] = 0;
+  }
 }
 
-// All subunit pairs i < k in 256 x 256 tiles (grid-stride over tile pairs): a pair whose spheres
-// come closer than the contact distance (plus the FP32 margin) is a candidate.
-__global__ void __launch_bounds__(kTile) k_an_candidates(const float4* __restrict__ sph, const AnParams P,
-                                                         int2* __restrict__ cand, unsigned int* __restrict__ cnt) {
-  __shared__ float4 tile[kTile];
-  const int T = (P.S + kTile - 1) / kTile;
-  for (long t = blockIdx.x; t < (long)T * T; t += gridDim.x) {
-    const int ti = (int)(t / T), tk = (int)(t % T);
-    if (tk < ti) continue;
-    __syncthreads();
-    const int kk = tk * kTile + threadIdx.x;
-    if (kk < P.S) tile[threadIdx.x] = sph[kk];
-    __syncthreads();
-    const int i = ti * kTile + threadIdx.x;
-    if (i >= P.S) continue;
+// Subunit pairs i < k whose spheres come closer than the contact distance (plus the FP32 margin):
+// the candidates.  Warp per pair of rows, folded (warp w takes rows w and S-1-w) so every warp has
+// the same share of pairs; blockIdx.y selects a segment of kCandSeg values of k, staged in shared
+// memory.  Hits are gathered in shared memory and reserved in the global list with one atomic per
+// block.
+__global__ void __launch_bounds__(kCandWarps * 32) k_an_candidates(const float4* __restrict__ sph, const AnParams P,
+                                                                   int2* __restrict__ cand,
+                                                                   unsigned int* __restrict__ cnt) {
+  __shared__ float4 seg[kCandSeg];
+  __shared__ int2 hits[kCandBuf];
+  __shared__ unsigned n_hits, base;
+  const int lane = threadIdx.x & 31;
+  const int w = blockIdx.x * kCandWarps + (threadIdx.x >> 5);
+  const int c0 = blockIdx.y * kCandSeg, c1 = min(P.S, c0 + kCandSeg);
+  // rows of this block lie in [first, S - first); a segment at or below its smallest row has nothing
+  const int first = blockIdx.x * kCandWarps;
+  if (c1 <= first + 1) return;
+  const bool active = w < (P.S + 1) / 2;  // warps past the fold have no rows
+  const int row0 = w, row1 = P.S - 1 - w;
+  const bool two = active && row1 > row0;
+  if (threadIdx.x == 0) n_hits = 0;
+  for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) seg[k - c0] = sph[k];
+  __syncthreads();
+  for (int r = 0; r < 2; r++) {
+    if (!(r == 0 ? active : two)) continue;
+    const int i = r == 0 ? row0 : row1;
     const float4 si = sph[i];
-    const int kend = min(kTile, P.S - tk * kTile);
-    const int kbeg = tk == ti ? threadIdx.x + 1 : 0;
-    for (int k = kbeg; k < kend; k++) {
-      const float4 sk = tile[k];
-      const float reach = si.w + sk.w + P.contact;
-      if (min_image2_f(si, sk, P.Lf, P.halff) < reach * reach) {
-        const unsigned slot = atomicAdd(cnt + C_NCAND, 1u);
-        if (slot < (unsigned)P.cap) cand[slot] = make_int2(i, tk * kTile + k);
-        else atomicOr(cnt + C_FLAGS, F_CAND_OVERFLOW);
+    for (int kb = max(c0, i + 1); kb < c1; kb += 128) {
+      // four independent tests per lane, then the (rare) hits
+      bool hit[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int k = kb + lane + 32 * j;
+        hit[j] = false;
+        if (k < c1) {
+          const float4 sk = seg[k - c0];
+          const float reach = si.w + sk.w + P.contact;
+          hit[j] = min_image2_f(si, sk, P.Lf, P.halff) < reach * reach;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        if (!hit[j]) continue;
+        const int k = kb + lane + 32 * j;
+        const unsigned slot = atomicAdd(&n_hits, 1u);
+        if (slot < kCandBuf) {
+          hits[slot] = make_int2(i, k);
+        } else {  // a very dense block: straight to the global list
+          const unsigned g = atomicAdd(cnt + C_NCAND, 1u);
+          if (g < (unsigned)P.cap) cand[g] = make_int2(i, k);
+          else atomicOr(cnt + C_FLAGS, F_CAND_OVERFLOW);
+        }
       }
     }
   }
+  __syncthreads();
+  const unsigned nh = min(n_hits, (unsigned)kCandBuf);
+  if (threadIdx.x == 0 && nh) base = atomicAdd(cnt + C_NCAND, nh);
+  __syncthreads();
+  for (unsigned h = threadIdx.x; h < nh; h += blockDim.x) {
+    if (base + h < (unsigned)P.cap) cand[base + h] = hits[h];
+    else atomicOr(cnt + C_FLAGS, F_CAND_OVERFLOW);
+  }
+}
+
+// Local indices of the beads of a staged subunit that satisfy `keep`, ascending, into list;
+// returns their number.  Whole warp.
+template <class Keep>
+__device__ __forceinline__ int warp_select(const float4* beads, int np, Keep keep, unsigned char* list) {
+  const int lane = threadIdx.x & 31;
+  int n = 0;
+  for (int base = 0; base < np; base += 32) {
+    const int l = base + lane;
+    const bool k = l < np && keep(beads[l]);
+    const unsigned m = __ballot_sync(0xffffffffu, k);
+    if (k) list[n + __popc(m & ((1u << lane) - 1))] = (unsigned char)l;
+    n += __popc(m);
+  }
+  __syncwarp();
+  return n;
+}
+
+// Contact of bead a (global index ga) and bead b (global gb) from their FP32 copies; decided in
+// FP64 where FP32 cannot tell.
+__device__ __forceinline__ bool contact_test(const float4 pa, const float4 pb, const double* __restrict__ pos, int ga,
+                                             int gb, const AnParams& P, unsigned& fp64) {
+  bool unsure = false;
+  const float r2 = sep2_f(pa, pb, P, unsure);
+  if (!unsure && r2 < P.lo2) return true;
+  if (!unsure && r2 >= P.hi2) return false;
+  fp64++;
+  return exact_sep(pos, ga, gb, P) < P.contact;
 }
 
 // Warp per work item: items [0, n_cand) are candidate subunit pairs, items [n_cand, n_cand + S)
 // are single subunits (pairs of beads inside one subunit, which only matter for sub-oligomers).
-__global__ void __launch_bounds__(kContactWarps * 32)
-    k_an_contacts(const double* __restrict__ pos, const float4* __restrict__ posf, const int2* __restrict__ cand,
-                  const AnParams P, int* parent_sub, int* parent_bead, unsigned int* __restrict__ cnt) {
-  __shared__ float4 sb[kContactWarps][kMaxBeadsPerSubunit];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+// Both subunits are staged in shared memory.  For a pair item only beads within reach of the other
+// subunit's sphere can touch it (every separation rule here is at least the minimum image), so
+// each side is cut to those beads first; their pairs are scanned 32 at a time until a contact
+// joins the subunits, then the so-type pairs among them are tested, each contact joining two
+// beads.
+__global__ void __launch_bounds__(kContactWarps * 32, 5)
+    k_an_contacts(const double* __restrict__ pos, const float4* __restrict__ posf, const float4* __restrict__ sph,
+                  const int2* __restrict__ cand, const AnParams P, int* parent_sub, int* parent_bead,
+                  unsigned int* __restrict__ cnt) {
+  extern __shared__ float4 stage[];  // [kContactWarps][2][np]
+  __shared__ unsigned char sel[kContactWarps][4][kMaxBeadsPerSubunit];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, np = P.np;
+  float4* A = stage + (size_t)wid * 2 * np;
+  float4* B = A + np;
+  unsigned char* la = sel[wid][0];
+  unsigned char* lb = sel[wid][1];
+  unsigned char* sa = sel[wid][2];
+  unsigned char* sb = sel[wid][3];
   const int n_cand = (int)min(__ldcg(cnt + C_NCAND), (unsigned)P.cap);
   const long items = (long)n_cand + P.S;
   unsigned fp64 = 0;
@@ -235,82 +339,145 @@ __global__ void __launch_bounds__(kContactWarps * 32)
       si = c.x;
       sk = c.y;
     }
-    const int bi = si * P.np, bk = sk * P.np;
+    const int bi = si * np, bk = sk * np;
     __syncwarp();
-    for (int b = lane; b < P.np; b += 32) sb[wid][b] = posf[bk + b];
+    for (int b = lane; b < np; b += 32) {
+      A[b] = posf[bi + b];
+      if (!self) B[b] = posf[bk + b];
+    }
     __syncwarp();
-    // self items only look for so-type contacts; pair items look for any contact until found
-    bool joined = self;
-    for (int a = 0; a < P.np; a++) {
-      const float4 pa = posf[bi + a];
-      const bool a_so = type_of(pa) == P.so_type;
-      if (joined && !a_so) continue;
-      bool hit_any = false;
-      for (int b = self ? a + 1 + lane : lane; b < P.np; b += 32) {
-        const float4 pb = sb[wid][b];
-        const bool pair_so = a_so && type_of(pb) == P.so_type;
-        if (joined && !pair_so) continue;
-        bool unsure = false;
-        const float r2 = sep2_f(pa, pb, P, unsure);
-        bool hit;
-        if (!unsure && r2 < P.lo2) hit = true;
-        else if (!unsure && r2 >= P.hi2) hit = false;
-        else {
-          hit = exact_sep(pos, bi + a, bk + b, P) < P.contact;
-          fp64++;
+    if (self) {
+      const int na = warp_select(A, np, [&](float4 p) { return type_of(p) == P.so_type; }, sa);
+      for (int t = lane; t < na * na; t += 32) {
+        const int x = sa[t / na], y = sa[t % na];
+        if (y <= x) continue;
+        if (contact_test(A[x], A[y], pos, bi + x, bi + y, P, fp64)) uf_union(parent_bead, bi + x, bi + y, cnt + C_FLAGS);
+      }
+      continue;
+    }
+    // beads of each side within reach of the other side's sphere
+    const float4 ci = sph[si], ck = sph[sk];
+    const float ri = ci.w + P.contact, rk = ck.w + P.contact;
+    const int na = warp_select(A, np, [&](float4 p) { return min_image2_f(p, ck, P.Lf, P.halff) < rk * rk; }, la);
+    const int nb = warp_select(B, np, [&](float4 p) { return min_image2_f(p, ci, P.Lf, P.halff) < ri * ri; }, lb);
+    const int nab = na * nb;
+    bool joined = false;
+    if (nab > 0) {
+      int x = lane / nb, y = lane % nb;  // pair t = x * nb + y, tracked as t advances by 32
+      const int sx = 32 / nb, sy = 32 % nb;
+      for (int base = 0; base < nab && !joined; base += 32) {
+        bool hit = false;
+        if (base + lane < nab) {
+          const int a = la[x], b = lb[y];
+          hit = contact_test(A[a], B[b], pos, bi + a, bk + b, P, fp64);
         }
-        if (hit) {
-          hit_any = true;
-          if (pair_so) uf_union(parent_bead, bi + a, bk + b, cnt + C_FLAGS);
+        joined = __any_sync(0xffffffffu, hit);
+        x += sx;
+        y += sy;
+        if (y >= nb) {
+          y -= nb;
+          x++;
         }
       }
-      if (!joined && __any_sync(0xffffffffu, hit_any)) {
-        joined = true;
-        if (lane == 0) uf_union(parent_sub, si, sk, cnt + C_FLAGS);
-      }
+    }
+    if (!joined) continue;  // no contact: no so-type contact either
+    if (lane == 0) uf_union(parent_sub, si, sk, cnt + C_FLAGS);
+    const int ma = warp_select(A, np, [&](float4 p) {
+      return type_of(p) == P.so_type && min_image2_f(p, ck, P.Lf, P.halff) < rk * rk; }, sa);
+    const int mb = warp_select(B, np, [&](float4 p) {
+      return type_of(p) == P.so_type && min_image2_f(p, ci, P.Lf, P.halff) < ri * ri; }, sb);
+    for (int t = lane; t < ma * mb; t += 32) {
+      const int a = sa[t / mb], b = sb[t % mb];
+      if (contact_test(A[a], B[b], pos, bi + a, bk + b, P, fp64)) uf_union(parent_bead, bi + a, bk + b, cnt + C_FLAGS);
     }
   }
   if (fp64) atomicAdd(cnt + C_FP64, fp64);
 }
 
-// All pairs of pcf beads, 256 x 256 tiles, warp-private histograms in shared memory.
-__global__ void __launch_bounds__(kTile) k_an_pcf(const double* __restrict__ pos, const float4* __restrict__ posf,
-                                                  const int* __restrict__ pcf_idx, const AnParams P,
-                                                  unsigned long long* __restrict__ gr, unsigned int* __restrict__ cnt) {
-  extern __shared__ unsigned int hist[];  // copies x bins
-  __shared__ float4 tile[kTile];
-  __shared__ int tidx[kTile];
-  const int copies = P.bins <= 512 ? kTile / 32 : 1;
+// All pairs of pcf beads, kPcfTile x kPcfTile tiles over the upper triangle (grid-stride).  Pairs
+// past the cut-off are rejected on the squared separation before any square root.  With at most
+// kPrivBins bins every thread counts into its own 16-bit histogram column in shared memory (no
+// atomics, no bank conflicts), flushed to the global histogram before a count could wrap; with
+// more bins, warp-private 32-bit histograms with shared atomics.
+template <int IMAGE>
+__global__ void __launch_bounds__(kPcfTile) k_an_pcf(const double* __restrict__ pos, const float4* __restrict__ posf,
+                                                     const int* __restrict__ pcf_idx, const AnParams P,
+                                                     unsigned long long* __restrict__ gr, unsigned int* __restrict__ cnt) {
+  extern __shared__ unsigned int hist[];
+  __shared__ float4 tile[kPcfTile];
+  __shared__ int tidx[kPcfTile];
+  const bool priv = IMAGE == SOUFFLE_IMAGE_MINIMUM && P.bins <= kPrivBins;
+  unsigned short* ph = reinterpret_cast<unsigned short*>(hist);  // [bins][kPcfTile] when priv
+  const int copies = priv ? 0 : (P.bins <= 512 ? kPcfTile / 32 : 1);
   unsigned int* h = hist + (copies > 1 ? (threadIdx.x >> 5) * P.bins : 0);
-  for (int k = threadIdx.x; k < copies * P.bins; k += blockDim.x) hist[k] = 0;
-  const int n = (int)__ldcg(cnt + C_NPCF);
-  const int T = (n + kTile - 1) / kTile;
-  unsigned fp64 = 0;
-  for (long t = blockIdx.x; t < (long)T * T; t += gridDim.x) {
-    const int ti = (int)(t / T), tk = (int)(t % T);
-    if (tk < ti) continue;
+  const int words = priv ? P.bins * kPcfTile / 2 : copies * P.bins;
+  for (int k = threadIdx.x; k < words; k += blockDim.x) hist[k] = 0;
+  // adds the shared counts to the global histogram and clears them (whole block)
+  auto flush = [&]() {
     __syncthreads();
-    const int kk = tk * kTile + threadIdx.x;
+    if (priv) {  // warp per bin, lanes along the bin's row (conflict-free)
+      const int lane = threadIdx.x & 31;
+      for (int k = threadIdx.x >> 5; k < P.bins; k += kPcfTile / 32) {
+        unsigned s = 0;
+        for (int c = lane; c < kPcfTile; c += 32) {
+          s += ph[k * kPcfTile + c];
+          ph[k * kPcfTile + c] = 0;
+        }
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0 && s) atomicAdd(gr + k, (unsigned long long)s);
+      }
+    } else {
+      for (int k = threadIdx.x; k < P.bins; k += blockDim.x) {
+        unsigned long long s = 0;
+        for (int c = 0; c < copies; c++) {
+          s += hist[c * P.bins + k];
+          hist[c * P.bins + k] = 0;
+        }
+        if (s) atomicAdd(gr + k, s);
+      }
+    }
+  };
+  const int n = (int)__ldcg(cnt + C_NPCF);
+  const long T = (n + kPcfTile - 1) / kPcfTile;
+  const long n_tiles = T * (T + 1) / 2;
+  const float far2 = (P.halff + P.tol_r) * (P.halff + P.tol_r);
+  unsigned fp64 = 0;
+  int tiles_since_flush = 0;
+  for (long t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    // upper-triangle index t -> (ti, tk), ti <= tk, row by row
+    long ti = (long)((2 * T + 1 - sqrt((double)(2 * T + 1) * (2 * T + 1) - 8.0 * t)) / 2);
+    while (ti > 0 && ti * T - ti * (ti - 1) / 2 > t) ti--;
+    while ((ti + 1) * T - (ti + 1) * ti / 2 <= t) ti++;
+    const long tk = ti + (t - (ti * T - ti * (ti - 1) / 2));
+    if (priv && ++tiles_since_flush > kPrivFlushTiles) {  // each tile adds at most kPcfTile to a count
+      flush();
+      tiles_since_flush = 1;
+    }
+    __syncthreads();
+    const long kk = tk * kPcfTile + threadIdx.x;
     if (kk < n) {
       tidx[threadIdx.x] = pcf_idx[kk];
       tile[threadIdx.x] = posf[tidx[threadIdx.x]];
     }
     __syncthreads();
-    const int ii = ti * kTile + threadIdx.x;
+    const long ii = ti * kPcfTile + threadIdx.x;
     if (ii >= n) continue;
     const int gi = pcf_idx[ii];
     const float4 pi = posf[gi];
-    const int kend = min(kTile, n - tk * kTile);
+    const int kend = (int)min((long)kPcfTile, n - tk * kPcfTile);
+#pragma unroll 4
     for (int k = tk == ti ? threadIdx.x + 1 : 0; k < kend; k++) {
       bool unsure = false;
-      const float r = sqrtf(sep2_f(pi, tile[k], P, unsure));
+      const float r2 = sep2_f_t<IMAGE>(pi, tile[k], P, unsure);
+      if (!unsure && r2 >= far2) continue;
+      const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
       int bin = -1;
       if (!unsure && r < P.halff - P.tol_r) {
         const float x = r * P.inv_dgf;
         const float f = floorf(x);
         if (x - f >= P.tol_bin && x - f <= 1.0f - P.tol_bin) bin = (int)f;
         else unsure = true;
-      } else if (!unsure && r < P.halff + P.tol_r) {
+      } else {
         unsure = true;
       }
       if (unsure) {
@@ -321,15 +488,14 @@ __global__ void __launch_bounds__(kTile) k_an_pcf(const double* __restrict__ pos
           bin = b < (double)P.bins ? (int)b : -1;  // r/dg rounding up to bins: past the reference's histogram
         }
       }
-      if (bin >= 0) atomicAdd(h + min(bin, P.bins - 1), 1u);
+      if (bin >= 0) {
+        bin = min(bin, P.bins - 1);
+        if (priv) ph[bin * kPcfTile + threadIdx.x] += 1;
+        else atomicAdd(h + bin, 1u);
+      }
     }
   }
-  __syncthreads();
-  for (int k = threadIdx.x; k < P.bins; k += blockDim.x) {
-    unsigned long long s = 0;
-    for (int c = 0; c < copies; c++) s += hist[c * P.bins + k];
-    if (s) atomicAdd(gr + k, s);
-  }
+  flush();
   if (fp64) atomicAdd(cnt + C_FP64, fp64);
 }
 
@@ -346,16 +512,32 @@ __global__ void k_an_finish(const float4* __restrict__ posf, const AnParams P, i
 }
 
 // Size histograms: oligomers of k + 1 subunits; sub-oligomers in bins of three beads.
-__global__ void k_an_hist(const float4* __restrict__ posf, const AnParams P, const int* __restrict__ labels,
-                          const int* __restrict__ size_sub, const int* __restrict__ parent_bead,
-                          const int* __restrict__ size_bead, unsigned long long* __restrict__ olig,
-                          unsigned long long* __restrict__ so, unsigned int* __restrict__ cnt) {
+__global__ void __launch_bounds__(256) k_an_hist(const float4* __restrict__ posf, const AnParams P,
+                                                 const int* __restrict__ labels, const int* __restrict__ size_sub,
+                                                 const int* __restrict__ parent_bead, const int* __restrict__ size_bead,
+                                                 unsigned long long* __restrict__ olig, unsigned long long* __restrict__ so,
+                                                 unsigned int* __restrict__ cnt) {
+  // most components are small: their bins are counted in shared memory first, so that thousands
+  // of single subunits or beads do not queue on one global counter
+  __shared__ unsigned lo[kHistLocal], ls[kHistLocal];
+  for (int k = threadIdx.x; k < kHistLocal; k += blockDim.x) lo[k] = ls[k] = 0;
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < P.S && labels[i] == i) atomicAdd(olig + size_sub[i] - 1, 1ull);
+  if (i < P.S && labels[i] == i) {
+    const int bin = size_sub[i] - 1;
+    if (bin < kHistLocal) atomicAdd(lo + bin, 1u);
+    else atomicAdd(olig + bin, 1ull);
+  }
   if (i < P.N && type_of(posf[i]) == P.so_type && parent_bead[i] == i) {
     const int bin = (size_bead[i] - 1) / 3;
-    if (bin < 2 * P.S) atomicAdd(so + bin, 1ull);
-    else atomicOr(cnt + C_FLAGS, F_SO_OVERFLOW);
+    if (bin >= 2 * P.S) atomicOr(cnt + C_FLAGS, F_SO_OVERFLOW);
+    else if (bin < kHistLocal) atomicAdd(ls + bin, 1u);
+    else atomicAdd(so + bin, 1ull);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kHistLocal; k += blockDim.x) {
+    if (lo[k]) atomicAdd(olig + k, (unsigned long long)lo[k]);
+    if (ls[k]) atomicAdd(so + k, (unsigned long long)ls[k]);
   }
 }
 
@@ -380,6 +562,7 @@ struct souffle_analysis {
   DevBuf<unsigned int> cnt;
   DevBuf<unsigned long long> gr, olig, so;
   unsigned int* cnt_host = nullptr;  // pinned copy of the counters of the last enqueued frame
+  size_t contact_smem = 0;           // dynamic shared memory of k_an_contacts (two staged subunits per warp)
   bool have_types = false;
 };
 
@@ -413,25 +596,27 @@ souffle_status enqueue(souffle_analysis* h, const double* pos, const int* types,
   const AnParams& P = h->P;
   cudaStream_t st = h->st;
   AN_CHECK(cudaMemsetAsync(h->cnt.p, 0, sizeof(unsigned int) * C_COUNT, st));
-  AN_CHECK(cudaMemsetAsync(gr, 0, sizeof(unsigned long long) * P.bins, st));
-  AN_CHECK(cudaMemsetAsync(olig, 0, sizeof(unsigned long long) * P.S, st));
-  AN_CHECK(cudaMemsetAsync(so, 0, sizeof(unsigned long long) * 2 * P.S, st));
   const int nmax = std::max(P.N, P.S);
-  k_an_prep<<<(nmax + 255) / 256, 256, 0, st>>>(pos, types, P, h->posf.p, h->parent_bead.p, h->size_bead.p,
-                                                 h->parent_sub.p, h->size_sub.p, h->pcf_idx.p, h->cnt.p);
-  k_an_spheres<<<(P.S + 7) / 8, 256, 0, st>>>(pos, P, h->sph.p);
-  const long T = (P.S + kTile - 1) / kTile;
-  const int gcand = (int)std::min<long>(T * T, 4L * h->sms);
-  k_an_candidates<<<gcand, kTile, 0, st>>>(h->sph.p, P, h->cand.p, h->cnt.p);
+  k_an_prep<<<(P.S + 7) / 8, 256, 0, st>>>(pos, types, P, h->posf.p, h->sph.p, h->parent_bead.p, h->size_bead.p,
+                                            h->parent_sub.p, h->size_sub.p, h->pcf_idx.p, gr, olig, so, h->cnt.p);
+  const int cand_warps = (P.S + 1) / 2;
+  const dim3 gcand((cand_warps + kCandWarps - 1) / kCandWarps, (P.S + kCandSeg - 1) / kCandSeg);
+  k_an_candidates<<<gcand, kCandWarps * 32, 0, st>>>(h->sph.p, P, h->cand.p, h->cnt.p);
   const long items_max = (long)P.cap + P.S;
   const int gcon = (int)std::min<long>((items_max + kContactWarps - 1) / kContactWarps, 8L * h->sms);
-  k_an_contacts<<<gcon, kContactWarps * 32, 0, st>>>(pos, h->posf.p, h->cand.p, P, h->parent_sub.p,
-                                                     h->parent_bead.p, h->cnt.p);
-  const long Tp = (P.N + kTile - 1) / kTile;
-  const int gpcf = (int)std::min<long>(Tp * Tp, 4L * h->sms);
-  const int copies = P.bins <= 512 ? kTile / 32 : 1;
-  k_an_pcf<<<gpcf, kTile, sizeof(unsigned int) * copies * P.bins, st>>>(pos, h->posf.p, h->pcf_idx.p, P, gr,
-                                                                        h->cnt.p);
+  k_an_contacts<<<gcon, kContactWarps * 32, h->contact_smem, st>>>(pos, h->posf.p, h->sph.p, h->cand.p, P,
+                                                                   h->parent_sub.p, h->parent_bead.p, h->cnt.p);
+  const long Tp = (P.N + kPcfTile - 1) / kPcfTile;
+  const int gpcf = (int)std::min<long>(Tp * (Tp + 1) / 2, 8L * h->sms);
+  // the reference rule counts few pairs (those the long way round is short for), the minimum image
+  // about half of all pairs: per-thread histograms only pay off for the latter
+  const size_t pcf_smem = P.image == SOUFFLE_IMAGE_MINIMUM && P.bins <= kPrivBins
+                              ? sizeof(unsigned short) * P.bins * kPcfTile
+                              : sizeof(unsigned int) * (P.bins <= 512 ? kPcfTile / 32 : 1) * P.bins;
+  if (P.image == SOUFFLE_IMAGE_REFERENCE)
+    k_an_pcf<SOUFFLE_IMAGE_REFERENCE><<<gpcf, kPcfTile, pcf_smem, st>>>(pos, h->posf.p, h->pcf_idx.p, P, gr, h->cnt.p);
+  else
+    k_an_pcf<SOUFFLE_IMAGE_MINIMUM><<<gpcf, kPcfTile, pcf_smem, st>>>(pos, h->posf.p, h->pcf_idx.p, P, gr, h->cnt.p);
   k_an_finish<<<(nmax + 255) / 256, 256, 0, st>>>(h->posf.p, P, h->parent_sub.p, h->parent_bead.p,
                                                    h->size_sub.p, h->size_bead.p, labels);
   k_an_hist<<<(nmax + 255) / 256, 256, 0, st>>>(h->posf.p, P, labels, h->size_sub.p, h->parent_bead.p,
@@ -519,7 +704,10 @@ souffle_status souffle_analysis_create(int64_t n_beads, int32_t beads_per_subuni
   P.tol_bin = (float)(P.tol_r / P.dg + 4e-6 * (o.pcf_bins + 1));
   P.sph_margin = (float)(8 * tol + 1e-4);
   P.cap = std::max(4096, 32 * P.S);
-  cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  h->contact_smem = sizeof(float4) * 2 * kContactWarps * (size_t)P.np;
+  cudaError_t e = cudaFuncSetAttribute(k_an_contacts, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)h->contact_smem);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   const size_t N = (size_t)P.N, S = (size_t)P.S;
   if (e == cudaSuccess) e = h->pos.alloc(3 * N);
   if (e == cudaSuccess) e = h->types.alloc(N);

@@ -123,6 +123,23 @@ def test_other_subunit_sizes_types_and_bins():
     _check_frames(frames, L, np_, ao.IMAGE_REFERENCE, pcf_type=0, pcf_bins=7, so_type=5, contact=2.5)
 
 
+@pytest.mark.parametrize("np_", [1, 3, 10, 32, 33, 100])
+def test_subunit_sizes_around_the_warp_width(np_):
+    """The contact kernel walks np x np bead pairs 32 at a time; sizes below, at and above the
+    warp width, with random types, against the oracle under both rules."""
+    rng = np.random.default_rng(np_)
+    S, L = max(6, 2400 // np_), 24.0
+    off = rng.uniform(-1.2, 1.2, (np_, 3))
+    t = rng.choice(np.array([0, 1, 5], dtype=np.int32), size=np_, p=[0.1, 0.7, 0.2] if np_ > 10 else None)
+    centres = rng.uniform(-L / 2, L / 2, (S, 3))
+    centres[1::2] = centres[0::2][: len(centres[1::2])] + rng.normal(0, 1.5, (len(centres[1::2]), 3))
+    p = (centres[:, None, :] + off[None]).reshape(-1, 3)
+    p = (p + L / 2) % L - L / 2
+    types = np.tile(t, S)
+    for image in (ao.IMAGE_REFERENCE, ao.IMAGE_MINIMUM):
+        _check_frames([(types, p)], L, np_, image)
+
+
 def test_edge_cases():
     from souffle_gb300.gpu import SouffleError
 

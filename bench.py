@@ -121,7 +121,10 @@ def bench_replicas(args):
     import torch
     from souffle_gb300 import gpu, workloads
     t0 = time.perf_counter()
-    reps = workloads.replicas(args.replicas, seed=2024)
+    if args.replica_subunits:
+        reps = workloads.uniform_replicas(args.replicas, args.replica_subunits)
+    else:
+        reps = workloads.replicas(args.replicas, seed=2024)
     gen_s = time.perf_counter() - t0
     params = [gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local) for w in reps]
     s = gpu.GpuSystem(reps[0].template, params)
@@ -143,8 +146,21 @@ def bench_replicas(args):
     e1.record(ext)
     s.synchronize()
     ms = e0.elapsed_time(e1)
+    a += k
+    prof = s.md_profile(a, 20)
     sizes = [int(w.opt.S) for w in reps]
     lens = [s.pairlist_stats(i)["mean_length"] for i in range(0, len(reps), max(1, len(reps) // 16))]
+    n_bar = float(np.mean(lens))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    value = n * k / (ms / 1e3)
+    forces_ms = prof["forces_ms"] / prof["steps"]
+    kern_gbs = (16 + 4 * n_bar + 24 + 48 + 16) * n / (forces_ms / 1e3) / 1e9
+    step_b = 112 + 4 * n_bar + (4 * n_bar + 16) / B
     print(json.dumps({
         "metric": "bead-steps/s", "value": n * k / (ms / 1e3), "unit": "bead-steps/s", "n_gpus": 1,
         "steps": k, "warmup": args.warmup, "ms_per_step": ms / k, "higher_is_better": True,
@@ -153,7 +169,14 @@ def bench_replicas(args):
         "config": {"workload": f"replicas: {len(reps)} systems of bilayer capsomeres, {sum(sizes)} "
                                f"subunits, {n} beads, subunits per system {min(sizes)}-{max(sizes)}",
                    "l2": "working set larger than L2" if n * 300 > 129e6 else "warm L2, whole windows"},
-        "pairlist_mean_length_sampled": float(np.mean(lens)), "generation_s": gen_s,
+        "pairlist_mean_length_sampled": n_bar, "generation_s": gen_s,
+        "kernels_ms": {"k_forces": forces_ms, "k_drift": prof["drift_ms"] / prof["steps"],
+                       "rebuild": prof["rebuild_ms"] / max(1, prof["rebuilds"])},
+        "roofline": {"bound": "hbm", "kernel": "k_forces", "achieved": kern_gbs, "peak": peak,
+                     "unit": "GB/s", "frac": kern_gbs / peak, "traffic": None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800"},
+        "roofline_step": {"achieved": step_b * value / 1e9, "peak": peak, "unit": "GB/s",
+                          "frac": step_b * value / 1e9 / peak, "bytes_per_bead_step": step_b},
         "autotune": tuning}))
 
 
@@ -182,13 +205,13 @@ def bench_surrogate(args):
     import torch
     from souffle_gb300 import gpu, workloads
     torch.cuda.set_device(0)
-    w = workloads.plain_large(args.subunits)
+    w = workloads.plain_large(args.subunits, debye_length=args.debye_length, conc_um=args.concentration)
     p = gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local)
     s = gpu.GpuSystem(w.template, [p])
     s.set_state(w.state.pos, w.state.vel)
     np_ = w.template.n_beads
     n_out = 6 + 3 * np_
-    far_cap = max(4096, 4 * int(w.opt.S))
+    far_cap = max(4096, args.far_per_subunit * int(w.opt.S))
     batch = 4096
     net = gpu.Mlp(64, n_out, max_batch=max(far_cap, batch), seed=7)
     gpu.surrogate_attach(s, net, w.template.pos, far_capacity=far_cap)
@@ -270,7 +293,8 @@ def bench_surrogate(args):
         "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 network (fp32 accumulate) + f32/i64 exact path", "data": "synthetic",
         "config": {"workload": f"plain_large: {args.subunits} bilayer capsomeres x 42 beads = {w.n_beads} "
-                               f"beads, 800 uM, switch radius 3.5 sigma (closest bead pair), judge 1 % "
+                               f"beads, {w.opt.C:g} uM, Debye length {1 / w.derived.kappa:.3g} sigma (-c {w.opt.c:.4g}), "
+                               f"switch radius 3.5 sigma (closest bead pair), judge 1 % "
                                f"of far pairs every 100 steps",
                    "l2": "flushed (256 MB write) before every timed step"},
         "plain": plain, "surrogate": surr, "gain": surr["value"] / plain["value"],
@@ -278,6 +302,173 @@ def bench_surrogate(args):
         "force_rms_rel_error": rms, "far_pairs": far_pairs,
         "training": {"rows": total, "frames": frames, "epochs": args.epochs, "batch": batch,
                      "final_loss_normalised": loss, "generation_s": gen_s, "fit_s": fit_s}}))
+
+
+def bench_surrogate_batched(args):
+    """Surrogate + batching against the plain GPU path on the replica sweep: 256 independent
+    systems of 20-500 bilayer capsomeres with per-system attraction, screening length (0.5-2
+    sigma) and concentration (200-1600 uM).  One network is trained on exact far-pair data from
+    the batched run (the descriptor carries the screening length and attraction), then:
+      plain     every replica alone in its own handle with exact forces (the plain GPU path, one
+                system per run), L2 flushed before each replica's timed window;
+      batched   all replicas in one handle, exact forces;
+      surrogate all replicas in one handle, far subunit pairs from the network.
+    Batched windows run whole rebuild windows as CUDA graphs; their working set is larger than
+    L2.  Also reported: total-force RMS error of the surrogate batch against exact forces at the
+    same state, and temperature and potential-energy statistics of the systems with the longest
+    screening lengths, exact against surrogate."""
+    import numpy as np
+    import torch
+    from souffle_gb300 import gpu, workloads
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    reps = workloads.replicas(args.replicas, seed=2024)
+    gen_s = time.perf_counter() - t0
+    params = [gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local) for w in reps]
+    tpl = reps[0].template
+    s = gpu.GpuSystem(tpl, params)
+    pos0 = np.concatenate([w.state.pos for w in reps])
+    vel0 = np.concatenate([w.state.vel for w in reps])
+    s.set_state(pos0, vel0)
+    n = s.n
+    S_tot = sum(int(w.opt.S) for w in reps)
+    B = int(reps[0].opt.B)
+    np_ = tpl.n_beads
+    n_out = 6 + 3 * np_
+    far_cap = max(4096, args.far_per_subunit * S_tot)
+    batch = 4096
+    net = gpu.Mlp(64, n_out, max_batch=max(far_cap, batch), seed=7)
+    gpu.surrogate_attach(s, net, tpl.pos, far_capacity=far_cap)
+    ext = torch.cuda.ExternalStream(s.stream())
+
+    rows = args.train_rows
+    X = torch.empty(rows, 64, device="cuda")
+    T = torch.empty(rows, n_out, device="cuda")
+    xb = torch.empty(far_cap, 64, device="cuda")
+    tb = torch.empty(far_cap, n_out, device="cuda")
+    s.md_begin()
+    t0 = time.perf_counter()
+    total, frames, a = 0, 0, 0
+    while total < rows and frames < args.max_frames:
+        m = gpu.surrogate_collect(s, xb.data_ptr(), tb.data_ptr(), far_cap)
+        # a sample of each frame's pairs, so that the data set spans more of the trajectory
+        keep = min(m, rows - total, max(1, rows // 20))
+        idx = torch.randperm(m, device="cuda")[:keep] if m > keep else torch.arange(m, device="cuda")
+        X[total:total + keep] = xb[idx]
+        T[total:total + keep] = tb[idx]
+        total += keep
+        frames += 1
+        s.md_steps(a, B)
+        a += B
+    torch.cuda.synchronize()
+    collect_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = gpu.surrogate_fit(s, X.data_ptr(), T.data_ptr(), total, args.epochs, batch, 1e-3, seed=11)
+    fit_s = time.perf_counter() - t0
+    del X, T, xb, tb
+    torch.cuda.empty_cache()
+    pos, vel = s.get_state()
+    exact = s.forces(rebuild=True)
+    gpu.surrogate_enable(s, True)
+    sur = s.forces(rebuild=True)
+    far_pairs = gpu.surrogate_stats(s)["far_pairs"]
+    rms = float(np.sqrt(((sur - exact) ** 2).sum() / (exact ** 2).sum()))
+    # per system: the worst replica's error
+    offs = np.cumsum([0] + [w.n_beads for w in reps])
+    per_sys = [float(np.sqrt(((sur[offs[i]:offs[i + 1]] - exact[offs[i]:offs[i + 1]]) ** 2).sum()
+                             / (exact[offs[i]:offs[i + 1]] ** 2).sum())) for i in range(len(reps))]
+    lam = [1.0 / w.derived.kappa for w in reps]
+    watch = [int(i) for i in np.argsort(lam)[-4:]]  # the longest screening lengths
+    k = max(B, (args.steps // B) * B)
+
+    def run_batch(enabled):
+        gpu.surrogate_enable(s, enabled)
+        s.set_state(pos, vel)
+        s.md_begin()
+        s.md_steps(0, 2 * B)
+        a0 = 2 * B
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(ext)
+        s.md_enqueue(a0, k)
+        e1.record(ext)
+        s.synchronize()
+        ms = e0.elapsed_time(e1)
+        a1 = a0 + k
+        temps = {i: [] for i in watch}
+        pots = {i: [] for i in watch}
+        for q in range(args.stat_steps // 20):
+            s.md_steps(a1, 20)
+            a1 += 20
+            for i in watch:
+                ke, _, _ = s.md_scalars(i)
+                temps[i].append(2 * ke / (3 * reps[i].n_beads))
+                if q % 5 == 0:
+                    e = s.energies(i)
+                    pots[i].append(e["stretching"] + e["bending"] + e["lj"] + e["electrostatic"])
+        st = gpu.surrogate_stats(s) if enabled else None
+        return {"value": n * k / (ms / 1e3), "ms_per_step": ms / k,
+                "T_mean": {str(i): float(np.mean(temps[i])) for i in watch},
+                "potential_mean": {str(i): float(np.mean(pots[i])) for i in watch},
+                "potential_std": {str(i): float(np.std(pots[i])) for i in watch},
+                "judge": {"judged": st["judged"], "classes_off": st["classes_off"],
+                          "last_error": st["last_error"]} if st else None}
+
+    batched = run_batch(False)
+    surr = run_batch(True)
+    s.close()
+    net.close()
+
+    # the plain GPU path: each replica alone, exact
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    sample = list(range(0, len(reps), max(1, len(reps) // max(1, args.plain_sample))))
+    plain_ms, plain_beads = 0.0, 0
+    for i in sample:
+        w = reps[i]
+        si = gpu.GpuSystem(tpl, [params[i]])
+        si.set_state(pos[offs[i]:offs[i + 1]], vel[offs[i]:offs[i + 1]])
+        si.md_begin()
+        si.md_steps(0, 2 * B)
+        exi = torch.cuda.ExternalStream(si.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(exi):
+            flush.zero_()
+        e0.record(exi)
+        si.md_enqueue(2 * B, k)
+        e1.record(exi)
+        si.synchronize()
+        plain_ms += e0.elapsed_time(e1)
+        plain_beads += w.n_beads
+        si.close()
+    plain_value = plain_beads * k / (plain_ms / 1e3)
+    sizes = [int(w.opt.S) for w in reps]
+    print(json.dumps({
+        "metric": "bead-steps/s on 1 GB300: surrogate+batched vs plain GPU at <=1e-3 force RMS err",
+        "value": surr["value"], "unit": "bead-steps/s", "n_gpus": 1, "steps": k, "warmup": 2 * B,
+        "ms_per_step": surr["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 network (fp32 accumulate) + f32/i64 exact path",
+        "data": "synthetic (seeded replicas)",
+        "config": {"workload": f"replica sweep: {len(reps)} systems of bilayer capsomeres, {S_tot} "
+                               f"subunits, {n} beads, subunits per system {min(sizes)}-{max(sizes)}, "
+                               f"eps 1.5-3.0, Debye length 0.5-2.0 sigma, 200-1600 uM; switch radius "
+                               f"3.5 sigma (closest bead pair), judge 1 % of far pairs every 100 steps",
+                   "l2": "batched: working set larger than L2, whole rebuild windows; plain: L2 "
+                         "flushed before each replica's window"},
+        "gain": surr["value"] / plain_value,
+        "gain_batching": batched["value"] / plain_value,
+        "gain_surrogate": surr["value"] / batched["value"],
+        "plain": {"value": plain_value, "replicas_timed": len(sample), "beads_timed": plain_beads,
+                  "ms_total": plain_ms},
+        "batched": batched, "surrogate": surr,
+        "force_rms_rel_error": rms, "force_rms_rel_error_worst_system": max(per_sys),
+        "far_pairs": far_pairs, "far_capacity": far_cap,
+        "watched_systems": {str(i): {"subunits": sizes[i], "debye_length": lam[i],
+                                     "eps": float(reps[i].opt.E), "conc_um": float(reps[i].opt.C)}
+                            for i in watch},
+        "training": {"rows": total, "frames": frames, "epochs": args.epochs, "batch": batch,
+                     "final_loss_normalised": loss, "collect_s": collect_s, "fit_s": fit_s},
+        "generation_s": gen_s}))
 
 
 def cpu_analysis_port(n_sub: int, seconds: float = 10.0):
@@ -431,6 +622,9 @@ def main():
     ap.add_argument("--replicas", type=int, default=0,
                     help="run a batch of this many independent replicas (20-500 subunits each, "
                          "per-replica epsilon, Debye length and concentration) instead")
+    ap.add_argument("--replica-subunits", type=int, default=0,
+                    help="with --replicas: every replica this many subunits at the plain workload's "
+                         "parameters (default: sizes and parameters drawn per replica)")
     ap.add_argument("--surrogate", action="store_true",
                     help="learned far-field surrogate vs the plain path on the same workload")
     ap.add_argument("--analysis", action="store_true",
@@ -439,7 +633,16 @@ def main():
     ap.add_argument("--max-frames", type=int, default=6000)
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--stat-steps", type=int, default=2000)
+    ap.add_argument("--debye-length", type=float, default=0.0,
+                    help="screening length in sigma (default 1: -c 94.27)")
+    ap.add_argument("--concentration", type=float, default=0.0, help="subunits in uM (default 800)")
+    ap.add_argument("--plain-sample", type=int, default=256,
+                    help="with --replicas --surrogate: replicas timed alone for the plain path")
+    ap.add_argument("--far-per-subunit", type=int, default=4,
+                    help="surrogate far-pair list capacity per subunit")
     args = ap.parse_args()
+    if args.replicas and args.surrogate:
+        return bench_surrogate_batched(args)
     if args.replicas:
         return bench_replicas(args)
     if args.surrogate:
@@ -450,10 +653,13 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from souffle_gb300 import workloads
-    w = workloads.plain_large(args.subunits, seed=12345 + rank)
+    w = workloads.plain_large(args.subunits, seed=12345 + rank, debye_length=args.debye_length,
+                              conc_um=args.concentration)
     config = {"workload": f"plain_large: {args.subunits} bilayer capsomeres x 42 beads = "
-                          f"{w.n_beads} beads, 800 uM, -e 5 -L 0.3 -B 10 -t 0.005 -q 5",
-              "l2": "flushed (256 MB write) before every timed step; working set < L2",
+                          f"{w.n_beads} beads, {w.opt.C:g} uM, -c {w.opt.c:.4g} (Debye length "
+                          f"{1 / w.derived.kappa:.3g} sigma) -e 5 -L 0.3 -B 10 -t 0.005 -q 5",
+              "l2": "flushed (256 MB write) before every timed step" + (
+                  "; working set < L2" if w.n_beads * 400 < 129e6 else "; working set > L2"),
               "parallelism": f"replicas x{world}"}
 
     if args.impl == "reference":
@@ -591,7 +797,9 @@ def main():
     kern_bytes = (16 + 4 * n_bar + 24 + 48 + 16) * w.n_beads
     achieved = kern_bytes / (forces_ms / 1e3) / 1e9
     step_bytes = (112 + 4 * n_bar + (4 * n_bar + 16) / B) * w.n_beads
-    traffic = _profile_traffic()
+    # the committed ncu figure is for the default workload only
+    default_workload = args.subunits == 2000 and not args.debye_length and not args.concentration
+    traffic = _profile_traffic() if default_workload else None
     out = {
         "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,

@@ -47,7 +47,7 @@ struct PairArgs {
   unsigned int* intra_mask;  // [S_total * np * words]
   int* inter_ids;            // [N][cap] row-major
   int* inter_count;          // [N]
-  const unsigned char* cand_far = nullptr;  // [S_total * cand_cap]: candidate left to the surrogate
+  const unsigned char* cand_far = nullptr;  // [S_total * cand_cap]: nonzero = not in the pair list (1 left to the surrogate, 2 beyond every cut-off)
   const int* far_ok = nullptr;              // the far flags apply (no far-list overflow)
   int* ref_len;              // [N] reference list length (intra + inter)
   int inter_cap;

@@ -159,11 +159,19 @@ __device__ __forceinline__ void body_coords(const FarArgs& a, int s, const Frame
 __global__ void __launch_bounds__(128) k_far_classify(FarArgs a) {
   extern __shared__ int4 s_pa[];  // [np]
   __shared__ int s_cnt;
+  __shared__ float s_reach2;
   const int i = blockIdx.x, np = a.np;
   for (int t = threadIdx.x; t < np; t += blockDim.x) s_pa[t] = a.pos32[(size_t)i * np + t];
-  if (threadIdx.x == 0) s_cnt = 0;
+  const SysParams& P = a.sys[a.sub_sys[i]];
+  if (threadIdx.x == 0) {
+    s_cnt = 0;
+    // reach of every pair term: the DH cut-off (+inf without one) and the LJ/WCA cut-offs
+    float r2 = P.ecut_el2;
+    for (int k = 0; k < kMaxSpecies * kMaxSpecies; k++) r2 = fmaxf(r2, a.pt->cut2[k]);
+    s_reach2 = r2 * 1.0001f;
+  }
   __syncthreads();
-  const float unit = a.sys[a.sub_sys[i]].unit32;
+  const float unit = P.unit32;
   const int ncand = a.cand_count[i];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   int my_far = 0;
@@ -184,8 +192,12 @@ __global__ void __launch_bounds__(128) k_far_classify(FarArgs a) {
     if (lane == 0) {
       const float dmin = sqrtf(d2);
       bool far = (j != i) && dmin >= a.r_switch;
+      // a far pair with every bead pair beyond every cut-off exerts no force: it is left out of
+      // both the pair list and the far list (2)
+      const bool inert = far && d2 > s_reach2;
       if (far && a.class_off && a.class_off[dist_class(dmin, a.r_switch)]) far = false;
-      a.cand_far[(size_t)i * a.cand_cap + c] = far ? 1 : 0;
+      far = far && !inert;
+      a.cand_far[(size_t)i * a.cand_cap + c] = inert ? 2 : (far ? 1 : 0);
       a.cand_dmin[(size_t)i * a.cand_cap + c] = dmin;
       my_far += far ? 1 : 0;
     }
@@ -233,7 +245,7 @@ __global__ void k_far_write(FarArgs a) {
   const int nc = a.cand_count[i];
   for (int c = 0; c < nc; c++) {
     const size_t e = (size_t)i * a.cand_cap + c;
-    if (!a.cand_far[e]) continue;
+    if (a.cand_far[e] != 1) continue;
     a.far_pair[k] = make_int2(i, a.cand[e]);
     a.far_dmin[k] = a.cand_dmin[e];
     k++;

@@ -71,8 +71,16 @@ def plain_small(seed: int = 12345) -> Workload:
     return make(geometry.patch_n3(), 20, seed, name="plain_small")
 
 
-def plain_large(n_sub: int = 2000, seed: int = 12345) -> Workload:
-    return make(geometry.bilayer_n5(), n_sub, seed, name="plain_large")
+def plain_large(n_sub: int = 2000, seed: int = 12345, debye_length: float = 0.0,
+                conc_um: float = 0.0) -> Workload:
+    """The bilayer workload; ``debye_length`` (sigma) and ``conc_um`` (micromolar) override the
+    default screening length of 1 sigma and concentration of 800 uM when nonzero."""
+    over = {}
+    if debye_length:
+        over["c"] = state.salt_for_debye_length(debye_length)
+    if conc_um:
+        over["C"] = conc_um
+    return make(geometry.bilayer_n5(), n_sub, seed, name="plain_large", **over)
 
 
 def replicas(n: int = 256, seed: int = 2024, sub_range=(20, 500)) -> List[Workload]:
@@ -88,6 +96,13 @@ def replicas(n: int = 256, seed: int = 2024, sub_range=(20, 500)) -> List[Worklo
         salt = state.salt_for_debye_length(lam)
         out.append(make(t, S, seed=seed * 1000 + k, name=f"replica{k}", E=eps, c=salt, C=conc))
     return out
+
+
+def uniform_replicas(n: int, n_sub: int, seed: int = 4040) -> List[Workload]:
+    """``n`` independent copies of the bilayer workload at ``n_sub`` subunits each (800 uM,
+    Debye length 1 sigma), each from its own seeded initial state."""
+    t = geometry.bilayer_n5()
+    return [make(t, n_sub, seed=seed * 1000 + k, name=f"replica{k}") for k in range(n)]
 
 
 def analysis_frames(n_sub: int = 2000, n_frames: int = 4, seed: int = 4242, conc_um: float = 800.0,

@@ -39,7 +39,11 @@ def frame(pos_sub, center, b1, b2, box):
     return e1, e2, e3, m, d
 
 
-def far_pairs(pos, n_sub, np_, center, box, r_list, r_switch):
+def far_pairs(pos, n_sub, np_, center, box, r_list, r_switch, reach=np.inf):
+    """Candidate subunit pairs (the centre-bead prefilter) whose closest bead pair is at least
+    r_switch apart, leaving out pairs whose closest bead pair lies beyond ``reach`` (the largest
+    pair cut-off, with the GPU classifier's 1e-4 relative margin on the square): those exert no
+    force and are in neither list."""
     p = pos.reshape(n_sub, np_, 3)
     c = p[:, center, :]
     out = []
@@ -51,7 +55,7 @@ def far_pairs(pos, n_sub, np_, center, box, r_list, r_switch):
                 continue
             dd = min_image(p[a][:, None, :] - p[b][None, :, :], box)
             dmin = float(np.sqrt((dd ** 2).sum(-1).min()))
-            if dmin >= r_switch:
+            if dmin >= r_switch and not dmin * dmin > reach * reach * 1.0001:
                 out.append((a, int(b), dmin))
     return out
 

@@ -48,7 +48,8 @@ def test_collect_matches_oracle():
     n = gpu.surrogate_collect(s, x.data_ptr(), t.data_ptr(), CAP)
     np_ = w.template.n_beads
     L = float(w.derived.box)
-    ref = SO.far_pairs(w.state.pos, int(w.opt.S), np_, w.center_local, L, w.derived.nlist_cutoff, 3.5)
+    ref = SO.far_pairs(w.state.pos, int(w.opt.S), np_, w.center_local, L, w.derived.nlist_cutoff, 3.5,
+                       reach=max(w.derived.ecut_el, w.derived.ecut))
     assert n == len(ref) and n > 20
     b1, b2 = SO.anchors(w.template.pos, w.center_local)
     wts = SO.dh_weights(w.template.charge, w.template.diameter, w.derived.kappa, w.derived.lb)
@@ -68,6 +69,39 @@ def test_collect_matches_oracle():
         # targets reconstruct the exact forces, and agree with the oracle's decomposition
         np.testing.assert_allclose(SO.reconstruct(T[k], db, J), g, atol=2e-4 * scale, rtol=0)
         np.testing.assert_allclose(T[k, :3], tr[:3], atol=2e-4 * np.abs(tr[:3]).max() + 1e-12, rtol=0)
+
+
+def test_collect_spans_the_systems_of_one_handle():
+    """Two systems with different screening lengths (1 and 2 sigma) in one handle: the far list
+    is the union of each system's far pairs, pairs beyond every cut-off left out, and each row's
+    descriptor carries its own system's screening length."""
+    from souffle_gb300 import geometry, gpu, state, workloads
+    torch = _torch()
+    t = geometry.bilayer_n5()
+    ws = [workloads.make(t, 150, seed=31, C=2000),
+          workloads.make(t, 120, seed=32, C=1500, c=state.salt_for_debye_length(2.0))]
+    ps = [gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local) for w in ws]
+    s = gpu.GpuSystem(t, ps)
+    s.set_state(np.concatenate([w.state.pos for w in ws]), np.concatenate([w.state.vel for w in ws]))
+    n_out = 6 + 3 * t.n_beads
+    net = gpu.Mlp(64, n_out, max_batch=CAP, seed=3)
+    gpu.surrogate_attach(s, net, t.pos, far_capacity=CAP)
+    x = torch.zeros(CAP, 64, device="cuda")
+    y = torch.zeros(CAP, n_out, device="cuda")
+    n = gpu.surrogate_collect(s, x.data_ptr(), y.data_ptr(), CAP)
+    counts = []
+    for w in ws:
+        ref = SO.far_pairs(w.state.pos, int(w.opt.S), t.n_beads, w.center_local, float(w.derived.box),
+                           w.derived.nlist_cutoff, 3.5, reach=max(w.derived.ecut_el, w.derived.ecut))
+        allp = SO.far_pairs(w.state.pos, int(w.opt.S), t.n_beads, w.center_local, float(w.derived.box),
+                            w.derived.nlist_cutoff, 3.5)
+        counts.append(len(ref))
+        if w is ws[0]:
+            assert len(allp) > len(ref)       # at 1 sigma some candidates lie beyond the cut-off
+    assert counts[1] > 0 and n == sum(counts)
+    lam = x[:n, 37].cpu().numpy()
+    assert np.sum(np.isclose(lam, 1 / ws[0].derived.kappa, rtol=1e-6)) == counts[0]
+    assert np.sum(np.isclose(lam, 1 / ws[1].derived.kappa, rtol=1e-6)) == counts[1]
 
 
 def _train(w, s, torch, x, t, frames=12, stride=20, epochs=60):
@@ -102,7 +136,8 @@ def test_training_and_force_accuracy():
     np_ = w.template.n_beads
     pos, _ = s.get_state()
     L = float(w.derived.box)
-    ref = SO.far_pairs(pos, int(w.opt.S), np_, w.center_local, L, w.derived.nlist_cutoff, 3.5)
+    ref = SO.far_pairs(pos, int(w.opt.S), np_, w.center_local, L, w.derived.nlist_cutoff, 3.5,
+                       reach=max(w.derived.ecut_el, w.derived.ecut))
     assert n == len(ref)
     wts = SO.dh_weights(w.template.charge, w.template.diameter, w.derived.kappa, w.derived.lb)
     P = pos.reshape(-1, np_, 3)

@@ -330,51 +330,80 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   // (no barrier: phase 2 adds into the same zeroed limbs, in any order)
 
   // Phase 2: inter-subunit pairs (DH + LJ/WCA, src/forces.cpp:81-138).  The CTA's beads' lists
-  // are one flat sequence (s_pref: exclusive prefix sums of their lengths) dealt out evenly over
-  // all threads, so a bead with a long list does not hold up its CTA; each pair force is added
-  // to the bead's limbs exactly in fixed point (order-independent, deterministic).
+  // are one flat sequence (s_pref: exclusive prefix sums of their lengths) cut into equal
+  // contiguous runs, one per thread, so a bead with a long list does not hold up its CTA.  A
+  // thread walks its run bead by bead, sums the pair forces of each bead exactly in 2^-32 fixed
+  // point in registers and adds the sum to the bead's limbs when it moves to the next bead
+  // (order-independent, deterministic).
   {
     const int n_inter = s_pref[nbead];
-    for (int p = threadIdx.x; p < n_inter; p += blockDim.x) {
-      int lo = 0, hi = nbead;  // s_pref[lo] <= p < s_pref[hi]: the pair belongs to bead lo
+    const int run = (n_inter + blockDim.x - 1) / blockDim.x;
+    int p = threadIdx.x * run;
+    const int pend = min(n_inter, p + run);
+    if (p < pend) {
+      int lo = 0, hi = nbead;  // s_pref[lo] <= p < s_pref[hi]: the run starts in bead lo
       while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (s_pref[mid] <= p) lo = mid;
         else hi = mid;
       }
-      const int b = lo, g = bead0 + b, l = b % np;
-      const int j = __ldg(a.inter_ids + (size_t)g * a.inter_cap + (p - s_pref[b]));
-      const int4 pj = __ldg(&a.pos32[j]);
-      const int4 pi = s_pos[b];
-      const int si = species[l];
-      const int lj = pj.w;
-      const float3 d = dvec(pi, pj, unit);
-      const float r2 = dot3(d, d);
-      float c = 0.f;
-      const float wi = s_w[l], wj = s_w[lj];
-      if (wi * wj != 0.f && r2 < ecut_el2) {
-        const float ir = rsqrtf(r2);
-        const float r = r2 * ir;
-        c = wi * wj * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
+      int b = lo, l = b % np, bend = s_pref[b + 1];
+      int4 pi = s_pos[b];
+      int si = species[l];
+      float wi = s_w[l];
+      // the row of bead b holds its pairs s_pref[b] .. s_pref[b + 1] - 1 of the flat sequence
+      long long row = (long long)(bead0 + b) * a.inter_cap - s_pref[b];
+      long long ax = 0, ay = 0, az = 0;
+      for (; p < pend; p++) {
+        if (p >= bend) {  // next bead with pairs: add this bead's sums to its limbs
+          limbs_add(s_F + 9 * b, ax);
+          limbs_add(s_F + 9 * b + 3, ay);
+          limbs_add(s_F + 9 * b + 6, az);
+          ax = ay = az = 0;
+          do {
+            b++;
+            bend = s_pref[b + 1];
+          } while (p >= bend);
+          l = b % np;
+          pi = s_pos[b];
+          si = species[l];
+          wi = s_w[l];
+          row = (long long)(bead0 + b) * a.inter_cap - s_pref[b];
+        }
+        const int j = __ldg(a.inter_ids + (row + p));
+        const int4 pj = __ldg(&a.pos32[j]);
+        const int lj = pj.w;
+        const float3 d = dvec(pi, pj, unit);
+        const float r2 = dot3(d, d);
+        float c = 0.f;
+        const float wj = s_w[lj];
+        if (wi * wj != 0.f && r2 < ecut_el2) {
+          const float ir = rsqrtf(r2);
+          const float r = r2 * ir;
+          c = wi * wj * __expf(-kappa * r) * (ir * ir) * (kappa + ir);
+        }
+        const int sj = species[lj];
+        const int pidx = si * kMaxSpecies + sj;
+        if (r2 < pt.cut2[pidx]) {
+          const bool att = (L.lj_att_bits[si] >> sj) & 1;
+          const float eps = att ? (((L.type7_bits >> sj) & 1) ? 50.0f : P.elj_att) : 1.0f;
+          const float ir2 = 1.0f / r2;
+          const float s6 = pt.sig6[pidx] * ir2 * ir2 * ir2;
+          c += 48.0f * eps * s6 * (s6 - 0.5f) * ir2;
+        }
+        const float3 f = d * c;
+        if (!(isfinite(f.x) && isfinite(f.y) && isfinite(f.z)) ||
+            fmaxf(fmaxf(fabsf(f.x), fabsf(f.y)), fabsf(f.z)) > 1.0e9f) {
+          atomicOr(a.err, kErrNonFinite);
+          continue;
+        }
+        ax += f32_to_fx32(f.x);
+        ay += f32_to_fx32(f.y);
+        az += f32_to_fx32(f.z);
       }
-      const int sj = species[lj];
-      const int pidx = si * kMaxSpecies + sj;
-      if (r2 < pt.cut2[pidx]) {
-        const bool att = (L.lj_att_bits[si] >> sj) & 1;
-        const float eps = att ? (((L.type7_bits >> sj) & 1) ? 50.0f : P.elj_att) : 1.0f;
-        const float ir2 = 1.0f / r2;
-        const float s6 = pt.sig6[pidx] * ir2 * ir2 * ir2;
-        c += 48.0f * eps * s6 * (s6 - 0.5f) * ir2;
-      }
-      const float3 f = d * c;
-      if (!(isfinite(f.x) && isfinite(f.y) && isfinite(f.z)) ||
-          fmaxf(fmaxf(fabsf(f.x), fabsf(f.y)), fabsf(f.z)) > 1.0e9f) {
-        atomicOr(a.err, kErrNonFinite);
-        continue;
-      }
-      limbs_add(s_F + 9 * b, f32_to_fx32(f.x));
-      limbs_add(s_F + 9 * b + 3, f32_to_fx32(f.y));
-      limbs_add(s_F + 9 * b + 6, f32_to_fx32(f.z));
+      limbs_add(s_F + 9 * b, ax);
+      limbs_add(s_F + 9 * b + 3, ay);
+      limbs_add(s_F + 9 * b + 6, az);
     }
   }
   __syncthreads();

@@ -1,4 +1,5 @@
-// tcgen05 GEMM: one CTA per 128 x BN output tile, 256 threads (8 warps).
+// tcgen05 GEMM: 128 x BN output tiles, 256 threads (8 warps) per CTA; at most one wave of CTAs,
+// each looping over row tiles, so a large row capacity with few live rows (*m_dyn) costs little.
 //   warp 0, lane 0  TMA producer: 128 x 64 A and BN x 64 B tiles (128-byte swizzle) into a
 //                   4-stage shared-memory ring, one mbarrier per stage ("full")
 //   warp 1, lane 0  MMA issuer: four K = 16 tcgen05.mma per stage into an FP32 accumulator in
@@ -15,6 +16,7 @@
 // flag word.
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "gemm.cuh"
@@ -44,7 +46,7 @@ struct GemmTile {
 __device__ __forceinline__ float sigmoid_fast(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 template <int BN, int ACT>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, BN <= 64 ? 2 : 1)
     k_gemm_bf16(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmEpi e) {
   using G = GemmTile<BN>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -55,10 +57,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile uint32_t* tmem_slot_ptr = reinterpret_cast<volatile uint32_t*>(smem_raw + (tmem_slot - raw));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m_rows = e.m_dyn ? min(e.M, *e.m_dyn) : e.M;
-  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
-  if (m0 >= m_rows) return;  // uniform over the CTA, before any allocation
+  const int m_tiles = (m_rows + kBM - 1) / kBM;
+  const int n0 = blockIdx.y * BN;
+  if ((int)blockIdx.x >= m_tiles) return;  // uniform over the CTA, before any allocation
   const int nk = (e.K + kBK - 1) / kBK;
   const uint32_t full0 = bars, empty0 = bars + 8 * kStages, accum = bars + 16 * kStages;
+  __shared__ int s_fail;
 
   if (warp == 0) {
     tmem_alloc(tmem_slot, G::kTmemCols);
@@ -71,6 +75,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     mbar_init(accum, 1);
     mbar_fence_init();
+    s_fail = 0;
   }
   if (threadIdx.x == 64) {
     tma_prefetch_map(&ta);
@@ -81,12 +86,21 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot_ptr;
 
+  // Row tiles blockIdx.x, blockIdx.x + gridDim.x, ... below the row count: the ring's stage and
+  // phase follow the k-step count over all tiles so far (g), the accumulator's phase the tile
+  // count (iter).  Each tile ends with a CTA barrier, after which the accumulator and the
+  // stages (the epilogue's staging) are free for the next tile.
+  int iter = 0;
+  for (int mt = blockIdx.x; mt < m_tiles; mt += gridDim.x, iter++) {
+  const int m0 = mt * kBM;
+  const int g0 = iter * nk;
   bool ok = true;
   if (warp == 0 && lane == 0) {
     int issued = 0;
     for (int kt = 0; kt < nk; kt++) {
-      const int s = kt % kStages;
-      const uint32_t use = (uint32_t)(kt / kStages);
+      const int g = g0 + kt;
+      const int s = g % kStages;
+      const uint32_t use = (uint32_t)(g / kStages);
       if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1u)) {
         ok = false;
         break;
@@ -97,14 +111,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       tma_load_2d(a_s + G::kA, &tb, kt * kBK, n0, full0 + 8 * s);
       issued = kt + 1;
     }
-    // every copy this thread started has landed before the CTA can leave
-    for (int kt = (issued > kStages ? issued - kStages : 0); kt < issued; kt++)
-      if (!mbar_wait(full0 + 8 * (kt % kStages), (uint32_t)(kt / kStages) & 1u)) ok = false;
+    // every copy this thread started has landed before the stages are reused or the CTA leaves
+    for (int kt = (issued > kStages ? issued - kStages : 0); kt < issued; kt++) {
+      const int g = g0 + kt;
+      if (!mbar_wait(full0 + 8 * (g % kStages), (uint32_t)(g / kStages) & 1u)) ok = false;
+    }
   } else if (warp == 1 && lane == 0) {
     constexpr uint32_t idesc = umma_idesc_bf16(kBM, BN);
     for (int kt = 0; kt < nk; kt++) {
-      const int s = kt % kStages;
-      if (!mbar_wait(full0 + 8 * s, (uint32_t)(kt / kStages) & 1u)) {
+      const int g = g0 + kt;
+      const int s = g % kStages;
+      if (!mbar_wait(full0 + 8 * s, (uint32_t)(g / kStages) & 1u)) {
         ok = false;
         break;
       }
@@ -120,7 +137,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (!ok) atomicOr(e.err, e.err_bit);
   __syncwarp();
 
-  if (mbar_wait(accum, 0)) {
+  if (mbar_wait(accum, (uint32_t)iter & 1u)) {
     tc_fence_after();
     const int quarter = warp & 3, half = warp >> 2;
     const int row = m0 + quarter * 32 + lane;
@@ -173,11 +190,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else {
     atomicOr(e.err, e.err_bit);
+    ok = false;
   }
+  if (!ok) s_fail = 1;
+  // the staging writes above precede the next tile's TMA writes into the same stages
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   tc_fence_before();
   __syncthreads();
+  tc_fence_after();
+  if (s_fail) break;  // uniform: read after the barrier
+  }
   if (warp == 0) {
-    tc_fence_after();
     tmem_dealloc(tmem, G::kTmemCols);
   }
 }
@@ -221,7 +244,20 @@ cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int 
   if (attr != cudaSuccess) return attr;
   CUtensorMap ta, tb;
   if (!make_map(&ta, A, e.M, e.K, lda, kBM) || !make_map(&tb, B, e.N, e.K, ldb, BN)) return cudaErrorInvalidValue;
-  dim3 grid((e.M + kBM - 1) / kBM, (e.N + BN - 1) / BN);
+  // at most one wave of CTAs; each loops over row tiles (rows beyond *m_dyn are never visited)
+  static int max_ctas = 0;
+  static std::once_flag once_occ;
+  std::call_once(once_occ, [] {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_bf16<BN, ACT>, kThreads, G::kSmem) ==
+            cudaSuccess)
+      max_ctas = sms * std::max(1, per_sm);
+  });
+  const int tiles_m = (e.M + kBM - 1) / kBM, tiles_n = (e.N + BN - 1) / BN;
+  const int gx = max_ctas > 0 ? std::min(tiles_m, std::max(1, max_ctas / tiles_n)) : tiles_m;
+  dim3 grid(gx, tiles_n);
   k_gemm_bf16<BN, ACT><<<grid, kThreads, G::kSmem, st>>>(ta, tb, e);
   return cudaGetLastError();
 }

@@ -11,6 +11,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -46,13 +47,17 @@ souffle_status fail(souffle_status s, const std::string& msg) {
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
 // x [m][n_in] FP32 -> a0 [m][ld] BF16 row-major and a0T [n_in][ldt] BF16
-__global__ void k_pack_input(const float* x, int m, int n_in, __nv_bfloat16* a0, int ld, __nv_bfloat16* a0t, int ldt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m * n_in) return;
-  const int r = i / n_in, c = i - r * n_in;
-  const __nv_bfloat16 v = __float2bfloat16_rn(x[i]);
-  a0[(size_t)r * ld + c] = v;
-  if (a0t) a0t[(size_t)c * ldt + r] = v;
+// (rows >= *m_dyn skipped when m_dyn is given; grid-stride over the rest)
+__global__ void k_pack_input(const float* x, int m, int n_in, __nv_bfloat16* a0, int ld, __nv_bfloat16* a0t, int ldt,
+                             const int* m_dyn = nullptr) {
+  const int rows = m_dyn ? min(m, *m_dyn) : m;
+  const long long n = (long long)rows * n_in;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / n_in), c = (int)(i - (long long)r * n_in);
+    const __nv_bfloat16 v = __float2bfloat16_rn(x[i]);
+    a0[(size_t)r * ld + c] = v;
+    if (a0t) a0t[(size_t)c * ldt + r] = v;
+  }
 }
 
 // dY = 2 (y - t) / (m n_out) as BF16 (row-major and transposed, zero beyond n_out), and per-block
@@ -303,8 +308,8 @@ constexpr unsigned int kErrSurrogateBit = 8u;  // the system's error word: surro
 cudaError_t mlp_forward_async(souffle_mlp* h, const float* x, int m_cap, const int* m_dyn, unsigned int* err,
                               cudaStream_t st, const float** y, int* ldy) {
   if (m_cap < 1 || m_cap > h->cap) return cudaErrorInvalidValue;
-  k_pack_input<<<blocks((long long)m_cap * h->n_in, 256), 256, 0, st>>>(x, m_cap, h->n_in, h->act[0].p, h->in_ld[0],
-                                                                       nullptr, h->cap);
+  k_pack_input<<<std::min(blocks((long long)m_cap * h->n_in, 256), 152 * 8), 256, 0, st>>>(
+      x, m_cap, h->n_in, h->act[0].p, h->in_ld[0], nullptr, h->cap, m_dyn);
   cudaError_t r = cudaGetLastError();
   if (r != cudaSuccess) return r;
   r = forward_on(h, m_cap, false, st, m_dyn, err, kErrSurrogateBit);

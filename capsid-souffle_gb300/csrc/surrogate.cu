@@ -257,6 +257,9 @@ __global__ void __launch_bounds__(128) k_sub_frames(FarArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.x * 4 + warp;
   if (s >= a.S) return;
+  // frames are read only for subunits in far pairs; the far relation is symmetric (the same
+  // closest distance from either side), so a subunit with no far pairs of its own is in none
+  if (a.far_start[s + 1] == a.far_start[s]) return;
   const int np = a.np;
   const SysParams& P = a.sys[a.sub_sys[s]];
   const int4 pc = a.pos32[(size_t)s * np + P.center_local];
@@ -334,9 +337,15 @@ __global__ void __launch_bounds__(128) k_sub_frames(FarArgs a) {
   }
 }
 
+__device__ void far_descr_one(const FarArgs& a, int p);
+
+// grid-stride over the far pairs of the list (the grid is sized for one wave, not the capacity)
 __global__ void k_far_descr(FarArgs a) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.far_total[0]) return;
+  const int n = a.far_total[0];
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) far_descr_one(a, p);
+}
+
+__device__ void far_descr_one(const FarArgs& a, int p) {
   const int2 ab = a.far_pair[p];
   const int np = a.np;
   const SysParams& P = a.sys[a.sub_sys[ab.x]];
@@ -769,7 +778,7 @@ void surrogate_forces(souffle_gpu_system* h, ForceArgs& fa) {
   FarArgs a = far_args(h);
   const int sb = (h->S + 3) / 4;
   k_sub_frames<<<sb, 128, 0, h->stream>>>(a);
-  k_far_descr<<<(c.far_cap + 127) / 128, 128, 0, h->stream>>>(a);
+  k_far_descr<<<std::min((c.far_cap + 127) / 128, 152 * 8), 128, 0, h->stream>>>(a);
   const float* y = nullptr;
   int ldy = 0;
   if (mlp_forward_async(c.net, c.x.p, c.far_cap, c.far_total.p, h->err.p, h->stream, &y, &ldy) != cudaSuccess) {
@@ -1028,7 +1037,7 @@ souffle_status souffle_surrogate_collect(souffle_gpu_system* h, float* x_dev, fl
   launch_classify(h, a);
   k_far_write<<<(h->S + 127) / 128, 128, 0, h->stream>>>(a);
   k_sub_frames<<<(h->S + 3) / 4, 128, 0, h->stream>>>(a);
-  k_far_descr<<<(c.far_cap + 127) / 128, 128, 0, h->stream>>>(a);
+  k_far_descr<<<std::min((c.far_cap + 127) / 128, 152 * 8), 128, 0, h->stream>>>(a);
   k_far_targets<<<(c.far_cap + 3) / 4, 128, 0, h->stream>>>(a);
   S_TRY(cudaGetLastError());
   int tot[3];

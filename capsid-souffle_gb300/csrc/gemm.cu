@@ -1,14 +1,15 @@
 // tcgen05 GEMM: 128 x BN output tiles, 256 threads (8 warps) per CTA; at most one wave of CTAs,
 // each looping over row tiles, so a large row capacity with few live rows (*m_dyn) costs little.
 //   warp 0, lane 0  TMA producer: 128 x 64 A and BN x 64 B tiles (128-byte swizzle) into a
-//                   4-stage shared-memory ring, one mbarrier per stage ("full")
+//                   3-stage shared-memory ring, one mbarrier per stage ("full"); two CTAs fit
+//                   an SM, so one CTA's epilogue overlaps the other's loads and MMAs
 //   warp 1, lane 0  MMA issuer: four K = 16 tcgen05.mma per stage into an FP32 accumulator in
 //                   tensor memory; tcgen05.commit frees the stage ("empty") and, after the last
 //                   stage, signals the epilogue ("accum")
 //   warps 0-7       epilogue: warp w reads accumulator lanes 32 (w % 4) .. + 31 (one output row
 //                   per thread) and half (w / 4) of the columns, 32 at a time (two tcgen05.ld in
-//                   flight, one wait), applies bias / activation, and stores through shared
-//                   memory so that global stores run along the rows
+//                   flight, one wait), applies bias (staged in shared memory) / activation, and
+//                   stores each thread's 32 contiguous row elements as 16-byte vectors
 // The epilogue is the long part of a small GEMM (it is latency-bound per thread), so it gets all
 // eight warps, the activation is a template parameter, and BN = 64 by default spreads a small M
 // over more SMs.  K tails and M/N edges are zero-filled by TMA (out-of-bounds box elements) and
@@ -24,9 +25,8 @@
 
 namespace souffle {
 
-constexpr int kBM = 128, kBK = 64, kStages = 4, kThreads = 256;
+constexpr int kBM = 128, kBK = 64, kStages = 3, kThreads = 256;
 constexpr int kStageCols = 32;                  // epilogue chunk per warp
-constexpr int kStagePitch = kStageCols + 1;     // conflict-free rows and columns
 
 template <int BN>
 struct GemmTile {
@@ -36,17 +36,21 @@ struct GemmTile {
   static constexpr int kBars = 2 * kStages + 1;
   static constexpr int kSmem = 1024 + kStages * kStage + kBars * 8 + 16;
   static constexpr int kTmemCols = BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
-  static constexpr int kEpiBytes = (kThreads / 32) * 2 * 32 * kStagePitch * 4;
   static_assert(kStage % 1024 == 0, "stages stay on 1024-byte boundaries (128-byte swizzle atoms)");
-  static_assert(kEpiBytes <= kStages * kStage, "epilogue staging fits in the freed stages");
   static_assert(BN % (2 * kStageCols) == 0, "each half of the columns is whole chunks");
 };
+
+// two floats rounded to BF16 (nearest even), low half = first
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
 
 // logistic function with the fast exponential and division (the BF16 outputs carry 8 bits)
 __device__ __forceinline__ float sigmoid_fast(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 template <int BN, int ACT>
-__global__ void __launch_bounds__(kThreads, BN <= 64 ? 2 : 1)
+__global__ void __launch_bounds__(kThreads, 2)
     k_gemm_bf16(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, GemmEpi e) {
   using G = GemmTile<BN>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -81,6 +85,13 @@ __global__ void __launch_bounds__(kThreads, BN <= 64 ? 2 : 1)
     tma_prefetch_map(&ta);
     tma_prefetch_map(&tb);
   }
+  __shared__ float s_bias[BN];
+  for (int t = threadIdx.x; t < BN; t += blockDim.x) s_bias[t] = (e.bias && n0 + t < e.N) ? e.bias[n0 + t] : 0.f;
+  // 16-byte vector stores/loads need 16-byte aligned rows
+  const bool vec_bf16 = e.out_bf16 && (e.ld_bf16 % 8) == 0 && (reinterpret_cast<uintptr_t>(e.out_bf16) & 15) == 0;
+  const bool vec_f32 = e.out_f32 && (e.ldo % 4) == 0 && (reinterpret_cast<uintptr_t>(e.out_f32) & 15) == 0;
+  const bool vec_z = e.z_out && (e.ldz % 4) == 0 && (reinterpret_cast<uintptr_t>(e.z_out) & 15) == 0;
+  const bool vec_zin = e.zin && (e.ldzin % 4) == 0 && (reinterpret_cast<uintptr_t>(e.zin) & 15) == 0;
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -88,8 +99,8 @@ __global__ void __launch_bounds__(kThreads, BN <= 64 ? 2 : 1)
 
   // Row tiles blockIdx.x, blockIdx.x + gridDim.x, ... below the row count: the ring's stage and
   // phase follow the k-step count over all tiles so far (g), the accumulator's phase the tile
-  // count (iter).  Each tile ends with a CTA barrier, after which the accumulator and the
-  // stages (the epilogue's staging) are free for the next tile.
+  // count (iter).  Each tile ends with a CTA barrier, after which the accumulator is free for
+  // the next tile.
   int iter = 0;
   for (int mt = blockIdx.x; mt < m_tiles; mt += gridDim.x, iter++) {
   const int m0 = mt * kBM;
@@ -141,60 +152,102 @@ __global__ void __launch_bounds__(kThreads, BN <= 64 ? 2 : 1)
     tc_fence_after();
     const int quarter = warp & 3, half = warp >> 2;
     const int row = m0 + quarter * 32 + lane;
+    const bool row_ok = row < m_rows && ok;
     const uint32_t t_row = tmem + ((uint32_t)(quarter * 32) << 16);
-    // Row-major outputs go through shared memory (the freed pipeline stages): each thread holds
-    // one row, so storing straight from registers would touch 32 sectors per warp store.  A
-    // 32 x 32 tile per warp is written by rows and stored with the lanes along the columns.
-    // Transposed outputs are already coalesced from registers (consecutive lanes = rows).
-    float* st_x = reinterpret_cast<float*>(smem_raw + (base - raw)) + warp * (2 * 32 * kStagePitch);
-    float* st_z = st_x + 32 * kStagePitch;
-    const bool rowmajor = e.out_f32 || e.out_bf16 || e.z_out;
+    // Each thread holds one output row: its 32 columns per chunk are contiguous in a row-major
+    // output, so they are stored as 16-byte vectors straight from registers (a few stores per
+    // chunk instead of one per element); transposed outputs are coalesced from registers
+    // (consecutive lanes = consecutive rows).
     for (int c = half * (BN / 2); c < (half + 1) * (BN / 2); c += kStageCols) {
       if (n0 + c >= e.N) break;  // uniform over the warp
+      const int nv = min(kStageCols, e.N - (n0 + c));  // valid columns in this chunk
       float v[kStageCols];
       tmem_ld32(t_row + (uint32_t)c, v);
+      float z[kStageCols];
+#pragma unroll
+      for (int i = 0; i < kStageCols; i++) z[i] = 0.f;
+      if (ACT == kActSiluGrad && row_ok) {
+        const float* zr = e.zin + (size_t)row * e.ldzin + n0 + c;
+        if (nv == kStageCols && vec_zin) {
+#pragma unroll
+          for (int q = 0; q < kStageCols / 4; q++) {
+            const float4 t = *reinterpret_cast<const float4*>(zr + 4 * q);
+            z[4 * q] = t.x; z[4 * q + 1] = t.y; z[4 * q + 2] = t.z; z[4 * q + 3] = t.w;
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < kStageCols; i++) z[i] = i < nv ? zr[i] : 0.f;
+        }
+      }
 #pragma unroll
       for (int i = 0; i < kStageCols; i++) {
-        const int n = n0 + c + i;
-        float x = v[i], z = 0.f;
-        if (row < m_rows && n < e.N) {
-          if (e.bias) x += e.bias[n];
-          z = x;
-          if (ACT == kActSilu) {
-            x = x * sigmoid_fast(x);
-          } else if (ACT == kActSiluGrad) {
-            const float zi = e.zin[(size_t)row * e.ldzin + n];
-            const float sg = sigmoid_fast(zi);
-            x *= sg * (1.0f + zi * (1.0f - sg));
-          }
-          if (e.out_bf16_t && ok) e.out_bf16_t[(size_t)n * e.ldt + row] = __float2bfloat16_rn(x);
+        float x = v[i] + s_bias[c + i];
+        if (ACT == kActSilu) {
+          z[i] = x;
+          x = x * sigmoid_fast(x);
+        } else if (ACT == kActSiluGrad) {
+          const float sg = sigmoid_fast(z[i]);
+          x *= sg * (1.0f + z[i] * (1.0f - sg));
+        } else {
+          z[i] = x;
         }
-        st_x[lane * kStagePitch + i] = x;
-        if (e.z_out) st_z[lane * kStagePitch + i] = z;
+        v[i] = x;
       }
-      __syncwarp();
-      if (rowmajor && ok) {
-        const int j = lane, n = n0 + c + lane;
-        if (j < min(kStageCols, e.N - (n0 + c))) {
-          for (int r = 0; r < 32; r++) {
-            const int gr = m0 + quarter * 32 + r;
-            if (gr >= m_rows) break;
-            const float x = st_x[r * kStagePitch + j];
-            if (e.out_f32) e.out_f32[(size_t)gr * e.ldo + n] = x;
-            if (e.out_bf16) e.out_bf16[(size_t)gr * e.ld_bf16 + n] = __float2bfloat16_rn(x);
-            if (e.z_out) e.z_out[(size_t)gr * e.ldz + n] = st_z[r * kStagePitch + j];
+      if (e.out_bf16_t && row_ok) {
+#pragma unroll
+        for (int i = 0; i < kStageCols; i++)
+          if (i < nv) e.out_bf16_t[(size_t)(n0 + c + i) * e.ldt + row] = __float2bfloat16_rn(v[i]);
+      }
+      if (!row_ok) continue;
+      const bool full = nv == kStageCols;
+      if (e.out_bf16) {
+        __nv_bfloat16* o = e.out_bf16 + (size_t)row * e.ld_bf16 + n0 + c;
+        if (full && vec_bf16) {
+#pragma unroll
+          for (int q = 0; q < kStageCols / 8; q++) {
+            uint4 u;
+            u.x = pack_bf16x2(v[8 * q], v[8 * q + 1]);
+            u.y = pack_bf16x2(v[8 * q + 2], v[8 * q + 3]);
+            u.z = pack_bf16x2(v[8 * q + 4], v[8 * q + 5]);
+            u.w = pack_bf16x2(v[8 * q + 6], v[8 * q + 7]);
+            *reinterpret_cast<uint4*>(o + 8 * q) = u;
           }
+        } else {
+#pragma unroll
+          for (int i = 0; i < kStageCols; i++)
+            if (i < nv) o[i] = __float2bfloat16_rn(v[i]);
         }
       }
-      __syncwarp();
+      if (e.out_f32) {
+        float* o = e.out_f32 + (size_t)row * e.ldo + n0 + c;
+        if (full && vec_f32) {
+#pragma unroll
+          for (int q = 0; q < kStageCols / 4; q++)
+            *reinterpret_cast<float4*>(o + 4 * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < kStageCols; i++)
+            if (i < nv) o[i] = v[i];
+        }
+      }
+      if (ACT != kActSiluGrad && e.z_out) {
+        float* o = e.z_out + (size_t)row * e.ldz + n0 + c;
+        if (full && vec_z) {
+#pragma unroll
+          for (int q = 0; q < kStageCols / 4; q++)
+            *reinterpret_cast<float4*>(o + 4 * q) = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < kStageCols; i++)
+            if (i < nv) o[i] = z[i];
+        }
+      }
     }
   } else {
     atomicOr(e.err, e.err_bit);
     ok = false;
   }
   if (!ok) s_fail = 1;
-  // the staging writes above precede the next tile's TMA writes into the same stages
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -244,16 +297,16 @@ cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int 
   if (attr != cudaSuccess) return attr;
   CUtensorMap ta, tb;
   if (!make_map(&ta, A, e.M, e.K, lda, kBM) || !make_map(&tb, B, e.N, e.K, ldb, BN)) return cudaErrorInvalidValue;
-  // at most one wave of CTAs; each loops over row tiles (rows beyond *m_dyn are never visited)
+  // at most one wave of CTAs, two per SM (shared memory <= 2 x 101.5 KB, tensor memory <= 2 x 128
+  // columns, <= 128 registers per thread); each loops over row tiles, and rows beyond *m_dyn are
+  // never visited
   static int max_ctas = 0;
   static std::once_flag once_occ;
   std::call_once(once_occ, [] {
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_bf16<BN, ACT>, kThreads, G::kSmem) ==
-            cudaSuccess)
-      max_ctas = sms * std::max(1, per_sm);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      max_ctas = 2 * sms;
   });
   const int tiles_m = (e.M + kBM - 1) / kBM, tiles_n = (e.N + BN - 1) / BN;
   const int gx = max_ctas > 0 ? std::min(tiles_m, std::max(1, max_ctas / tiles_n)) : tiles_m;

@@ -178,12 +178,23 @@ __global__ void __launch_bounds__(128) k_far_classify(FarArgs a) {
   for (int c = warp; c < ncand; c += nw) {
     const int j = a.cand[(size_t)i * a.cand_cap + c];
     float d2 = 3.0e38f;
+    bool near = j == i;
     if (j != i) {
-      for (int jj = lane; jj < np; jj += 32) {
-        const int4 pj = a.pos32[(size_t)j * np + jj];
-        for (int ii = 0; ii < np; ii++) {
-          const float3 d = dpos(s_pa[ii], pj, unit);
-          d2 = fminf(d2, dot3_(d, d));
+      // closest bead pair; stops as soon as any bead pair is inside the switch radius (a near
+      // pair needs no distance, and sqrtf is monotone, so the partial minimum decides it)
+      for (int base = 0; base < np && !near; base += 32) {
+        const int jj = base + lane;
+        const int4 pj = a.pos32[(size_t)j * np + min(jj, np - 1)];
+        for (int i0 = 0; i0 < np; i0 += 8) {
+          const int i1 = min(np, i0 + 8);
+          for (int ii = i0; ii < i1; ii++) {
+            const float3 d = dpos(s_pa[ii], pj, unit);
+            d2 = fminf(d2, dot3_(d, d));
+          }
+          if (__any_sync(0xffffffffu, sqrtf(d2) < a.r_switch)) {
+            near = true;
+            break;
+          }
         }
       }
 #pragma unroll
@@ -191,7 +202,7 @@ __global__ void __launch_bounds__(128) k_far_classify(FarArgs a) {
     }
     if (lane == 0) {
       const float dmin = sqrtf(d2);
-      bool far = (j != i) && dmin >= a.r_switch;
+      bool far = !near && dmin >= a.r_switch;
       // a far pair with every bead pair beyond every cut-off exerts no force: it is left out of
       // both the pair list and the far list (2)
       const bool inert = far && d2 > s_reach2;
@@ -207,29 +218,61 @@ __global__ void __launch_bounds__(128) k_far_classify(FarArgs a) {
   if (threadIdx.x == 0) a.far_count[i] = s_cnt;
 }
 
-// exclusive scan of far_count over all subunits in one CTA of 1024 threads
+// exclusive scan of far_count over all subunits in one CTA of 1024 threads: chunks of 8192
+// counts staged in shared memory with coalesced loads, eight consecutive counts per thread, a
+// warp scan and a scan of the warp totals, the running total carried between chunks
 __global__ void __launch_bounds__(1024) k_far_scan(FarArgs a) {
-  __shared__ int s[1024];
-  const int n = a.S, t = threadIdx.x;
-  const int per = (n + 1023) / 1024;
-  const int lo = min(n, t * per), hi = min(n, lo + per);
-  int sum = 0;
-  for (int i = lo; i < hi; i++) sum += a.far_count[i];
-  s[t] = sum;
+  constexpr int kChunk = 8192, kPer = kChunk / 1024;
+  __shared__ int s_v[kChunk];
+  __shared__ int s_w[32];
+  __shared__ int s_carry;
+  const int n = a.S, t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  if (t == 0) s_carry = 0;
   __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    const int v = t >= o ? s[t - o] : 0;
+  for (int c0 = 0; c0 < n; c0 += kChunk) {
+    const int m = min(kChunk, n - c0);
+    for (int i = t; i < kChunk; i += 1024) s_v[i] = i < m ? a.far_count[c0 + i] : 0;
     __syncthreads();
-    s[t] += v;
+    int v[kPer], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      v[k] = s_v[t * kPer + k];
+      sum += v[k];
+    }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_w[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      int x = s_w[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      s_w[lane] = x;
+    }
+    __syncthreads();
+    int run = s_carry + (wid ? s_w[wid - 1] : 0) + incl - sum;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      s_v[t * kPer + k] = run;
+      run += v[k];
+    }
+    const int chunk_total = s_w[31];
+    __syncthreads();
+    for (int i = t; i < m; i += 1024) a.far_start[c0 + i] = s_v[i];
+    if (t == 0) s_carry += chunk_total;
     __syncthreads();
   }
-  const int total = s[1023];
+  const int total = s_carry;
   const bool ok = total <= a.far_cap;
-  int run = s[t] - sum;
-  for (int i = lo; i < hi; i++) {
-    a.far_start[i] = ok ? run : 0;
-    run += a.far_count[i];
-  }
+  if (!ok)  // an overflowed list is empty
+    for (int i = t; i < n; i += 1024) a.far_start[i] = 0;
   if (t == 0) {
     a.far_start[n] = ok ? total : 0;
     a.far_total[0] = ok ? total : 0;

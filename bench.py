@@ -16,8 +16,19 @@ Verlet, the pair-list rebuild every 10th step, forces, centre-of-mass velocity r
   cpu_baseline / --impl reference: the oracle port of the reference algorithm (long double,
          OpenMP over subunits, all host cores) on a bounded sample of the same workload.
 
+  surrogate_batched (default run, N = 1): the replica sweep (256 systems of 20-500 capsomeres,
+         per-system attraction, screening length 0.5-2 sigma and concentration) with the
+         learned far-field surrogate, trained on the GPU from exact far-pair data of the same
+         run, against the plain GPU path (each replica alone, exact forces): throughput gain,
+         total-force RMS error, temperature and potential-energy statistics.
+
 --surrogate: the learned far-field surrogate (include/souffle_surrogate.h) against the plain
-path on the same workload and protocol; --replicas N: a batch of N uneven systems in one handle;
+path on one system (--debye-length, --concentration set its parameters); --replicas N: a batch
+of N uneven systems in one handle (--replica-subunits S: N systems of S subunits at the plain
+workload's parameters; with --surrogate: the surrogate+batched measurement alone);
+--gemm: the surrogate network's forward pass at several row counts against the tensor peak;
+--profile: a few steps without autotuning or timing, for a profiler (plain, --replicas, or
+--replicas --surrogate after training);
 --analysis: the post-run trajectory analysis (include/souffle_analysis.h), frames/s on frames of
 2000 43-bead capsomeres (86,000 beads).
 
@@ -129,6 +140,10 @@ def bench_replicas(args):
     params = [gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local) for w in reps]
     s = gpu.GpuSystem(reps[0].template, params)
     s.set_state(np.concatenate([w.state.pos for w in reps]), np.concatenate([w.state.vel for w in reps]))
+    if args.profile:  # a few plain steps for a profiler, no autotuning
+        s.md_begin()
+        print(json.dumps(s.md_profile(0, args.steps)))
+        return
     tuning = s.autotune(trials=20)
     s.md_begin()
     n = s.n
@@ -305,6 +320,10 @@ def bench_surrogate(args):
 
 
 def bench_surrogate_batched(args):
+    print(json.dumps(surrogate_batched(args)))
+
+
+def surrogate_batched(args):
     """Surrogate + batching against the plain GPU path on the replica sweep: 256 independent
     systems of 20-500 bilayer capsomeres with per-system attraction, screening length (0.5-2
     sigma) and concentration (200-1600 uM).  One network is trained on exact far-pair data from
@@ -414,6 +433,12 @@ def bench_surrogate_batched(args):
                 "judge": {"judged": st["judged"], "classes_off": st["classes_off"],
                           "last_error": st["last_error"]} if st else None}
 
+    if getattr(args, "profile", False):  # surrogate steps only, for a profiler's launch list
+        gpu.surrogate_enable(s, True)
+        s.set_state(pos, vel)
+        s.md_begin()
+        s.md_steps(0, args.steps)
+        return {"profile_steps": args.steps, "far_pairs": gpu.surrogate_stats(s)["far_pairs"]}
     batched = run_batch(False)
     surr = run_batch(True)
     s.close()
@@ -443,7 +468,7 @@ def bench_surrogate_batched(args):
         si.close()
     plain_value = plain_beads * k / (plain_ms / 1e3)
     sizes = [int(w.opt.S) for w in reps]
-    print(json.dumps({
+    return {
         "metric": "bead-steps/s on 1 GB300: surrogate+batched vs plain GPU at <=1e-3 force RMS err",
         "value": surr["value"], "unit": "bead-steps/s", "n_gpus": 1, "steps": k, "warmup": 2 * B,
         "ms_per_step": surr["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -468,7 +493,48 @@ def bench_surrogate_batched(args):
                             for i in watch},
         "training": {"rows": total, "frames": frames, "epochs": args.epochs, "batch": batch,
                      "final_loss_normalised": loss, "collect_s": collect_s, "fit_s": fit_s},
-        "generation_s": gen_s}))
+        "generation_s": gen_s}
+
+
+def bench_gemm(args):
+    """The surrogate network's forward pass (64 -> 256 -> 256 -> 256 -> 132, BF16 operands, FP32
+    accumulation; packing, four tcgen05 GEMMs, unpadding) at several row counts, wall clock
+    around synchronised calls through the C ABI, against the measured BF16 tensor peak."""
+    import torch
+    from souffle_gb300 import gpu
+    torch.cuda.set_device(0)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    rows = []
+    for m in (8192, 32768, 118016):
+        net = gpu.Mlp(64, 132, max_batch=m, seed=1)
+        x = torch.randn(m, 64, device="cuda")
+        y = torch.empty(m, 132, device="cuda")
+        for _ in range(3):
+            net.forward(x.data_ptr(), m, y.data_ptr())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            net.forward(x.data_ptr(), m, y.data_ptr())
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / args.steps
+        flop = 2.0 * m * (64 * 256 + 2 * 256 * 256 + 256 * 144)
+        rows.append({"rows": m, "us_per_forward": dt * 1e6, "tflops": flop / dt / 1e12})
+        net.close()
+    best = rows[-1]
+    print(json.dumps({
+        "metric": "surrogate network forward TFLOP/s", "value": best["tflops"], "unit": "TFLOP/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": 3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic",
+        "config": {"workload": "surrogate MLP 64-256-256-256-132 forward, padded output 144"},
+        "per_rows": rows,
+        "roofline": {"bound": "tensor", "achieved": best["tflops"], "peak": peak, "unit": "TFLOP/s",
+                     "frac": best["tflops"] / peak,
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured)" if peaks else "fallback 1900"}}))
 
 
 def cpu_analysis_port(n_sub: int, seconds: float = 10.0):
@@ -636,11 +702,17 @@ def main():
     ap.add_argument("--debye-length", type=float, default=0.0,
                     help="screening length in sigma (default 1: -c 94.27)")
     ap.add_argument("--concentration", type=float, default=0.0, help="subunits in uM (default 800)")
+    ap.add_argument("--gemm", action="store_true",
+                    help="the surrogate network's forward pass (tcgen05 GEMMs) at several row counts")
+    ap.add_argument("--no-surrogate-batched", action="store_true",
+                    help="skip the replica-sweep surrogate+batched measurement in the default run")
     ap.add_argument("--plain-sample", type=int, default=256,
                     help="with --replicas --surrogate: replicas timed alone for the plain path")
     ap.add_argument("--far-per-subunit", type=int, default=4,
                     help="surrogate far-pair list capacity per subunit")
     args = ap.parse_args()
+    if args.gemm:
+        return bench_gemm(args)
     if args.replicas and args.surrogate:
         return bench_surrogate_batched(args)
     if args.replicas:
@@ -823,6 +895,25 @@ def main():
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference(w, seconds=args.cpu_seconds)
+    if rank == 0 and world == 1 and not args.no_surrogate_batched:
+        # the replica sweep with the learned surrogate against the plain single-system path
+        s.close()
+        try:
+            sb = surrogate_batched(argparse.Namespace(
+                replicas=256, far_per_subunit=16, steps=100, stat_steps=400, plain_sample=64, profile=False,
+                train_rows=args.train_rows, max_frames=args.max_frames, epochs=args.epochs))
+            out["surrogate_batched"] = {k: sb[k] for k in (
+                "metric", "value", "unit", "gain", "gain_batching", "gain_surrogate", "config",
+                "force_rms_rel_error", "force_rms_rel_error_worst_system", "far_pairs")}
+            out["surrogate_batched"]["plain_value"] = sb["plain"]["value"]
+            out["surrogate_batched"]["batched_value"] = sb["batched"]["value"]
+            out["surrogate_batched"]["judge"] = sb["surrogate"]["judge"]
+            out["surrogate_batched"]["statistics"] = {
+                "T_mean": {"exact": sb["batched"]["T_mean"], "surrogate": sb["surrogate"]["T_mean"]},
+                "potential_mean": {"exact": sb["batched"]["potential_mean"],
+                                   "surrogate": sb["surrogate"]["potential_mean"]}}
+        except Exception as ex:  # the main line stands on its own
+            out["surrogate_batched"] = {"error": f"{type(ex).__name__}: {ex}"}
     if rank == 0:
         print(json.dumps(out))
     if dist:

@@ -61,7 +61,7 @@ struct ForceArgs {
   const SysParams* sys;
   SysState* state;
   const WorkItem* work;
-  const int2* sys_slots;     // per system: first work item, work-item (CTA) count
+  const int2* sys_slots;     // per system: first work item in system order, work-item (CTA) count
   const int4* pos32;
   const unsigned int* intra_mask;
   const int* inter_ids;      // [N][inter_cap] row-major, ascending

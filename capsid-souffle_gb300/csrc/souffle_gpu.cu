@@ -504,6 +504,24 @@ souffle_status plan_work(souffle_gpu_system* h, int subs, int threads) {
     slots.push_back(make_int2(first, (int)work.size() - first));
     sub0 += n;
   }
+  if (h->n_sys > 1) {
+    // Systems of a batch differ in pair density, so their items differ in cost: costliest items
+    // first (longest-processing-time order), so that the cheap ones fill the SMs at the end of
+    // the grid instead of a few long ones running alone.  Estimated cost of a subunit: its
+    // beads' intra-subunit pairs plus the inter-subunit pairs inside the list radius at the
+    // system's bead density.  Results do not depend on the order (exact integer sums).
+    const int np = h->tpl.np;
+    std::vector<double> cost(h->n_sys);
+    for (int k = 0; k < h->n_sys; k++) {
+      const souffle_params& q = h->prm[k];
+      const double rho = (double)q.n_subunits * np / (q.box * q.box * q.box);
+      const double r = q.nlist_cutoff;
+      cost[k] = np + rho * 4.18879 * r * r * r;  // 4/3 pi r^3
+    }
+    std::stable_sort(work.begin(), work.end(), [&](const WorkItem& x, const WorkItem& y) {
+      return cost[x.sys] * x.nsub > cost[y.sys] * y.nsub;
+    });
+  }
   CUDA_TRY(h->d_work.alloc(work.size()));
   CUDA_TRY(cudaMemcpy(h->d_work.p, work.data(), sizeof(WorkItem) * work.size(), cudaMemcpyHostToDevice));
   CUDA_TRY(h->d_slots.alloc(slots.size()));

@@ -435,9 +435,13 @@ __device__ void far_descr_one(const FarArgs& a, int p) {
   x[37] = 1.0f / P.kappa;
   x[38] = P.elj_att;
   x[39] = a.far_dmin[p];
-  float* out = a.x + (size_t)p * kDesc;
+  if (a.x_mean) {
 #pragma unroll
-  for (int k = 0; k < kDesc; k++) out[k] = a.x_mean ? (x[k] - a.x_mean[k]) * a.x_istd[k] : x[k];
+    for (int k = 0; k < kDesc; k++) x[k] = (x[k] - a.x_mean[k]) * a.x_istd[k];
+  }
+  float4* out = reinterpret_cast<float4*>(a.x + (size_t)p * kDesc);  // 256-byte rows
+#pragma unroll
+  for (int k = 0; k < kDesc / 4; k++) out[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
 }
 
 // force on this lane's beads of subunit A (body frame) from the network output row of one pair

@@ -7,6 +7,8 @@
 //                     j > i of the system (no pair list, no prefilter), energy credited to i;
 //                     shifted Debye-Hueckel, WCA (+1 shift), and attractive LJ shifted at ecut
 //                     with sbar^6 and epsilon = -E.
+//   k_energy_bigbeads update_LJ_ES_energies_bigbeads (src/energies.cpp:96-137) when the system
+//                     has encapsulation big beads
 //   k_energy_totals   per-system sums in bead order (src/md.cpp:586-594).
 // A float test on the high words skips pairs beyond every cut-off; the rest use exact
 // fixed-point differences in double.
@@ -174,6 +176,66 @@ __global__ void __launch_bounds__(128) k_energy_pairs(EnergyArgs a) {
   }
 }
 
+// Encapsulation big beads (update_LJ_ES_energies_bigbeads, src/energies.cpp:96-137): per
+// subunit bead, the unshifted screened Coulomb energy with each big bead inside the DH cut-off
+// (none without one) and the shifted WCA energy (+1) inside delta + 2^(1/6) shc, added to the
+// bead's ne / ce (the reference credits them to the subunit bead and to the big bead) and kept
+// apart for the big-bead totals.  Exact fixed-point differences in double.
+__global__ void __launch_bounds__(128) k_energy_bigbeads(EnergyArgs a) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.n) return;
+  const SysParams& P = a.sys[a.sysid];
+  const int gi = a.n0 + t, li = gi % a.L.np;
+  const double qj = a.q[li], sgj = a.sigma[li];
+  const double kappa = a.kappa, lb = a.lb, ecut_el = a.ecut_el;
+  const double shc = P.bb_shc_d, sigb = P.bb_sigma_d;
+  const double sigavg = (sigb + sgj) / 2;
+  const double delta = sigavg - shc;
+  const double shc6 = pow(shc, 6);
+  const double ys = exp(kappa * sigavg) / ((1 + kappa * sigb / 2) * (1 + kappa * sgj / 2));
+  double ce = 0.0, ne = 0.0;
+  for (int k = 0; k < P.nbb; k++) {
+    const int b = P.bb0 + k;
+    const double x = fixed_diff(a.bb_fx[b], a.px[gi], P.fx_to_len);
+    const double y = fixed_diff(a.bb_fx[a.bb_total + b], a.py[gi], P.fx_to_len);
+    const double z = fixed_diff(a.bb_fx[2 * a.bb_total + b], a.pz[gi], P.fx_to_len);
+    const double r = sqrt(x * x + y * y + z * z);
+    const double r6 = pow(r - delta, 6);
+    if (qj != 0 && r < ecut_el) ce += (P.bb_q * qj * lb * exp(-kappa * r) * ys) / r;
+    if (r < delta + 1.12246205 * shc) ne += (4 * (shc6 / r6) * ((shc6 / r6) - 1)) + 1;
+  }
+  a.ne[t] += ne;
+  a.ce[t] += ce;
+  a.ne_bb[t] = ne;
+  a.ce_bb[t] = ce;
+}
+
+// Big-bead energy totals (lj, electrostatic) in bead order with a fixed tree, one CTA.
+__global__ void k_energy_bb_totals(EnergyArgs a) {
+  __shared__ double red[2][512];
+  double s0 = 0, s1 = 0;
+  const int per = (a.n + blockDim.x - 1) / blockDim.x;
+  const int beg = threadIdx.x * per, end = min(a.n, beg + per);
+  for (int t = beg; t < end; t++) {
+    s0 += a.ne_bb[t];
+    s1 += a.ce_bb[t];
+  }
+  red[0][threadIdx.x] = s0;
+  red[1][threadIdx.x] = s1;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    a.bb_totals[0] = red[0][0];
+    a.bb_totals[1] = red[1][0];
+  }
+}
+
 // Totals in bead order with a fixed tree: one CTA of 1024 threads per call.
 __global__ void k_energy_totals(EnergyArgs a) {
   __shared__ double red[5][1024];
@@ -205,6 +267,10 @@ void launch_energies(const EnergyArgs& a, int n, cudaStream_t s) {
   const int g = (n + 127) / 128;
   k_energy_bonded<<<g, 128, 0, s>>>(a);
   k_energy_pairs<<<g, 128, 0, s>>>(a);
+  if (a.bb_totals) {
+    k_energy_bigbeads<<<g, 128, 0, s>>>(a);
+    k_energy_bb_totals<<<1, 512, 0, s>>>(a);
+  }
   k_energy_totals<<<1, 1024, 0, s>>>(a);
 }
 }  // namespace souffle

@@ -7,6 +7,8 @@
 //                (src/edge.cpp:69-188) over FACE::update_area_normal (src/face.cpp:11-17)
 //   pair terms   the neighbour loop of src/forces.cpp:67-145: Debye-Hueckel for charged pairs,
 //                then attractive LJ (directed table) or WCA for pairs in different subunits.
+//   big beads    forceCalculation_bigbead (src/forces.cpp:174-236) when the system has
+//                encapsulation big beads: added to the bead's total in the per-bead phase.
 // Forces are evaluated in FP32 from exact integer coordinate differences.  Two threads share a
 // bead (one takes stretching and the even intra/inter neighbours, the other bending and the odd
 // ones); their partial sums are combined in 64-bit fixed point (2^-32 units), so the total does
@@ -413,6 +415,37 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   for (int t = threadIdx.x; t < nbead; t += blockDim.x) {
     const int l = t % np, g = bead0 + t;
     long long Fx = limbs_value(s_F + 9 * t), Fy = limbs_value(s_F + 9 * t + 3), Fz = limbs_value(s_F + 9 * t + 6);
+    if (P.nbb) {
+      // encapsulation big beads (forceCalculation_bigbead, src/forces.cpp:192-227): for each big
+      // bead, r = big - subunit; screened Coulomb (q_big q_j lb e^(-kappa r) / r^2 (kappa + 1/r)
+      // times the Yukawa size factor) and WCA with hard-core distance shc shifted by delta =
+      // (sigma_big + sigma_j)/2 - shc; the subunit bead takes minus their sum
+      const int4 pi = s_pos[t];
+      const float wl = s_w[l];
+      const float delta = 0.5f * (P.bb_sigma + tpl_f[L.o_sigma + l]) - P.bb_shc;
+      const float wc = delta + 1.12246205f * P.bb_shc;
+      const float s3 = P.bb_shc * P.bb_shc * P.bb_shc, shc6 = s3 * s3;
+      float3 fb = f3(0.f, 0.f, 0.f);
+      for (int k = 0; k < P.nbb; k++) {
+        const float3 d = dvec(__ldg(&a.bb_pos32[P.bb0 + k]), pi, unit);
+        const float r2 = dot3(d, d);
+        const float r = sqrtf(r2);
+        float c = 0.f;
+        if (wl != 0.f && r2 < P.bb_dh_cut2) c = P.bb_w * wl * __expf(-kappa * r) / r2 * (kappa + 1.0f / r);
+        if (r2 < wc * wc) {
+          const float x = r - delta;
+          const float x3 = x * x * x, s6 = shc6 / (x3 * x3);
+          c += 48.0f * s6 * (s6 - 0.5f) / r / x;
+        }
+        fb = fb - d * c;
+      }
+      if (!(isfinite(fb.x) && isfinite(fb.y) && isfinite(fb.z)) ||
+          fmaxf(fmaxf(fabsf(fb.x), fabsf(fb.y)), fabsf(fb.z)) > 1.0e9f)
+        atomicOr(a.err, kErrNonFinite);
+      Fx += f32_to_fx32(fb.x);
+      Fy += f32_to_fx32(fb.y);
+      Fz += f32_to_fx32(fb.z);
+    }
     if (bd) {
       // Brownian: tforce + (fran - mean fran over the system) + fdrag (src/md.cpp:468-494,
       // src/bead.h:147-149)

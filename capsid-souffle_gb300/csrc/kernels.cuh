@@ -68,6 +68,7 @@ struct ForceArgs {
   const float4* surr_f = nullptr;  // [N] far-field forces from the surrogate, or null
   const long long* fdrag = nullptr;  // Brownian: [3][N] drag and random force of the step
   const long long* fran = nullptr;
+  const int4* bb_pos32 = nullptr;  // encapsulation big beads: high words of their positions
   const int* inter_count;
   int inter_cap;
   const float* dh_w;         // [n_sys * np] q * exp(kappa sigma/2)/(1 + kappa sigma/2) * sqrt(lb)
@@ -153,6 +154,12 @@ struct EnergyArgs {
   int n0, n;               // first bead of the system, beads in it
   double* se; double* be; double* ne; double* ce; double* ke;  // [n] (system-local)
   double* totals;          // [8] per call
+  // encapsulation big beads of the system: fixed-point positions [3][total], the big-bead parts
+  // of ne and ce per subunit bead [n] and their sums ([2]: lj, electrostatic)
+  const long long* bb_fx = nullptr;
+  int bb_total = 0;
+  double* ne_bb = nullptr; double* ce_bb = nullptr;
+  double* bb_totals = nullptr;
 };
 
 void launch_cells_count(const CellArgs& a, int grid, int block, cudaStream_t s);

@@ -77,7 +77,14 @@ struct SysParams {
   double ks_d, kb_d;        // double copies for the FP64 energy pass
   long long drift_fx;       // dt 2^32 / L in 2^-40 units: x_fixed += v_fixed * drift_fx >> 40
   int brownian;             // Brownian dynamics (src/md.cpp:415-431, 461-501) instead of the NHC
-  unsigned int lcg_step;    // Brownian noise: 16807^(6 n_beads) mod (2^31 - 1), one step of draws
+  unsigned int lcg_step;    // Brownian noise: 16807^(6 (n_beads + big beads)) mod (2^31 - 1), one step of draws
+  // encapsulation big beads (src/forces.cpp:174-236): first index and count in the handle's
+  // big-bead arrays; DH weight q e^(kappa sigma/2) / (1 + kappa sigma/2) sqrt(lb), diameter,
+  // hard-core distance, DH cut-off squared (0 without a cut-off: the reference's test
+  // r^2 < ecut_el^2 then never holds); double copies for the energy pass
+  int bb0, nbb;
+  float bb_w, bb_sigma, bb_shc, bb_dh_cut2;
+  double bb_q, bb_sigma_d, bb_shc_d;
 };
 
 // Thermostat chain and step scalars of one system, updated on the device.

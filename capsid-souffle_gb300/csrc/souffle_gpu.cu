@@ -405,6 +405,7 @@ ForceArgs force_args(souffle_gpu_system* h, int mode, bool want_parts) {
   a.n_beads_total = (int)N;
   a.fdrag = h->bd_fdrag.p;
   a.fran = h->bd_fran.p;
+  a.bb_pos32 = h->bb_pos32.p;
   a.max_sub = h->subs_per_cta;
   a.mode = mode;
   return a;
@@ -742,6 +743,73 @@ souffle_status souffle_gpu_destroy(souffle_gpu_system* h) {
 
 int64_t souffle_gpu_num_beads(const souffle_gpu_system* h) { return h ? h->N : 0; }
 
+souffle_status souffle_gpu_set_big_beads(souffle_gpu_system* h, int32_t system, int32_t n, const double* pos,
+                                         double sigma, double charge, double shc) {
+  constexpr int kMaxBigBeads = 4096;  // per system: each subunit bead loops over them every step
+  if (!h || system < 0 || system >= h->n_sys || n < 0 || (n > 0 && !pos))
+    return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  if (n > kMaxBigBeads) return fail(SOUFFLE_ERR_BAD_INPUT, "at most 4096 big beads per system");
+  if (n > 0 && !(sigma > 0 && shc > 0 && std::isfinite(charge) && std::isfinite(sigma) && std::isfinite(shc)))
+    return fail(SOUFFLE_ERR_BAD_INPUT, "big-bead diameter and hard-core distance must be positive");
+  for (int i = 0; i < 3 * n; i++)
+    if (!std::isfinite(pos[i]) || std::fabs(pos[i]) > 0.75 * h->prm[system].box)
+      return fail(SOUFFLE_ERR_BAD_INPUT, "big-bead position outside the box");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if ((int)h->bb_pos.size() != h->n_sys) h->bb_pos.resize(h->n_sys);
+  h->bb_pos[system].assign(pos, pos + 3 * (size_t)n);
+  const souffle_params& q = h->prm[system];
+  SysParams& P = h->sp[system];
+  P.bb_q = charge;
+  P.bb_sigma_d = sigma;
+  P.bb_shc_d = shc;
+  // the Yukawa size factor exp(kappa (s1 + s2)/2) / ((1 + kappa s1/2)(1 + kappa s2/2)) splits
+  // into one weight per bead, as for the subunit beads' dh_w
+  P.bb_w = (float)(charge * std::exp(q.kappa * sigma / 2) / (1 + q.kappa * sigma / 2) * std::sqrt(q.lb));
+  P.bb_sigma = (float)sigma;
+  P.bb_shc = (float)shc;
+  P.bb_dh_cut2 = q.ecut_el > 0 ? (float)(q.ecut_el * q.ecut_el) : 0.0f;
+  if (q.brownian) {
+    // one step draws six numbers per subunit bead, then six per big bead (src/md.cpp:482-487)
+    unsigned int m6 = 1, r = 1;
+    for (int k = 0; k < 6; k++) m6 = lcg_mul(m6, 16807u);
+    for (long long e = (long long)q.n_subunits * h->tpl.np + n; e > 0; e >>= 1) {
+      if (e & 1) r = lcg_mul(r, m6);
+      m6 = lcg_mul(m6, m6);
+    }
+    P.lcg_step = r;
+  }
+  // all systems' big beads, in system order, as fixed point in each system's box
+  int total = 0;
+  for (int k = 0; k < h->n_sys; k++) total += (int)(h->bb_pos[k].size() / 3);
+  std::vector<int4> p32(std::max(total, 1), make_int4(0, 0, 0, 0));
+  std::vector<long long> fx(3 * (size_t)std::max(total, 1), 0);
+  for (int k = 0, b = 0; k < h->n_sys; k++) {
+    SysParams& Q = h->sp[k];
+    const int nk = (int)(h->bb_pos[k].size() / 3);
+    Q.bb0 = b;
+    Q.nbb = nk;
+    const double invL = 1.0 / Q.box;
+    for (int i = 0; i < nk; i++, b++) {
+      const long long X = fixed_from_fraction(h->bb_pos[k][3 * i] * invL);
+      const long long Y = fixed_from_fraction(h->bb_pos[k][3 * i + 1] * invL);
+      const long long Z = fixed_from_fraction(h->bb_pos[k][3 * i + 2] * invL);
+      fx[b] = X;
+      fx[(size_t)std::max(total, 1) + b] = Y;
+      fx[2 * (size_t)std::max(total, 1) + b] = Z;
+      p32[b] = make_int4(hi_word(X), hi_word(Y), hi_word(Z), k);
+    }
+  }
+  CUDA_TRY(h->bb_pos32.alloc(p32.size()));
+  CUDA_TRY(cudaMemcpy(h->bb_pos32.p, p32.data(), p32.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  CUDA_TRY(h->bb_fx.alloc(fx.size()));
+  CUDA_TRY(cudaMemcpy(h->bb_fx.p, fx.data(), fx.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(h->d_sys.p, h->sp.data(), sizeof(SysParams) * h->n_sys, cudaMemcpyHostToDevice));
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);  // captured arguments changed
+  h->graphs.clear();
+  return SOUFFLE_OK;
+}
+
 souffle_status souffle_gpu_set_state(souffle_gpu_system* h, const double* pos, const double* vel) {
   if (!h || !pos) return fail(SOUFFLE_ERR_BAD_INPUT, "null argument");
   CUDA_TRY(cudaSetDevice(h->opt.device));
@@ -934,7 +1002,7 @@ souffle_status souffle_gpu_energies(souffle_gpu_system* h, int32_t system, souff
   const SysParams& P = h->sp[system];
   const souffle_params& p = h->prm[system];
   const int n = P.n_sub * h->tpl.np;
-  if (h->e_bead.n < (size_t)5 * n) CUDA_TRY(h->e_bead.alloc((size_t)5 * n));
+  if (h->e_bead.n < (size_t)7 * n) CUDA_TRY(h->e_bead.alloc((size_t)7 * n));
   EnergyArgs a{};
   a.L = h->L;
   a.tpl_i = h->tpl_i.p;
@@ -971,11 +1039,20 @@ souffle_status souffle_gpu_energies(souffle_gpu_system* h, int32_t system, souff
   a.ce = h->e_bead.p + 3 * (size_t)n;
   a.ke = h->e_bead.p + 4 * (size_t)n;
   a.totals = h->e_tot.p;
+  if (P.nbb > 0) {  // encapsulation big beads
+    a.bb_fx = h->bb_fx.p;
+    a.bb_total = (int)(h->bb_fx.n / 3);
+    a.ne_bb = h->e_bead.p + 5 * (size_t)n;
+    a.ce_bb = h->e_bead.p + 6 * (size_t)n;
+    a.bb_totals = h->e_tot.p + 5;
+  }
   launch_energies(a, n, h->stream);
   CUDA_TRY(cudaGetLastError());
   double tot[8];
   SysState S;
-  CUDA_TRY(cudaMemcpyAsync(tot, h->e_tot.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, h->stream));
+  tot[5] = tot[6] = 0.0;
+  CUDA_TRY(cudaMemcpyAsync(tot, h->e_tot.p, sizeof(double) * (P.nbb > 0 ? 7 : 5), cudaMemcpyDeviceToHost,
+                           h->stream));
   CUDA_TRY(cudaMemcpyAsync(&S, h->d_state.p + system, sizeof(SysState), cudaMemcpyDeviceToHost, h->stream));
   double* outs[5] = {se, be, ne, ce, ke};
   const int order[5] = {0, 1, 2, 3, 4};
@@ -1001,6 +1078,8 @@ souffle_status souffle_gpu_energies(souffle_gpu_system* h, int32_t system, souff
     out->thermo_ke = tke;
     out->temperature = tot[0] * 2 / (3.0 * n);
     out->vcom_magnitude = S.vcom_mag;
+    out->bigbead_lj = tot[5];
+    out->bigbead_electrostatic = tot[6];
   }
   return SOUFFLE_OK;
 }

@@ -86,6 +86,11 @@ struct souffle_gpu_system {
   DevBuf<long long> bd_drag, bd_fdrag, bd_fran;
   DevBuf<double> bd_noise;
   DevBuf<unsigned int> lcg_table;
+  // encapsulation big beads: positions per system (host, [n][3] box coordinates, in system
+  // order) and on the device as fixed point (high words as int4, full words [3][total])
+  std::vector<std::vector<double>> bb_pos;
+  DevBuf<int4> bb_pos32;
+  DevBuf<long long> bb_fx;
   // graphs keyed by (2 window length + rebuild-first, mask of steps in the window that end with
   // a surrogate judgement)
   std::map<std::pair<int, unsigned long long>, cudaGraphExec_t> graphs;

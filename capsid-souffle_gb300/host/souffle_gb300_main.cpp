@@ -10,7 +10,11 @@
 // The MD loop (src/md.cpp:387-688, molecular-dynamics branch) runs on the GPU through the C ABI
 // in include/souffle_gpu.h; the host only steps between output points.  -D b runs the Brownian
 // branch (src/md.cpp:400-470) on the same path; as in src/md.cpp:109-116 any -D other than 'm'
-// selects Brownian dynamics.  Encapsulation (-p) is not part of the GPU path and is rejected.
+// selects Brownian dynamics.  Encapsulation (-p true) places -m static big beads (-a radius,
+// -G charge, -H hard-core distance) as generate_big_beads does (src/initialize.cpp:566-680: the
+// newest outfiles/rb_*.out on restart, else the C library's rand() after srand(0)) and writes
+//   outfiles/capenergy.out       src/md.cpp:347-351,625-629 (created empty without -p)
+//   outfiles/rb_<a>.out          src/md.cpp:537-545, beside each restart file
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -195,12 +199,12 @@ bool read_infile(const string& path, Infile& in) {
 
 // Newest restart file: names containing "restart", shortest-then-lexicographic order
 // (src/functions.cpp:262-311, src/initialize.cpp:166-191).
-string newest_restart(const string& dir) {
+string newest_file(const string& dir, const char* key) {
   vector<string> names;
   if (DIR* dp = opendir(dir.c_str())) {
     while (dirent* e = readdir(dp)) {
       string n = e->d_name;
-      if (n.find("restart") != string::npos) names.push_back(n);
+      if (n.find(key) != string::npos) names.push_back(n);
     }
     closedir(dp);
   }
@@ -249,11 +253,8 @@ int main(int argc, char** argv) {
 namespace {
 
 int run_simulation(const Options& o) {
-  if (o.p) {
-    fprintf(stderr, "souffle_gb300: encapsulation (-p true) is not part of the GPU path\n");
-    return 1;
-  }
   ofstream traj("outfiles/energy.out", ios_base::app);
+  ofstream encapdata("outfiles/capenergy.out", ios::out);
   ofstream ofile("outfiles/ovito.lammpstrj", ios_base::app);
   ofstream sysdata("outfiles/model.parameters.out", ios::out);
   if (!traj || !ofile || !sysdata) {
@@ -281,7 +282,7 @@ int run_simulation(const Options& o) {
   vector<double> pos(3 * N), vel(3 * N, 0.0);
   double box_x = pow((o.S * 1000 / (o.C * pow(in.sigma_si, 3) * Avagadro)), 1.0 / 3.0);
   int loopStart = 0;
-  string rname = o.R ? newest_restart("outfiles/") : "";
+  string rname = o.R ? newest_file("outfiles/", "restart") : "";
   bool restart = !rname.empty();
   if (restart) {
     cout << "Restarting from: " << rname << endl;
@@ -404,6 +405,73 @@ int run_simulation(const Options& o) {
     for (auto& v : vel) v *= sf;
   }
 
+  // encapsulation big beads (generate_big_beads, src/initialize.cpp:566-680, called with
+  // sigma = 2 a, mass 100, type 3, charge G and 1000000 attempts at src/md.cpp:185)
+  const double big_sigma = 2 * o.a, big_mass = 100.0;
+  vector<double> big_pos, big_vel;
+  if (o.p) {
+    const int nb = o.m;
+    if (restart) {
+      const string rb = newest_file("outfiles/", "rb");
+      ifstream rf(("outfiles/" + rb).c_str());
+      for (int i = 0; i < nb; i++) {
+        double v[6];
+        for (double& x : v) rf >> x;
+        if (!rf || rb.empty()) {
+          cerr << "ERR: big-bead restart file outfiles/" << rb << " has fewer than " << nb << " beads" << endl;
+          return 1;
+        }
+        cout << v[0] << ", " << v[1] << ", " << v[2] << endl;
+        big_vel.insert(big_vel.end(), v, v + 3);
+        big_pos.insert(big_pos.end(), v + 3, v + 6);
+      }
+    } else {
+      srand(0);
+      const double R_squared = big_sigma * big_sigma;
+      for (int i = 0; i < nb; i++) {
+        bool placed = false;
+        unsigned attempts = 0;
+        while (!placed && attempts < 1000000u) {
+          const double x = (static_cast<double>(rand()) / RAND_MAX - 0.5) * box_x;
+          const double y = (static_cast<double>(rand()) / RAND_MAX - 0.5) * box_x;
+          const double z = (static_cast<double>(rand()) / RAND_MAX - 0.5) * box_x;
+          auto d2 = [&](double px, double py, double pz) {
+            double dx = x - px, dy = y - py, dz = z - pz;
+            dx -= box_x * floor(dx / box_x + 0.5);
+            dy -= box_x * floor(dy / box_x + 0.5);
+            dz -= box_x * floor(dz / box_x + 0.5);
+            return dx * dx + dy * dy + dz * dz;
+          };
+          bool collision = false;
+          for (long g = 0; g < N && !collision; g++) {
+            const double min_dist = in.sigma[g % np] / 2 + big_sigma / 2;
+            if (d2(pos[3 * g], pos[3 * g + 1], pos[3 * g + 2]) < min_dist * min_dist) collision = true;
+          }
+          for (size_t b = 0; b < big_pos.size() / 3 && !collision; b++)
+            if (d2(big_pos[3 * b], big_pos[3 * b + 1], big_pos[3 * b + 2]) < R_squared) collision = true;
+          if (!collision) {
+            big_pos.insert(big_pos.end(), {x, y, z});
+            big_vel.insert(big_vel.end(), {0.0, 0.0, 0.0});
+            placed = true;
+          }
+          attempts++;
+        }
+        if (attempts >= 1000000u) {
+          cerr << "Error: Failed to place big bead " << i + 1 << " after " << 1000000 << " attempts" << endl;
+          exit(1);
+        }
+      }
+    }
+  }
+  const int n_big = (int)(big_pos.size() / 3);
+  // BEAD::update_kinetic_energy (src/bead.h:129-131) of the static big beads
+  double big_ke = 0;
+  for (int i = 0; i < n_big; i++) {
+    const double v = sqrt(big_vel[3 * i] * big_vel[3 * i] + big_vel[3 * i + 1] * big_vel[3 * i + 1] +
+                          big_vel[3 * i + 2] * big_vel[3 * i + 2]);
+    big_ke += 0.5 * big_mass * v * v;
+  }
+
   souffle_template t{np, in.ne, in.nf, in.na, in.type.data(), in.q.data(), in.sigma.data(), in.mass.data(),
                      in.eb.data(), in.et.data(), in.len0.data(), in.fb.data(), in.lj.empty() ? nullptr : in.lj.data()};
   souffle_params p{};
@@ -430,6 +498,8 @@ int run_simulation(const Options& o) {
   check(souffle_gpu_create(&t, &p, 1, nullptr, &h), "souffle_gpu_create");
   // the reference wraps lattice positions only when they move; the fixed-point state wraps now
   check(souffle_gpu_set_state(h, pos.data(), vel.data()), "souffle_gpu_set_state");
+  if (n_big > 0)
+    check(souffle_gpu_set_big_beads(h, 0, n_big, big_pos.data(), big_sigma, o.G, o.H), "souffle_gpu_set_big_beads");
   check(souffle_gpu_md_begin(h), "souffle_gpu_md_begin");
 
   vector<double> be(N);
@@ -443,6 +513,11 @@ int run_simulation(const Options& o) {
          << setw(15) << e.thermo_pe / N << setw(15) << e.thermo_ke / N;
     if (with_vcom) traj << setw(15) << e.vcom_magnitude;
     traj << endl;
+    if (n_big > 0)  // src/md.cpp:347-351,625-629
+      encapdata << a << setw(15) << big_ke / n_big << setw(15) << e.bigbead_lj / n_big << setw(15)
+                << e.bigbead_electrostatic / n_big << setw(15)
+                << (big_ke + e.bigbead_lj + e.bigbead_electrostatic) / n_big << setw(15)
+                << big_ke * 2 / (3 * n_big) << endl;
   };
   energy_row(0, false);  // row 0 before the loop (src/md.cpp:339-346)
 
@@ -466,16 +541,28 @@ int run_simulation(const Options& o) {
            << setprecision(12) << pos[3 * i + 1] << setw(25) << setprecision(12) << pos[3 * i + 2] << setw(25)
            << setprecision(12) << endl;
       rs.close();
+      if (o.p) {
+        rs.open(("outfiles/rb_" + to_string(a) + ".out").c_str(), ios::out);
+        for (int i = 0; i < n_big; i++)
+          rs << big_vel[3 * i] << setw(25) << setprecision(12) << big_vel[3 * i + 1] << setw(25) << setprecision(12)
+             << big_vel[3 * i + 2] << setw(25) << setprecision(12) << big_pos[3 * i] << setw(25) << setprecision(12)
+             << big_pos[3 * i + 1] << setw(25) << setprecision(12) << big_pos[3 * i + 2] << setw(25)
+             << setprecision(12) << endl;
+        rs.close();
+      }
     }
     if (a % o.W == 0) energy_row(a, true);
     if (a % o.M == 0) {
-      ofile << "ITEM: TIMESTEP" << endl << a << endl << "ITEM: NUMBER OF ATOMS" << endl << N << endl
+      ofile << "ITEM: TIMESTEP" << endl << a << endl << "ITEM: NUMBER OF ATOMS" << endl << N + n_big << endl
             << "ITEM: BOX BOUNDS" << endl << -box_x / 2 << setw(15) << box_x / 2 << endl << -box_x / 2
             << setw(15) << box_x / 2 << endl << -box_x / 2 << setw(15) << box_x / 2 << endl
             << "ITEM: ATOMS index type x y z b charge" << endl;
       for (long g = 0; g < N; g++)
         ofile << g + 1 << setw(15) << in.type[g % np] << setw(15) << pos[3 * g] << setw(15) << pos[3 * g + 1]
               << setw(15) << pos[3 * g + 2] << setw(15) << be[g] << setw(15) << in.q[g % np] << endl;
+      for (int bb = 0; bb < n_big; bb++)  // type 3, no bending energy (src/md.cpp:670-675)
+        ofile << N + bb + 1 << setw(15) << 3 << setw(15) << big_pos[3 * bb] << setw(15) << big_pos[3 * bb + 1]
+              << setw(15) << big_pos[3 * bb + 2] << setw(15) << 0 << setw(15) << o.G << endl;
     }
     double pct = roundf(a / (totaltime / o.t) * 100 * 10) / 10;
     if (pct != pre) {

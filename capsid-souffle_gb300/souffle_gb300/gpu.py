@@ -23,6 +23,7 @@ STATUS = {0: "OK", 1: "BAD_INPUT", 2: "CUDA", 3: "NL_OVERFLOW", 4: "NONFINITE", 
 
 EXPORTED = [
     "souffle_gpu_create", "souffle_gpu_destroy", "souffle_gpu_num_beads", "souffle_gpu_set_state",
+    "souffle_gpu_set_big_beads",
     "souffle_gpu_get_state", "souffle_gpu_forces", "souffle_gpu_get_pairlist",
     "souffle_gpu_pairlist_stats", "souffle_gpu_energies", "souffle_gpu_kinetic_energy",
     "souffle_gpu_md_begin", "souffle_gpu_md_steps", "souffle_gpu_md_enqueue", "souffle_gpu_md_scalars",
@@ -89,7 +90,7 @@ class Tuning_(C.Structure):
 class Energies_(C.Structure):
     _fields_ = [(n, C.c_double) for n in ["kinetic", "stretching", "bending", "lj", "electrostatic",
                                            "thermo_pe", "thermo_ke", "temperature",
-                                           "vcom_magnitude"]]
+                                           "vcom_magnitude", "bigbead_lj", "bigbead_electrostatic"]]
 
 
 class PairStats_(C.Structure):
@@ -119,6 +120,7 @@ def load() -> C.CDLL:
     lib.souffle_gpu_num_beads.restype = C.c_int64
     lib.souffle_gpu_num_beads.argtypes = [vp]
     lib.souffle_gpu_set_state.argtypes = [vp, dp, dp]
+    lib.souffle_gpu_set_big_beads.argtypes = [vp, C.c_int32, C.c_int32, dp, C.c_double, C.c_double, C.c_double]
     lib.souffle_gpu_get_state.argtypes = [vp, dp, dp]
     lib.souffle_gpu_forces.argtypes = [vp, C.c_int32, dp, dp, dp]
     lib.souffle_gpu_get_pairlist.argtypes = [vp, C.c_int32, ip, ip]
@@ -234,6 +236,14 @@ class GpuSystem:
         assert pos.size == 3 * self.n
         v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
         _check(self.lib.souffle_gpu_set_state(self.h, _dp(pos), None if v is None else _dp(v)))
+
+    def set_big_beads(self, pos, sigma: float, charge: float, shc: float, system: int = 0):
+        """Encapsulation big beads of one system (include/souffle_gpu.h souffle_gpu_set_big_beads):
+        pos [n][3] in box coordinates; an empty array removes them."""
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        assert p.size % 3 == 0
+        _check(self.lib.souffle_gpu_set_big_beads(self.h, int(system), p.size // 3, _dp(p) if p.size else None,
+                                                  float(sigma), float(charge), float(shc)))
 
     def get_state(self):
         pos = np.empty((self.n, 3))

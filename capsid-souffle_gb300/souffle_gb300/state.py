@@ -137,8 +137,11 @@ def _exact(x: float) -> str:
     return s
 
 
-def write_restart(state: State, outdir: str, step: int = 0, big_beads: int = 1) -> None:
-    """Write ``restart_<step>.out`` and ``rb_<step>.out`` under ``outdir``."""
+def write_restart(state: State, outdir: str, step: int = 0, big_beads: int = 1,
+                  big_bead_pos: Optional[np.ndarray] = None) -> None:
+    """Write ``restart_<step>.out`` and ``rb_<step>.out`` under ``outdir``.  ``rb`` holds one
+    line per big bead (velocity, position: src/md.cpp:537-545); ``big_bead_pos`` [n][3] gives
+    their positions (at rest), else ``big_beads`` zero lines."""
     os.makedirs(outdir, exist_ok=True)
     lines = [f"Velocities & Positions for {step}"]
     for i in range(state.pos.shape[0]):
@@ -149,8 +152,12 @@ def write_restart(state: State, outdir: str, step: int = 0, big_beads: int = 1) 
     with open(os.path.join(outdir, f"restart_{step}.out"), "w") as fh:
         fh.write("\n".join(lines) + "\n")
     with open(os.path.join(outdir, f"rb_{step}.out"), "w") as fh:
-        for _ in range(big_beads):
-            fh.write("0 0 0 0 0 0\n")
+        if big_bead_pos is not None:
+            for p in np.asarray(big_bead_pos, dtype=np.float64).reshape(-1, 3):
+                fh.write(f"0 0 0 {_exact(p[0])} {_exact(p[1])} {_exact(p[2])}\n")
+        else:
+            for _ in range(big_beads):
+                fh.write("0 0 0 0 0 0\n")
 
 
 def read_restart(path: str, n_beads: Optional[int] = None):

@@ -106,6 +106,9 @@ typedef struct souffle_energies {
   double thermo_pe, thermo_ke;  /* Nose-Hoover chain energies (src/thermostat.h:43-52) */
   double temperature;           /* 2 KE / (3 N) (src/md.cpp:622) */
   double vcom_magnitude;        /* |mean velocity| removed at the last step (src/md.cpp:623) */
+  /* encapsulation: the big-bead pair parts of lj and electrostatic (already included in them),
+     i.e. the sums over all big beads of src/md.cpp:606-614 (capenergy.out) */
+  double bigbead_lj, bigbead_electrostatic;
 } souffle_energies;
 
 typedef struct souffle_pairlist_stats {
@@ -129,6 +132,19 @@ int64_t souffle_gpu_num_beads(const souffle_gpu_system* h);
 
 /* Copy a state in (host, double) / out.  vel may be NULL on set (zero). */
 souffle_status souffle_gpu_set_state(souffle_gpu_system* h, const double* pos, const double* vel);
+
+/* Encapsulation big beads (-p; replaces forceCalculation_bigbead src/forces.cpp:174-236 and
+ * update_LJ_ES_energies_bigbeads src/energies.cpp:96-137, as called at src/md.cpp:242,299,444,
+ * 584): n static beads of diameter sigma and charge q (e) in one system, at pos [n][3] (box
+ * coordinates, as generate_big_beads src/initialize.cpp:566-680 places or restarts them).
+ * Every subunit bead feels each big bead through the screened Coulomb term (no shift; none at
+ * all without a DH cut-off) and a WCA term shifted by delta = (sigma + sigma_j)/2 - shc with
+ * hard-core distance shc; the reference never moves them.  Forces (souffle_gpu_forces, MD and
+ * Brownian steps), energies and the Brownian noise sequence (three uniforms per big bead after
+ * the subunit beads' draws, src/md.cpp:482-487) include them from the next call on; n = 0
+ * removes them. */
+souffle_status souffle_gpu_set_big_beads(souffle_gpu_system* h, int32_t system, int32_t n, const double* pos,
+                                         double sigma, double charge, double shc);
 souffle_status souffle_gpu_get_state(souffle_gpu_system* h, double* pos, double* vel);
 
 /* forceCalculation: rebuild != 0 first rebuilds the pair lists (update_pairlist).

@@ -14,6 +14,13 @@
 //   N <i> <n> <ids...>                    per-bead pair list (up to the -1)
 //   E <i> se ke be ne ce                  per-bead energies
 //   K <ke>                                particle_kinetic_energy
+// With -p 1 (encapsulation) it also places the big beads with the reference's own
+// generate_big_beads (src/initialize.cpp:566-680; restart: the newest outfiles/rb_*.out),
+// adds forceCalculation_bigbead (src/forces.cpp:174-236) after forceCalculation and
+// update_LJ_ES_energies_bigbeads (src/energies.cpp:96-137) after the pair energies, as
+// src/md.cpp:242,299 do, and prints
+//   BB <i> x y z                          big-bead positions as held
+//   G <ne> <ce>                           big-bead energy sums (src/md.cpp:606-614)
 // Option letters match the reference driver (src/md.cpp:53-90).
 #include <cfloat>
 #include <cmath>
@@ -42,6 +49,9 @@ int main(int argc, char* argv[]) {
   std::string file_name = "41part_c";
   double capsomere_concentration = 200, salt_concentration = 500, number_capsomeres = 64;
   double ks = 50, kb = 20, ecut_c = 12, elj_att = 2, NListCutoff_c = 7.5;
+  bool encapsulation = false;
+  double radius_a = 3.0, charge_a = -78.0, shc = 3.5;
+  int number_bigbeads = 1;
   for (int a = 1; a + 1 < argc; a += 2) {
     const char* k = argv[a];
     const char* v = argv[a + 1];
@@ -54,6 +64,11 @@ int main(int argc, char* argv[]) {
     else if (!std::strcmp(k, "-e")) ecut_c = atof(v);
     else if (!std::strcmp(k, "-E")) elj_att = atof(v);
     else if (!std::strcmp(k, "-L")) NListCutoff_c = atof(v);
+    else if (!std::strcmp(k, "-p")) encapsulation = atoi(v) != 0;
+    else if (!std::strcmp(k, "-a")) radius_a = atof(v);
+    else if (!std::strcmp(k, "-G")) charge_a = atof(v);
+    else if (!std::strcmp(k, "-m")) number_bigbeads = atoi(v);
+    else if (!std::strcmp(k, "-H")) shc = atof(v);
     else {
       fprintf(stderr, "unknown option %s\n", k);
       return 2;
@@ -103,6 +118,13 @@ int main(int argc, char* argv[]) {
 
   forceCalculation(protein, lb, ni, qs, subunit_bead, ecut, ks, kb, lj_a, ecut_el, kappa, elj_att,
                    true, NListCutoff);
+  std::vector<BEAD> big_beads;
+  if (encapsulation) {
+    VECTOR3D box_size = VECTOR3D(box_x, box_x, box_x);
+    big_beads = generate_big_beads(number_bigbeads, 2 * radius_a, subunit_bead, box_size, 100.0, 3, charge_a,
+                                   1000000, restartFile);
+    forceCalculation_bigbead(big_beads, subunit_bead, ecut, lb, ni, qs, ecut_el, kappa, shc);
+  }
 
   printf("P restart_step %d\n", restartStep);
   printf("P n_beads %zu\n", subunit_bead.size());
@@ -151,6 +173,22 @@ int main(int argc, char* argv[]) {
       if (protein[i].itsE[kk]->type != 0) protein[i].itsE[kk]->update_bending_energy(kb);
   }
   update_LJ_ES_energies_simplified(subunit_bead, ecut, lj_a, elj_att, lb, ni, qs, ecut_el, kappa);
+  if (encapsulation) {
+    for (size_t i = 0; i < big_beads.size(); i++) {
+      big_beads[i].be = 0;
+      big_beads[i].ne = 0;
+      big_beads[i].ce = 0;
+    }
+    update_LJ_ES_energies_bigbeads(big_beads, subunit_bead, ecut, lb, ni, qs, ecut_el, kappa, shc);
+    double big_ne = 0, big_ce = 0;
+    for (size_t i = 0; i < big_beads.size(); i++) {
+      big_ne += big_beads[i].ne;
+      big_ce += big_beads[i].ce;
+      printf("BB %zu %La %La %La\n", i, (long double)big_beads[i].pos.x, (long double)big_beads[i].pos.y,
+             (long double)big_beads[i].pos.z);
+    }
+    printf("G %La %La\n", (long double)big_ne, (long double)big_ce);
+  }
   for (size_t i = 0; i < subunit_bead.size(); i++) {
     const BEAD& b = subunit_bead[i];
     printf("E %zu %La %La %La %La %La\n", i, (long double)b.se, (long double)b.ke,

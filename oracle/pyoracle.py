@@ -69,6 +69,8 @@ def load(variant: str = "ld") -> C.CDLL:
     lib.oracle_energies.argtypes = [vp, dp, dp, dp, dp, dp]
     lib.oracle_kinetic_energy.restype = C.c_double
     lib.oracle_kinetic_energy.argtypes = [vp]
+    lib.oracle_set_big_beads.argtypes = [vp, C.c_int, dp, C.c_double, C.c_double, C.c_double]
+    lib.oracle_big_bead_energies.argtypes = [vp, dp, dp]
     lib.oracle_nhc_init.argtypes = [C.POINTER(_Nhc), C.c_int, C.c_double, C.c_double, C.c_int]
     lib.oracle_md_step.restype = C.c_int
     lib.oracle_md_step.argtypes = [vp, C.POINTER(_Nhc), C.c_uint, C.c_double, C.c_int, dp, dp]
@@ -158,6 +160,18 @@ class Oracle:
         out = [np.empty(self.n) for _ in range(5)]
         self.lib.oracle_energies(self.h, *[_p(o, C.c_double) for o in out])
         return dict(zip(["se", "ke", "be", "ne", "ce"], out))
+
+    def set_big_beads(self, pos, sigma: float, charge: float, shc: float) -> None:
+        """Encapsulation big beads (src/forces.cpp:174-236, src/energies.cpp:96-137)."""
+        self._bb = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        self.lib.oracle_set_big_beads(self.h, self._bb.size // 3, _p(self._bb, C.c_double) if self._bb.size else None,
+                                      sigma, charge, shc)
+
+    def big_bead_energies(self):
+        """(lj, electrostatic) sums over big beads of the last energies() call."""
+        ne, ce = C.c_double(), C.c_double()
+        self.lib.oracle_big_bead_energies(self.h, C.byref(ne), C.byref(ce))
+        return ne.value, ce.value
 
     def kinetic_energy(self) -> float:
         return self.lib.oracle_kinetic_energy(self.h)

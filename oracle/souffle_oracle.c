@@ -24,6 +24,7 @@ typedef ORACLE_REAL real;
 
 #define SQRT(x) _Generic((x), long double: sqrtl, default: sqrt)(x)
 #define EXP(x) _Generic((x), long double: expl, default: exp)(x)
+#define POW(x, y) _Generic((x), long double: powl, default: pow)(x, y)
 
 typedef struct { real x, y, z; } vec3;
 
@@ -80,6 +81,12 @@ struct oracle_sys {
   int *nl_count;
   int overflow;
   real bx, hbx;
+  /* encapsulation big beads (static): positions, diameter, charge, hard-core distance, and the
+     big-bead sums of the last energy block (src/md.cpp:606-614) */
+  int nbb;
+  vec3* bb_pos;
+  double bb_sigma, bb_q, bb_shc;
+  double bb_ne_tot, bb_ce_tot;
 };
 
 static int threads_req = 0;
@@ -205,7 +212,7 @@ void oracle_destroy(oracle_sys* s) {
                   s->b_sigma, s->b_mass, s->e_len0, s->e_f,    s->bead_edges, s->bead_nedge,
                   s->pos,    s->vel,     s->tforce, s->sforce, s->bforce,   s->ke,
                   s->se,     s->be,      s->ne,     s->ce,     s->e_length, s->e_lvec,
-                  s->f_nrm,  s->f_area,  s->f_a,    s->nl,     s->nl_count};
+                  s->f_nrm,  s->f_area,  s->f_a,    s->nl,     s->nl_count, s->bb_pos};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
   free(s);
 }
@@ -475,6 +482,59 @@ static void pairs_subunit(oracle_sys* s, int i) {
   }
 }
 
+void oracle_set_big_beads(oracle_sys* s, int n, const double* pos, double sigma, double charge, double shc) {
+  free(s->bb_pos);
+  s->bb_pos = NULL;
+  s->nbb = n > 0 ? n : 0;
+  if (s->nbb) s->bb_pos = (vec3*)malloc(sizeof(vec3) * (size_t)n);
+  /* restart positions are read into the long double vector (src/initialize.cpp:584-587) */
+  for (int i = 0; i < s->nbb; i++) s->bb_pos[i] = v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+  s->bb_sigma = sigma;
+  s->bb_q = charge;
+  s->bb_shc = shc;
+  s->bb_ne_tot = s->bb_ce_tot = 0;
+}
+
+/* forceCalculation_bigbead (src/forces.cpp:174-236): every big bead with every subunit bead;
+ * the subunit bead's eforce / ljforce start at zero, take minus each pair force in big-bead
+ * order, and join tforce as tforce + ljforce + eforce.  r is GetMagnitude (a double root),
+ * r2 the long double square; pow(r - delta, 6) is a long double power rounded to double. */
+static void bigbead_forces(oracle_sys* s) {
+  const int n = s->n, np = s->d.np;
+  const real bx = s->bx, hbx = s->hbx;
+  const double ecut_el = s->d.ecut_el, kappa = s->d.kappa, lb = s->d.lb, shc = s->bb_shc;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < n; j++) {
+    vec3 ef = v3(0, 0, 0), lf = v3(0, 0, 0);
+    const double qj = s->b_q[j % np];
+    const int electrostatic = (qj != 0);
+    for (int i = 0; i < s->nbb; i++) {
+      vec3 eForce = v3(0, 0, 0), ljForce = v3(0, 0, 0);
+      const vec3 r_vec = pbc(vsub(s->bb_pos[i], s->pos[j]), bx, hbx);
+      const real r = vnorm(r_vec);
+      const real r2 = vnorm2(r_vec);
+      const double sig1 = s->bb_sigma, sig2 = s->b_sigma[j % np];
+      const double sigavg = (sig1 + sig2) / 2;
+      const double delta = sigavg - shc;
+      const double shc6 = pow(shc, 6);
+      const double r6 = (double)POW(r - delta, (real)6);
+      const double yukawa_scale = exp(kappa * sigavg) / ((1 + kappa * sig1 / 2) * (1 + kappa * sig2 / 2));
+      if (electrostatic && r2 < (ecut_el * ecut_el))
+        eForce = vscale(r_vec, ((s->bb_q * qj * lb * EXP(-kappa * r) / (r2)) * (kappa + 1 / r) * yukawa_scale));
+      if (r2 < (delta + 1.12246205 * shc) * (delta + 1.12246205 * shc))
+        ljForce = vscale(r_vec, (48 * ((shc6 / r6) * ((shc6 / r6) - 0.5))) * (1 / r) * (1 / (r - delta)));
+      ef = vsub(ef, eForce);
+      lf = vsub(lf, ljForce);
+    }
+    s->tforce[j] = vadd(vadd(s->tforce[j], lf), ef);
+  }
+}
+
+void oracle_big_bead_energies(const oracle_sys* s, double* big_ne, double* big_ce) {
+  if (big_ne) *big_ne = s->bb_ne_tot;
+  if (big_ce) *big_ce = s->bb_ce_tot;
+}
+
 int oracle_forces(oracle_sys* s, int rebuild) {
   const int S = s->d.n_sub;
   int over = 0;
@@ -489,6 +549,7 @@ int oracle_forces(oracle_sys* s, int rebuild) {
     pairs_subunit(s, i);
   }
   s->overflow = over;
+  if (s->nbb > 0) bigbead_forces(s);
   return over;
 }
 
@@ -640,6 +701,35 @@ void oracle_energies(oracle_sys* s, double* se, double* ke, double* be, double* 
           s->ne[i] += 0;
         }
       }
+    }
+  }
+  if (s->nbb > 0) {
+    /* update_LJ_ES_energies_bigbeads (src/energies.cpp:96-137): credited to both beads; the
+       big-bead sums in big-bead order, then over big beads (src/md.cpp:606-614) */
+    const double shc = s->bb_shc;
+    s->bb_ne_tot = s->bb_ce_tot = 0;
+    for (int i = 0; i < s->nbb; i++) {
+      double bce = 0, bne = 0;
+      for (int j = 0; j < n; j++) {
+        const double qj = s->b_q[j % np];
+        const int electrostatic = (qj != 0);
+        double cej = 0.0, nej = 0.0;
+        const real r = vnorm(pbc(vsub(s->bb_pos[i], s->pos[j]), bx, hbx));
+        const double sig1 = s->bb_sigma, sig2 = s->b_sigma[j % np];
+        const double sigavg = (sig1 + sig2) / 2;
+        const double delta = sigavg - shc;
+        const double shc6 = pow(shc, 6);
+        const double r6 = (double)POW(r - delta, (real)6);
+        const double yukawa_scale = exp(kappa * sigavg) / ((1 + kappa * sig1 / 2) * (1 + kappa * sig2 / 2));
+        if (electrostatic && r < ecut_el) cej = (double)((s->bb_q * qj * lb * EXP(-kappa * r) * yukawa_scale) / (r));
+        bce += cej;
+        s->ce[j] += cej;
+        if (r < delta + 1.12246205 * shc) nej = ((4 * (shc6 / r6) * ((shc6 / r6) - 1)) + 1);
+        bne += nej;
+        s->ne[j] += nej;
+      }
+      s->bb_ce_tot += bce;
+      s->bb_ne_tot += bne;
     }
   }
   for (int g = 0; g < n; g++) {

@@ -69,6 +69,13 @@ void oracle_get_pairlist(const oracle_sys* s, int* counts, int* ids);
 void oracle_energies(oracle_sys* s, double* se, double* ke, double* be, double* ne, double* ce);
 double oracle_kinetic_energy(oracle_sys* s);
 
+/* Encapsulation big beads (src/forces.cpp:174-236, src/energies.cpp:96-137): n static beads at
+ * pos [n][3] of diameter sigma, charge q and hard-core distance shc.  oracle_forces adds their
+ * forces to tforce and oracle_energies their energies to ne and ce; n = 0 removes them.
+ * oracle_big_bead_energies: the big-bead sums of the last oracle_energies (src/md.cpp:606-614). */
+void oracle_set_big_beads(oracle_sys* s, int n, const double* pos, double sigma, double charge, double shc);
+void oracle_big_bead_energies(const oracle_sys* s, double* big_ne, double* big_ce);
+
 /* Nose-Hoover chain (src/md.cpp:187-196). */
 typedef struct oracle_nhc {
   int m;             /* chain length */

@@ -6,7 +6,7 @@ energy block; ref_run: run_simulation), on seeded synthetic states, and stores
 inputs and outputs as .npz.  Needs the reference tree (default /root/reference,
 or REF=...) only when regenerating; the tests read the committed fixtures.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--bigbead-only]
 """
 from __future__ import annotations
 
@@ -110,5 +110,72 @@ def main():
             print(name, n, "beads; mean list", counts.mean(), "max", counts.max(), "cap", cap)
 
 
+# Encapsulation (-p): the plain_small state with three big beads (-a 3: diameter 6, -G -78,
+# -H 3.5) set 4 sigma from the centroids of subunits 0, 5 and 10, so that subunit beads sit
+# inside the shifted WCA range and the DH cut-off of a big bead.
+BIG = dict(S=20, C=800.0, seed=12345, gap=1.0, subs=(0, 5, 10), dist=4.0, a=3.0, G=-78.0, H=3.5)
+
+
+def bigbead_args():
+    return ["-p", "1", "-m", str(len(BIG["subs"])), "-a", repr(BIG["a"]), "-G", repr(BIG["G"]), "-H", repr(BIG["H"])]
+
+
+def run_args_p():
+    return ["-p", "true", "-m", str(len(BIG["subs"])), "-a", repr(BIG["a"]), "-G", repr(BIG["G"]), "-H", repr(BIG["H"])]
+
+
+def make_bigbead():
+    t = geometry.template_by_name("patch_n3")
+    S, C = BIG["S"], BIG["C"]
+    L = state.box_length(S, C)
+    st = state.random_state(t, S, L, seed=BIG["seed"], min_gap=BIG["gap"])
+    rng = np.random.default_rng(99)
+    big = []
+    for k in BIG["subs"]:
+        c = st.pos[k * t.n_beads:(k + 1) * t.n_beads].mean(axis=0)
+        d = rng.normal(size=3)
+        p = c + BIG["dist"] * d / np.linalg.norm(d)
+        big.append((p + L / 2) % L - L / 2)
+    big = np.array(big)
+    with tempfile.TemporaryDirectory() as wd:
+        os.makedirs(f"{wd}/infiles")
+        os.makedirs(f"{wd}/outfiles")
+        geometry.write_infile(t, f"{wd}/infiles/patch_n3")
+        state.write_restart(st, f"{wd}/outfiles", big_bead_pos=big)
+        _, vel, pos = state.read_restart(f"{wd}/outfiles/restart_0.out")
+        d = refdump.run_dump(wd, cli("patch_n3", S, C) + bigbead_args())
+        o = workloads.base_options()
+        runs = {}
+        for mode, extra in (("md", ["-D", "m", "-q", str(int(o.q)), "-Q", repr(o.Q)]),
+                            ("bd", ["-D", "b", "-d", repr(BD_DAMP)])):
+            rd = f"{wd}/{mode}"
+            os.makedirs(f"{rd}/outfiles")
+            shutil.copytree(f"{wd}/infiles", f"{rd}/infiles")
+            for f in ("restart_0.out", "rb_0.out"):
+                shutil.copy(f"{wd}/outfiles/{f}", f"{rd}/outfiles/{f}")
+            args = cli("patch_n3", S, C) + extra + ["-B", str(o.B), "-t", repr(o.t), "-K", repr(o.K),
+                                                  "-T", str(MD_STEPS), "-W", "1", "-M", "1000000",
+                                                  "-w", str(MD_STEPS)] + run_args_p()
+            subprocess.run([refdump.REF_RUN] + args, cwd=rd, check=True, capture_output=True)
+            _, v, p = state.read_restart(f"{rd}/outfiles/restart_{MD_STEPS}.out")
+            runs[mode] = dict(pos=p, vel=v, args=np.array(args),
+                              energy_rows=np.loadtxt(f"{rd}/outfiles/energy.out", skiprows=1, usecols=range(11)),
+                              cap_text=np.array(open(f"{rd}/outfiles/capenergy.out").read()),
+                              energy_text=np.array(open(f"{rd}/outfiles/energy.out").read()))
+        np.savez_compressed(
+            os.path.join(HERE, "bigbead.npz"),
+            template=np.array("patch_n3"), n_sub=S, conc=C, seed=BIG["seed"], gap=BIG["gap"],
+            pos=pos, vel=vel, big_pos_in=big, big_pos=d["big_pos"], big_sigma=2 * BIG["a"],
+            big_charge=BIG["G"], big_shc=BIG["H"], box=d["params"]["box"],
+            center=int(d["params"]["center_bead"]), kappa=d["params"]["kappa"],
+            ld_mant_dig=int(d["params"]["long_double_mant_dig"]),
+            tforce=d["tforce"], ne=d["ne"], ce=d["ce"], big_ne=d["big_energies"][0],
+            big_ce=d["big_energies"][1], md_steps=MD_STEPS,
+            **{f"{m}_{k}": v for m, r in runs.items() for k, v in r.items()})
+        print("bigbead", S * t.n_beads, "beads,", len(big), "big beads; big-bead energies", d["big_energies"])
+
+
 if __name__ == "__main__":
-    main()
+    if "--bigbead-only" not in sys.argv:
+        main()
+    make_bigbead()

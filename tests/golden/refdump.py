@@ -27,8 +27,9 @@ def available() -> bool:
 def run_dump(workdir: str, args: list[str]) -> dict:
     out = subprocess.run([REF_DUMP] + args, cwd=workdir, check=True, capture_output=True,
                          text=True).stdout
-    P, F, N, E = {}, {}, {}, {}
+    P, F, N, E, BB = {}, {}, {}, {}, {}
     ke = None
+    big = None
     for line in out.splitlines():
         t = line.split()
         if not t:
@@ -43,9 +44,14 @@ def run_dump(workdir: str, args: list[str]) -> dict:
             E[int(t[1])] = [_num(x) for x in t[2:7]]
         elif t[0] == "K":
             ke = _num(t[1])
+        elif t[0] == "BB":
+            BB[int(t[1])] = [_num(x) for x in t[2:5]]
+        elif t[0] == "G":
+            big = (_num(t[1]), _num(t[2]))
     n = len(F)
     f = np.array([F[i] for i in range(n)])
     e = np.array([E[i] for i in range(n)])
     return dict(params=P, tforce=f[:, 0:3], sforce=f[:, 3:6], bforce=f[:, 6:9],
                 nlist=[N[i] for i in range(n)], se=e[:, 0], ke=e[:, 1], be=e[:, 2],
-                ne=e[:, 3], ce=e[:, 4], ke_total=ke)
+                ne=e[:, 3], ce=e[:, 4], ke_total=ke,
+                big_pos=np.array([BB[i] for i in range(len(BB))]).reshape(-1, 3), big_energies=big)

@@ -23,7 +23,8 @@ def _run_driver(tmp_path, g, key="md_args"):
     os.makedirs(tmp_path / "infiles")
     os.makedirs(tmp_path / "outfiles")
     geometry.write_infile(t, str(tmp_path / "infiles" / t.name))
-    state.write_restart(state.State(g["pos"], g["vel"], float(g["box"])), str(tmp_path / "outfiles"))
+    state.write_restart(state.State(g["pos"], g["vel"], float(g["box"])), str(tmp_path / "outfiles"),
+                        big_bead_pos=g["big_pos_in"] if "big_pos_in" in g else None)
     args = [str(x) for x in g[key]]
     r = subprocess.run([DRIVER] + args, cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
@@ -108,3 +109,32 @@ def test_driver_rejects_missing_infile(tmp_path):
                        text=True, timeout=60)
     assert r.returncode == 1
     assert "NOT OPENED" in r.stderr
+
+
+@pytest.mark.parametrize("mode", ["md", "bd"])
+def test_driver_encapsulation_run_matches_reference_run(tmp_path, mode):
+    """-p true with three big beads read from outfiles/rb_0.out: energy.out and capenergy.out
+    rows and the final restart file against the reference's own run from the same state."""
+    g = load_golden("bigbead")
+    _run_driver(tmp_path, g, f"{mode}_args")
+    rows_r = np.asarray(g[f"{mode}_energy_rows"])
+    _, rows_g = _rows(open(tmp_path / "outfiles" / "energy.out").read())
+    rows_g = np.array([r[:11] for r in rows_g])
+    assert rows_g.shape == rows_r.shape
+    np.testing.assert_allclose(rows_g[:, 1:], rows_r[:, 1:], rtol=5e-5, atol=5e-6)
+    cap_r = np.array([[float(x) for x in ln.split()] for ln in str(g[f"{mode}_cap_text"]).strip().splitlines()])
+    cap_g = np.array([[float(x) for x in ln.split()]
+                      for ln in open(tmp_path / "outfiles" / "capenergy.out").read().strip().splitlines()])
+    assert cap_g.shape == cap_r.shape and cap_r.shape[1] == 6
+    assert np.array_equal(cap_g[:, 0], cap_r[:, 0])
+    np.testing.assert_allclose(cap_g[:, 1:], cap_r[:, 1:], rtol=5e-5, atol=5e-6)
+    from souffle_gb300 import state
+    T = int(g["md_steps"])
+    _, vel, pos = state.read_restart(str(tmp_path / "outfiles" / f"restart_{T}.out"))
+    L = float(g["box"])
+    dp = pos - g[f"{mode}_pos"]
+    dp -= L * np.round(dp / L)
+    assert np.abs(dp).max() < 1e-6
+    assert (tmp_path / "outfiles" / f"rb_{T}.out").exists()
+    rb = np.loadtxt(str(tmp_path / "outfiles" / f"rb_{T}.out"))
+    np.testing.assert_allclose(rb[:, 3:6], g["big_pos_in"], rtol=1e-11, atol=1e-11)

@@ -107,3 +107,32 @@ def test_oracle_rejects_bending_edge_without_faces():
     _, opt, d = golden_workload(g)
     with pytest.raises(ValueError):
         pyoracle.Oracle(t, 20, d, opt.s, opt.b, opt.E, 5)
+
+
+def test_oracle_big_beads_match_reference():
+    """Encapsulation: forceCalculation_bigbead and update_LJ_ES_energies_bigbeads
+    (src/forces.cpp:174-236, src/energies.cpp:96-137) restated, against the reference's own
+    forces and energies with three big beads among the subunits."""
+    g = load_golden("bigbead")
+    o, t, opt, d = _oracle(g)
+    assert np.array_equal(g["big_pos"], g["big_pos_in"])
+    o.set_big_beads(g["big_pos"], float(g["big_sigma"]), float(g["big_charge"]), float(g["big_shc"]))
+    tf, _, _, over = o.forces(True)
+    assert over == 0
+    e = o.energies()
+    big_ne, big_ce = o.big_bead_energies()
+    assert big_ne > 0 and big_ce != 0   # beads inside both ranges
+    if _same_platform(g):
+        assert np.array_equal(tf, g["tforce"])
+        assert np.array_equal(e["ne"], g["ne"]) and np.array_equal(e["ce"], g["ce"])
+        assert big_ne == float(g["big_ne"]) and big_ce == float(g["big_ce"])
+    else:
+        np.testing.assert_allclose(tf, g["tforce"], rtol=1e-9, atol=1e-9 * np.abs(g["tforce"]).max())
+        np.testing.assert_allclose(e["ne"], g["ne"], rtol=1e-9, atol=1e-12)
+        np.testing.assert_allclose(e["ce"], g["ce"], rtol=1e-9, atol=1e-12)
+        assert big_ne == pytest.approx(float(g["big_ne"]), rel=1e-9)
+        assert big_ce == pytest.approx(float(g["big_ce"]), rel=1e-9)
+    # without the big beads the forces differ
+    o.set_big_beads(np.zeros((0, 3)), 6.0, -78.0, 3.5)
+    tf0, _, _, _ = o.forces(True)
+    assert np.abs(tf0 - g["tforce"]).max() > 1.0

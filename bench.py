@@ -27,6 +27,7 @@ path on one system (--debye-length, --concentration set its parameters); --repli
 of N uneven systems in one handle (--replica-subunits S: N systems of S subunits at the plain
 workload's parameters; with --surrogate: the surrogate+batched measurement alone);
 --gemm: the surrogate network's forward pass at several row counts against the tensor peak;
+--big-beads M: the default workload with M encapsulation big beads (-p true -a 3 -G -78 -H 3.5);
 --profile: a few steps without autotuning or timing, for a profiler (plain, --replicas, or
 --replicas --surrogate after training);
 --analysis: the post-run trajectory analysis (include/souffle_analysis.h), frames/s on frames of
@@ -98,7 +99,10 @@ def _profile_traffic():
     return None
 
 
-def cpu_reference(w, seconds: float = 10.0, max_steps: int = 30, threads: int = 0):
+BIG_BEAD = dict(sigma=6.0, charge=-78.0, shc=3.5)  # the reference's defaults -a 3 -G -78 -H 3.5
+
+
+def cpu_reference(w, seconds: float = 10.0, max_steps: int = 30, threads: int = 0, big_beads=None):
     """Time the oracle port (long double, OpenMP) on the workload: bead-steps/s."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle
@@ -107,6 +111,8 @@ def cpu_reference(w, seconds: float = 10.0, max_steps: int = 30, threads: int = 
                         w.center_local)
     o.set_threads(threads)
     o.set_state(w.state.pos, w.state.vel)
+    if big_beads is not None and len(big_beads):
+        o.set_big_beads(big_beads, BIG_BEAD["sigma"], BIG_BEAD["charge"], BIG_BEAD["shc"])
     o.forces(True)
     ke = o.kinetic_energy()
     o.nhc_init(int(w.opt.q), w.opt.Q, w.opt.K)
@@ -702,6 +708,8 @@ def main():
     ap.add_argument("--debye-length", type=float, default=0.0,
                     help="screening length in sigma (default 1: -c 94.27)")
     ap.add_argument("--concentration", type=float, default=0.0, help="subunits in uM (default 800)")
+    ap.add_argument("--big-beads", type=int, default=0,
+                    help="encapsulation: this many big beads (-a 3 -G -78 -H 3.5) in the workload")
     ap.add_argument("--gemm", action="store_true",
                     help="the surrogate network's forward pass (tcgen05 GEMMs) at several row counts")
     ap.add_argument("--no-surrogate-batched", action="store_true",
@@ -727,9 +735,12 @@ def main():
     from souffle_gb300 import workloads
     w = workloads.plain_large(args.subunits, seed=12345 + rank, debye_length=args.debye_length,
                               conc_um=args.concentration)
+    big = workloads.place_big_beads(w, args.big_beads) if args.big_beads else None
     config = {"workload": f"plain_large: {args.subunits} bilayer capsomeres x 42 beads = "
                           f"{w.n_beads} beads, {w.opt.C:g} uM, -c {w.opt.c:.4g} (Debye length "
-                          f"{1 / w.derived.kappa:.3g} sigma) -e 5 -L 0.3 -B 10 -t 0.005 -q 5",
+                          f"{1 / w.derived.kappa:.3g} sigma) -e 5 -L 0.3 -B 10 -t 0.005 -q 5" + (
+                              f", encapsulation -p true -m {args.big_beads} -a 3 -G -78 -H 3.5"
+                              if args.big_beads else ""),
               "l2": "flushed (256 MB write) before every timed step" + (
                   "; working set < L2" if w.n_beads * 400 < 129e6 else "; working set > L2"),
               "parallelism": f"replicas x{world}"}
@@ -737,7 +748,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_reference(w, seconds=args.cpu_seconds)
+        cb = cpu_reference(w, seconds=args.cpu_seconds, big_beads=big)
         steps_ms = w.n_beads / cb["value"] * 1e3
         print(json.dumps({
             "impl": "reference", "metric": "bead-steps/s", "value": cb["value"],
@@ -764,6 +775,8 @@ def main():
     p = gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local)
     s = gpu.GpuSystem(w.template, [p])
     s.set_state(w.state.pos, w.state.vel)
+    if big is not None:
+        s.set_big_beads(big, BIG_BEAD["sigma"], BIG_BEAD["charge"], BIG_BEAD["shc"])
     tuning = s.autotune(trials=20) if not args.profile else None
     s.md_begin()
     if args.profile:
@@ -894,8 +907,8 @@ def main():
         "clocks": _summarize_clocks(samples),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_reference(w, seconds=args.cpu_seconds)
-    if rank == 0 and world == 1 and not args.no_surrogate_batched:
+        out["cpu_baseline"] = cpu_reference(w, seconds=args.cpu_seconds, big_beads=big)
+    if rank == 0 and world == 1 and not args.no_surrogate_batched and not args.big_beads:
         # the replica sweep with the learned surrogate against the plain single-system path
         s.close()
         try:

@@ -60,6 +60,71 @@ __device__ __forceinline__ long long limbs_value(const unsigned int* L) {
   return (long long)(hi + ((unsigned long long)L[1] << 21) + (unsigned long long)L[0]);
 }
 
+// Encapsulation big beads (forceCalculation_bigbead, src/forces.cpp:192-227) on one subunit bead
+// at high words pi (DH weight wl, diameter sl): for each big bead (those flagged in mask, or all),
+// r = big - subunit; screened Coulomb q_big q_j lb e^(-kappa r) / r^2 (kappa + 1/r) times the
+// Yukawa size factor, and WCA with hard-core distance shc shifted by delta = (sigma_big +
+// sigma_j)/2 - shc; the subunit bead takes minus their sum.  Out of line: it runs only for
+// systems with big beads and keeps the force kernel's registers for the common path.
+__device__ __noinline__ float3 bigbead_force(const ForceArgs& a, const SysParams& P, int4 pi, float wl, float sl,
+                                             float unit, const unsigned int* mask) {
+  const float kappa = P.kappa;
+  const float delta = 0.5f * (P.bb_sigma + sl) - P.bb_shc;
+  const float wc = delta + 1.12246205f * P.bb_shc;
+  const float s3 = P.bb_shc * P.bb_shc * P.bb_shc, shc6 = s3 * s3;
+  float3 fb = f3(0.f, 0.f, 0.f);
+  for (int k = 0; k < P.nbb; k++) {
+    if (mask) {  // next big bead within reach of the CTA
+      const unsigned int m = mask[k >> 5] >> (k & 31);
+      if (!m) {
+        k |= 31;
+        continue;
+      }
+      k += __ffs(m) - 1;
+    }
+    const float3 d = dvec(__ldg(&a.bb_pos32[P.bb0 + k]), pi, unit);
+    const float r2 = dot3(d, d);
+    const float r = sqrtf(r2);
+    float c = 0.f;
+    if (wl != 0.f && r2 < P.bb_dh_cut2) c = P.bb_w * wl * __expf(-kappa * r) / r2 * (kappa + 1.0f / r);
+    if (r2 < wc * wc) {
+      const float x = r - delta;
+      const float x3 = x * x * x, s6 = shc6 / (x3 * x3);
+      c += 48.0f * s6 * (s6 - 0.5f) / r / x;
+    }
+    fb = fb - d * c;
+  }
+  return fb;
+}
+
+constexpr int kBBWords = 8;   // per-subunit flags for up to 256 big beads (more: all visited)
+
+// Flags the big beads within reach of each of the CTA's nsub subunits (bit k of mask[s * kBBWords
+// ...]): a subunit's beads lie within R of its centre bead (R from the coordinates relative to
+// the centre bead, s_rel), and a big bead farther than R + the reach of every big-bead pair term
+// (bb_reach2, with a 1 % margin) acts on none of them.  A warp per subunit; all threads of the
+// CTA call it.
+__device__ __noinline__ void bigbead_mask(const ForceArgs& a, const SysParams& P, const int4* s_pos,
+                                          const float4* s_rel, int nsub, int np, float unit, unsigned int* mask) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const float reach = sqrtf(P.bb_reach2);
+  for (int s = wid; s < nsub; s += nw) {
+    float r2 = 0.f;
+    for (int l = lane; l < np; l += 32) {
+      const float4 q = s_rel[s * np + l];
+      r2 = fmaxf(r2, q.x * q.x + q.y * q.y + q.z * q.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+    const float lim = sqrtf(r2) * 1.01f + reach;
+    const int4 c = s_pos[s * np + P.center_local];
+    for (int k = lane; k < P.nbb; k += 32) {
+      const float3 d = dvec(__ldg(&a.bb_pos32[P.bb0 + k]), c, unit);
+      if (dot3(d, d) < lim * lim) atomicOr(&mask[s * kBBWords + (k >> 5)], 1u << (k & 31));
+    }
+  }
+}
+
 // 5 CTAs of 256 threads per SM (<= 51 registers) so 3-subunit work items fit one wave of
 // 152 x 5 CTAs at the 2000-subunit workload.
 __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
@@ -106,6 +171,10 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
                            __ldg(&a.dh_w[w.sys * np + l]));
   }
   for (int t = threadIdx.x; t < 9 * nbead; t += blockDim.x) s_F[t] = 0u;  // the beads' force limbs
+  // big beads within reach of each of the CTA's subunits (s_bbm), flagged before phase 3
+  __shared__ unsigned int s_bbm[16 * kBBWords];
+  const bool bb_filter = P.nbb > 0 && P.nbb <= 32 * kBBWords && w.nsub <= 16;
+  if (threadIdx.x < 16 * kBBWords) s_bbm[threadIdx.x] = 0u;
   // exclusive prefix sums of the beads' inter-subunit list lengths (s_pref[nbead] = total): each
   // thread a run of `per` beads, a warp scan, then the warp totals (s_red is free until the end)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -408,6 +477,7 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       limbs_add(s_F + 9 * b + 6, az);
     }
   }
+  if (bb_filter) bigbead_mask(a, P, s_pos, s_rel, w.nsub, np, unit, s_bbm);
   __syncthreads();
 
   // Phase 3: the bead's total force, the second half kick and the kinetic-energy and momentum
@@ -416,29 +486,8 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
     const int l = t % np, g = bead0 + t;
     long long Fx = limbs_value(s_F + 9 * t), Fy = limbs_value(s_F + 9 * t + 3), Fz = limbs_value(s_F + 9 * t + 6);
     if (P.nbb) {
-      // encapsulation big beads (forceCalculation_bigbead, src/forces.cpp:192-227): for each big
-      // bead, r = big - subunit; screened Coulomb (q_big q_j lb e^(-kappa r) / r^2 (kappa + 1/r)
-      // times the Yukawa size factor) and WCA with hard-core distance shc shifted by delta =
-      // (sigma_big + sigma_j)/2 - shc; the subunit bead takes minus their sum
-      const int4 pi = s_pos[t];
-      const float wl = s_w[l];
-      const float delta = 0.5f * (P.bb_sigma + tpl_f[L.o_sigma + l]) - P.bb_shc;
-      const float wc = delta + 1.12246205f * P.bb_shc;
-      const float s3 = P.bb_shc * P.bb_shc * P.bb_shc, shc6 = s3 * s3;
-      float3 fb = f3(0.f, 0.f, 0.f);
-      for (int k = 0; k < P.nbb; k++) {
-        const float3 d = dvec(__ldg(&a.bb_pos32[P.bb0 + k]), pi, unit);
-        const float r2 = dot3(d, d);
-        const float r = sqrtf(r2);
-        float c = 0.f;
-        if (wl != 0.f && r2 < P.bb_dh_cut2) c = P.bb_w * wl * __expf(-kappa * r) / r2 * (kappa + 1.0f / r);
-        if (r2 < wc * wc) {
-          const float x = r - delta;
-          const float x3 = x * x * x, s6 = shc6 / (x3 * x3);
-          c += 48.0f * s6 * (s6 - 0.5f) / r / x;
-        }
-        fb = fb - d * c;
-      }
+      const float3 fb = bigbead_force(a, P, s_pos[t], s_w[l], tpl_f[L.o_sigma + l], unit,
+                                      bb_filter ? s_bbm + (t / np) * kBBWords : nullptr);
       if (!(isfinite(fb.x) && isfinite(fb.y) && isfinite(fb.z)) ||
           fmaxf(fmaxf(fabsf(fb.x), fabsf(fb.y)), fabsf(fb.z)) > 1.0e9f)
         atomicOr(a.err, kErrNonFinite);

@@ -84,6 +84,7 @@ struct SysParams {
   // r^2 < ecut_el^2 then never holds); double copies for the energy pass
   int bb0, nbb;
   float bb_w, bb_sigma, bb_shc, bb_dh_cut2;
+  float bb_reach2;          // (1.01 max(DH cut-off, largest shifted WCA range))^2: beyond, no force
   double bb_q, bb_sigma_d, bb_shc_d;
 };
 

@@ -769,6 +769,11 @@ souffle_status souffle_gpu_set_big_beads(souffle_gpu_system* h, int32_t system, 
   P.bb_sigma = (float)sigma;
   P.bb_shc = (float)shc;
   P.bb_dh_cut2 = q.ecut_el > 0 ? (float)(q.ecut_el * q.ecut_el) : 0.0f;
+  {
+    const double smax = *std::max_element(h->tpl.sigma.begin(), h->tpl.sigma.end());
+    const double reach = std::max(q.ecut_el > 0 ? q.ecut_el : 0.0, 0.5 * (sigma + smax) - shc + 1.12246205 * shc);
+    P.bb_reach2 = (float)(1.01 * reach * 1.01 * reach);
+  }
   if (q.brownian) {
     // one step draws six numbers per subunit bead, then six per big bead (src/md.cpp:482-487)
     unsigned int m6 = 1, r = 1;

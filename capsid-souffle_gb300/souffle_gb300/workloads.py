@@ -105,6 +105,28 @@ def uniform_replicas(n: int, n_sub: int, seed: int = 4040) -> List[Workload]:
     return [make(t, n_sub, seed=seed * 1000 + k, name=f"replica{k}") for k in range(n)]
 
 
+def place_big_beads(w: Workload, n: int, radius: float = 3.0, seed: int = 31) -> np.ndarray:
+    """``n`` encapsulation big beads of the given radius at seeded uniform positions in the
+    workload's box, each at least (sigma_bead + 2 radius)/2 from every subunit bead and 2 radius
+    from the other big beads (the placement rule of generate_big_beads,
+    src/initialize.cpp:603-672, with numpy's generator instead of rand())."""
+    rng = np.random.default_rng(seed)
+    L = float(w.derived.box)
+    sig = np.tile(np.asarray(w.template.diameter, dtype=np.float64), int(w.opt.S))
+    min_d = sig / 2 + radius
+    out = []
+    while len(out) < n:
+        p = (rng.random(3) - 0.5) * L
+        d = w.state.pos - p
+        d -= L * np.floor(d / L + 0.5)
+        if np.any((d * d).sum(axis=1) < min_d * min_d):
+            continue
+        if any(np.sum(((q - p) - L * np.floor((q - p) / L + 0.5)) ** 2) < (2 * radius) ** 2 for q in out):
+            continue
+        out.append(p)
+    return np.array(out).reshape(-1, 3)
+
+
 def analysis_frames(n_sub: int = 2000, n_frames: int = 4, seed: int = 4242, conc_um: float = 800.0,
                     cluster_frac: float = 0.6, sigma_si: float = 1e-9):
     """Frames for the post-run analysis: 43-bead capsomeres (the bilayer patch plus a centre

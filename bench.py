@@ -99,6 +99,18 @@ def _profile_traffic():
     return None
 
 
+def rank_aggregate(total_ms: float, beads_per_rank: int, steps: int, world: int, dist=None):
+    """Whole-job figures of a weak-scaling run (every rank an independent replica of the
+    workload): the slowest rank's timed region (max over ranks, ms) and the total bead-steps/s
+    of all ranks over it."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, world * beads_per_rank * steps / (total_ms / 1e3)
+
+
 BIG_BEAD = dict(sigma=6.0, charge=-78.0, shc=3.5)  # the reference's defaults -a 3 -G -78 -H 3.5
 
 
@@ -817,11 +829,7 @@ def main():
     th.join()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
     total_ms = float(sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * w.n_beads * args.steps / (total_ms / 1e3)
+    total_ms, value = rank_aggregate(total_ms, w.n_beads, args.steps, world, dist)
 
     # warm-L2 throughput: the same K steps as whole graph windows, no flush
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -27,6 +27,8 @@ path on one system (--debye-length, --concentration set its parameters); --repli
 of N uneven systems in one handle (--replica-subunits S: N systems of S subunits at the plain
 workload's parameters; with --surrogate: the surrogate+batched measurement alone);
 --gemm: the surrogate network's forward pass at several row counts against the tensor peak;
+--drift-steps K: extended-energy drift per 10^4 steps, temperature, potential and radius of
+gyration over K steps of the default workload;
 --big-beads M: the default workload with M encapsulation big beads (-p true -a 3 -G -78 -H 3.5);
 --profile: a few steps without autotuning or timing, for a profiler (plain, --replicas, or
 --replicas --surrogate after training);
@@ -555,6 +557,55 @@ def bench_gemm(args):
                      "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured)" if peaks else "fallback 1900"}}))
 
 
+def bench_drift(args):
+    """Long-run statistics of the plain path on the default workload: extended energy (particle
+    kinetic + potential + thermostat energies) per bead sampled every 500 steps over --drift-steps
+    MD steps, its linear drift per bead per 10^4 steps, mean temperature and potential energy,
+    and the mean subunit radius of gyration (each subunit unwrapped around its first bead)."""
+    import numpy as np
+    from souffle_gb300 import gpu, workloads
+    w = workloads.plain_large(args.subunits, debye_length=args.debye_length, conc_um=args.concentration,
+                              nhc_mass=args.nhc_mass)
+    p = gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local)
+    s = gpu.GpuSystem(w.template, [p])
+    s.set_state(w.state.pos, w.state.vel)
+    s.md_begin()
+    n, np_, L = w.n_beads, w.template.n_beads, float(w.derived.box)
+    every = 500
+
+    def rg():
+        pos, _ = s.get_state()
+        q = pos.reshape(-1, np_, 3)
+        d = q - q[:, :1, :]
+        d -= L * np.round(d / L)
+        c = d.mean(axis=1, keepdims=True)
+        return float(np.sqrt(((d - c) ** 2).sum(axis=2).mean(axis=1)).mean())
+
+    rows = []
+    t0 = time.perf_counter()
+    for a in range(0, args.drift_steps + 1, every):
+        if a:
+            s.md_steps(a - every + 1, every)
+        e = s.energies()
+        pot = e["stretching"] + e["bending"] + e["lj"] + e["electrostatic"]
+        rows.append((a, e["temperature"], pot / n, (pot + e["kinetic"] + e["thermo_pe"] + e["thermo_ke"]) / n, rg()))
+    wall = time.perf_counter() - t0
+    r = np.array(rows)
+    half = len(r) // 2
+    slope = float(np.polyfit(r[:, 0], r[:, 3], 1)[0] * 1e4)
+    print(json.dumps({
+        "metric": "extended-energy drift per bead per 1e4 steps", "value": slope, "unit": "kT per bead",
+        "n_gpus": 1, "steps": args.drift_steps, "higher_is_better": False, "dtype": "f32+i64 fixed / f64",
+        "data": "synthetic", "config": {"workload": f"plain_large: {args.subunits} bilayer capsomeres x 42 "
+                                                    f"beads = {n} beads, {w.opt.C:g} uM, -e 5 -L 0.3 -B 10 "
+                                                    f"-t 0.005 -q 5 -Q {w.opt.Q:g}", "sample_every": every},
+        "T_mean_second_half": float(r[half:, 1].mean()), "T_std_second_half": float(r[half:, 1].std()),
+        "potential_per_bead_mean_second_half": float(r[half:, 2].mean()),
+        "rg_mean_second_half": float(r[half:, 4].mean()),
+        "extended_energy_per_bead_first_last": [float(r[0, 3]), float(r[-1, 3])],
+        "wall_s": wall}))
+
+
 def cpu_analysis_port(n_sub: int, seconds: float = 10.0):
     """Time the C restatement of the reference's analysis loops (oracle/analysis_port.c, long
     double, one thread, as the reference's analyze_output) on frames of the same generator at two
@@ -722,6 +773,9 @@ def main():
     ap.add_argument("--concentration", type=float, default=0.0, help="subunits in uM (default 800)")
     ap.add_argument("--big-beads", type=int, default=0,
                     help="encapsulation: this many big beads (-a 3 -G -78 -H 3.5) in the workload")
+    ap.add_argument("--nhc-mass", type=float, default=0.0, help="-Q for --drift-steps (default 10)")
+    ap.add_argument("--drift-steps", type=int, default=0,
+                    help="long-run statistics: extended-energy drift, T, potential, Rg over this many steps")
     ap.add_argument("--gemm", action="store_true",
                     help="the surrogate network's forward pass (tcgen05 GEMMs) at several row counts")
     ap.add_argument("--no-surrogate-batched", action="store_true",
@@ -733,6 +787,8 @@ def main():
     args = ap.parse_args()
     if args.gemm:
         return bench_gemm(args)
+    if args.drift_steps:
+        return bench_drift(args)
     if args.replicas and args.surrogate:
         return bench_surrogate_batched(args)
     if args.replicas:

@@ -72,10 +72,13 @@ def plain_small(seed: int = 12345) -> Workload:
 
 
 def plain_large(n_sub: int = 2000, seed: int = 12345, debye_length: float = 0.0,
-                conc_um: float = 0.0) -> Workload:
-    """The bilayer workload; ``debye_length`` (sigma) and ``conc_um`` (micromolar) override the
-    default screening length of 1 sigma and concentration of 800 uM when nonzero."""
+                conc_um: float = 0.0, nhc_mass: float = 0.0) -> Workload:
+    """The bilayer workload; ``debye_length`` (sigma), ``conc_um`` (micromolar) and ``nhc_mass``
+    (-Q) override the default screening length of 1 sigma, concentration of 800 uM and chain
+    mass of 10 when nonzero."""
     over = {}
+    if nhc_mass:
+        over["Q"] = nhc_mass
     if debye_length:
         over["c"] = state.salt_for_debye_length(debye_length)
     if conc_um:

@@ -369,7 +369,10 @@ def surrogate_batched(args):
     from souffle_gb300 import gpu, workloads
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    reps = workloads.replicas(args.replicas, seed=2024)
+    if getattr(args, "replica_subunits", 0):
+        reps = workloads.uniform_replicas(args.replicas, args.replica_subunits)
+    else:
+        reps = workloads.replicas(args.replicas, seed=2024)
     gen_s = time.perf_counter() - t0
     params = [gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local) for w in reps]
     tpl = reps[0].template
@@ -444,6 +447,12 @@ def surrogate_batched(args):
         a1 = a0 + k
         temps = {i: [] for i in watch}
         pots = {i: [] for i in watch}
+        if args.stat_steps <= 0:  # throughput only
+            st = gpu.surrogate_stats(s) if enabled else None
+            return {"value": n * k / (ms / 1e3), "ms_per_step": ms / k, "T_mean": None, "potential_mean": None,
+                    "potential_std": None,
+                    "judge": {"judged": st["judged"], "classes_off": st["classes_off"],
+                              "last_error": st["last_error"]} if st else None}
         for q in range(args.stat_steps // 20):
             s.md_steps(a1, 20)
             a1 += 20
@@ -502,9 +511,11 @@ def surrogate_batched(args):
         "ms_per_step": surr["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 network (fp32 accumulate) + f32/i64 exact path",
         "data": "synthetic (seeded replicas)",
-        "config": {"workload": f"replica sweep: {len(reps)} systems of bilayer capsomeres, {S_tot} "
+        "config": {"workload": f"replicas: {len(reps)} systems of bilayer capsomeres, {S_tot} "
                                f"subunits, {n} beads, subunits per system {min(sizes)}-{max(sizes)}, "
-                               f"eps 1.5-3.0, Debye length 0.5-2.0 sigma, 200-1600 uM; switch radius "
+                               + ("eps 2.1, Debye length 1 sigma, 800 uM" if getattr(args, "replica_subunits", 0)
+                                  else "eps 1.5-3.0, Debye length 0.5-2.0 sigma, 200-1600 uM")
+                               + f"; switch radius "
                                f"3.5 sigma (closest bead pair), judge 1 % of far pairs every 100 steps",
                    "l2": "batched: working set larger than L2, whole rebuild windows; plain: L2 "
                          "flushed before each replica's window"},

@@ -111,12 +111,33 @@ void forceCalculation(vector<SUBUNIT>& protein, double lb, double ni, double qs,
   }
 }
 
-// The encapsulation term (src/forces.cpp:174-236) is outside the GPU path; a build that links
-// this file runs without -p.
+// The encapsulation term (src/forces.cpp:174-236), called right after forceCalculation
+// (src/md.cpp:242,444).  The big beads never move, so the first call hands them to the handle
+// (souffle_gpu_set_big_beads: positions, diameter and charge of big_bead[0], hard-core distance)
+// and re-evaluates the forces with them (same pair list); from then on forceCalculation's GPU
+// forces already hold the big-bead terms and this call adds nothing.  The big beads' own
+// eforce / ljforce / tforce, which run_simulation never reads, are not filled in.
 void forceCalculation_bigbead(vector<BEAD>& big_bead, vector<BEAD>& subunit_bead, double ecut, double lb,
                               double ni, double qs, double ecut_el, double kappa, double shc) {
-  (void)big_bead; (void)subunit_bead; (void)ecut; (void)lb; (void)ni; (void)qs; (void)ecut_el;
-  (void)kappa; (void)shc;
-  fprintf(stderr, "souffle_gb300: encapsulation (-p true) is not supported by the GPU forces\n");
-  exit(1);
+  (void)ecut; (void)lb; (void)ni; (void)qs; (void)ecut_el; (void)kappa;
+  static bool big_set = false;
+  if (big_set || big_bead.empty()) return;
+  if (!g_handle) {
+    fprintf(stderr, "souffle_gb300: forceCalculation_bigbead before forceCalculation\n");
+    exit(1);
+  }
+  vector<double> bp(3 * big_bead.size());
+  for (size_t i = 0; i < big_bead.size(); i++) {
+    bp[3 * i] = (double)big_bead[i].pos.x;
+    bp[3 * i + 1] = (double)big_bead[i].pos.y;
+    bp[3 * i + 2] = (double)big_bead[i].pos.z;
+  }
+  souffle_status st = souffle_gpu_set_big_beads(g_handle, 0, (int32_t)big_bead.size(), bp.data(),
+                                                big_bead[0].sigma, big_bead[0].q, shc);
+  if (st != SOUFFLE_OK) die(st, "souffle_gpu_set_big_beads");
+  big_set = true;
+  st = souffle_gpu_forces(g_handle, 0, g_tf.data(), nullptr, nullptr);
+  if (st != SOUFFLE_OK) die(st, "souffle_gpu_forces");
+  for (size_t i = 0; i < subunit_bead.size(); i++)
+    subunit_bead[i].tforce = VECTOR3D(g_tf[3 * i], g_tf[3 * i + 1], g_tf[3 * i + 2]);
 }

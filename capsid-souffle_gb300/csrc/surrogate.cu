@@ -178,23 +178,13 @@ __global__ void __launch_bounds__(128) k_far_classify(FarArgs a) {
   for (int c = warp; c < ncand; c += nw) {
     const int j = a.cand[(size_t)i * a.cand_cap + c];
     float d2 = 3.0e38f;
-    bool near = j == i;
-    if (j != i) {
-      // closest bead pair; stops as soon as any bead pair is inside the switch radius (a near
-      // pair needs no distance, and sqrtf is monotone, so the partial minimum decides it)
-      for (int base = 0; base < np && !near; base += 32) {
-        const int jj = base + lane;
-        const int4 pj = a.pos32[(size_t)j * np + min(jj, np - 1)];
-        for (int i0 = 0; i0 < np; i0 += 8) {
-          const int i1 = min(np, i0 + 8);
-          for (int ii = i0; ii < i1; ii++) {
-            const float3 d = dpos(s_pa[ii], pj, unit);
-            d2 = fminf(d2, dot3_(d, d));
-          }
-          if (__any_sync(0xffffffffu, sqrtf(d2) < a.r_switch)) {
-            near = true;
-            break;
-          }
+    const bool near = j == i;
+    if (j != i) {  // closest bead pair (an early exit at the switch radius measured slower)
+      for (int jj = lane; jj < np; jj += 32) {
+        const int4 pj = a.pos32[(size_t)j * np + jj];
+        for (int ii = 0; ii < np; ii++) {
+          const float3 d = dpos(s_pa[ii], pj, unit);
+          d2 = fminf(d2, dot3_(d, d));
         }
       }
 #pragma unroll

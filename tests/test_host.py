@@ -138,3 +138,30 @@ def test_replica_draws_are_seeded_and_in_range():
     for x, y in zip(a, b):
         assert x.opt.S == y.opt.S and x.opt.E == y.opt.E and np.array_equal(x.state.pos, y.state.pos)
         assert 20 <= x.opt.S <= 500 and 1.5 <= x.opt.E <= 3.0 and 200 <= x.opt.C <= 1600
+
+
+def test_big_bead_placement_keeps_its_distances():
+    """Bench placement of encapsulation big beads: inside the box, at least sigma_bead/2 + radius
+    from every subunit bead and 2 radius from each other (the rule of generate_big_beads)."""
+    from souffle_gb300 import workloads
+    w = workloads.plain_small(seed=7)
+    big = workloads.place_big_beads(w, 5, radius=3.0, seed=3)
+    L = float(w.derived.box)
+    assert big.shape == (5, 3) and np.all(np.abs(big) <= L / 2)
+    for i, p in enumerate(big):
+        d = w.state.pos - p
+        d -= L * np.floor(d / L + 0.5)
+        assert np.sqrt((d * d).sum(axis=1)).min() >= 0.5 + 3.0
+        for q in big[:i]:
+            e = q - p
+            e -= L * np.floor(e / L + 0.5)
+            assert np.sqrt((e * e).sum()) >= 6.0
+    assert np.array_equal(big, workloads.place_big_beads(w, 5, radius=3.0, seed=3))
+
+
+def test_uniform_replicas_are_independent_copies():
+    from souffle_gb300 import workloads
+    reps = workloads.uniform_replicas(3, 12)
+    assert [int(r.opt.S) for r in reps] == [12, 12, 12]
+    assert reps[0].derived.box == reps[2].derived.box
+    assert not np.array_equal(reps[0].state.pos, reps[1].state.pos)

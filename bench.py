@@ -984,6 +984,12 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_forces", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800"},
+        # the compute side of the same kernel: ~40 FP32 operations per pair of the reference list
+        # (n_bar pairs per bead, the survey's estimate) against the nominal FP32 rate
+        "roofline_fp32": {"achieved": 40.0 * n_bar * w.n_beads / (forces_ms / 1e3) / 1e12,
+                          "peak": 152 * 128 * 2 * 2.07e9 / 1e12, "unit": "TFLOP/s",
+                          "frac": 40.0 * n_bar * w.n_beads / (forces_ms / 1e3) / (152 * 128 * 2 * 2.07e9),
+                          "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz"},
         "roofline_step": {"achieved": step_bytes * value / w.n_beads / 1e9, "peak": peak,
                           "unit": "GB/s", "frac": step_bytes * value / w.n_beads / 1e9 / peak,
                           "bytes_per_bead_step": step_bytes / w.n_beads},

@@ -116,13 +116,22 @@ def rank_aggregate(total_ms: float, beads_per_rank: int, steps: int, world: int,
 BIG_BEAD = dict(sigma=6.0, charge=-78.0, shc=3.5)  # the reference's defaults -a 3 -G -78 -H 3.5
 
 
-def cpu_reference(w, seconds: float = 10.0, max_steps: int = 30, threads: int = 0, big_beads=None):
-    """Time the oracle port (long double, OpenMP) on the workload: bead-steps/s."""
+def cpu_reference(w, seconds: float = 10.0, max_steps: int = 30, threads: int = 0, big_beads=None,
+                  steps: int = 0, warmup: int = 1, variant: str = "ld"):
+    """Time the oracle port (OpenMP over subunits) on the workload: bead-steps/s.
+
+    With ``steps`` > 0, exactly ``warmup`` untimed steps (the first with a pair-list rebuild)
+    then exactly ``steps`` timed steps; otherwise one warm-up step and a bounded sample of
+    3..max_steps steps or about ``seconds``.  ``variant`` "ld" is the restatement in the
+    reference's long double; "f64" the same algorithm with long double replaced by double (a
+    labelled variant, not the reference)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import platform
+
     import pyoracle
     threads = threads or os.cpu_count()
     o = pyoracle.Oracle(w.template, int(w.opt.S), w.derived, w.opt.s, w.opt.b, w.opt.E,
-                        w.center_local)
+                        w.center_local, variant=variant)
     o.set_threads(threads)
     o.set_state(w.state.pos, w.state.vel)
     if big_beads is not None and len(big_beads):
@@ -130,20 +139,51 @@ def cpu_reference(w, seconds: float = 10.0, max_steps: int = 30, threads: int = 
     o.forces(True)
     ke = o.kinetic_energy()
     o.nhc_init(int(w.opt.q), w.opt.Q, w.opt.K)
-    ke, _, _ = o.md_step(0, w.opt.t, int(w.opt.B), ke)  # warm-up step (with a rebuild)
+    n_warm = max(1, warmup) if steps > 0 else 1
+    for a in range(n_warm):  # the first warm-up step rebuilds the pair list (a % B == 0)
+        ke, _, _ = o.md_step(a, w.opt.t, int(w.opt.B), ke)
     t0 = time.perf_counter()
-    steps = 0
-    while steps < max_steps and (steps < 3 or time.perf_counter() - t0 < seconds):
-        ke, _, _ = o.md_step(1 + steps, w.opt.t, int(w.opt.B), ke)
-        steps += 1
+    done = 0
+    while (done < steps) if steps > 0 else (done < max_steps and (done < 3 or time.perf_counter() - t0 < seconds)):
+        ke, _, _ = o.md_step(n_warm + done, w.opt.t, int(w.opt.B), ke)
+        done += 1
     dt = time.perf_counter() - t0
-    import platform
-    return {"value": w.n_beads * steps / dt, "unit": "bead-steps/s", "cores": threads,
-            "kind": "port",
-            "sample": f"{steps} MD steps (rebuild every {int(w.opt.B)}) of the {w.n_beads}-bead "
-                      f"workload after one warm-up step; long double = "
-                      f"{'x87 80-bit' if platform.machine() in ('x86_64', 'AMD64') else 'IEEE binary128 (software)'}"
-                      f" on {platform.machine()}"}
+    if variant == "ld":
+        arith = ("long double = " + ("x87 80-bit" if platform.machine() in ("x86_64", "AMD64")
+                                     else "IEEE binary128 (software)") + f" on {platform.machine()}")
+    else:
+        arith = f"long double replaced by double (FP64-patched variant, not the reference) on {platform.machine()}"
+    return {"value": w.n_beads * done / dt, "unit": "bead-steps/s", "cores": threads,
+            "kind": "port", "steps": done, "warmup": n_warm,
+            "sample": f"{done} MD steps (rebuild every {int(w.opt.B)}) of the {w.n_beads}-bead "
+                      f"workload after {n_warm} warm-up step{'s' if n_warm > 1 else ''}; {arith}"}
+
+
+def oracle_parity(w, s):
+    """Forces and pair lists of the handle ``s`` (state just set, before any step) against the
+    oracle in long double on the same state: per-bead force RMS relative errors and whether the
+    pair lists are identical in content and order."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import numpy as np
+
+    import pyoracle
+    tf, sf, bf = s.forces(rebuild=True, parts=True)
+    o = pyoracle.Oracle(w.template, int(w.opt.S), w.derived, w.opt.s, w.opt.b, w.opt.E, w.center_local)
+    o.set_threads(os.cpu_count())
+    o.set_state(w.state.pos, w.state.vel)
+    otf, osf, obf, over = o.forces(True)
+    oc, oi = o.pairlist()
+    gc, gi = s.pairlist(o.cap)
+    wdt = oi.shape[1]
+    o_pad = np.where(np.arange(wdt)[None, :] < oc[:, None], oi, -1)
+    same = bool(over == 0 and np.array_equal(gc, oc) and np.array_equal(gi[:, :wdt], o_pad))
+    tot2 = float((otf ** 2).sum())
+    return {"force_rms_rel_error": float(np.sqrt(((tf - otf) ** 2).sum() / tot2)),
+            "bending_rms_rel_error": float(np.sqrt(((bf - obf) ** 2).sum() / (obf ** 2).sum())),
+            "stretching_rms_error_vs_total": float(np.sqrt(((sf - osf) ** 2).sum() / tot2)),
+            "pairlist_identical": same, "pairs": int(oc.sum()),
+            "against": "oracle (C restatement in long double, pinned bit for bit to the compiled reference "
+                       "on x86-64), same seeded initial state, one rebuild + forces"}
 
 
 def bench_replicas(args):
@@ -771,6 +811,8 @@ def main():
     ap.add_argument("--subunits", type=int, default=2000)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the forces / pair-list check against the oracle on the initial state")
     ap.add_argument("--profile", action="store_true",
                     help="md_begin, then --steps MD steps as direct launches (no graphs); for ncu")
     ap.add_argument("--replicas", type=int, default=0,
@@ -835,17 +877,23 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_reference(w, seconds=args.cpu_seconds, big_beads=big)
+        # exactly --warmup untimed then --steps timed MD steps of the oracle port
+        cb = cpu_reference(w, big_beads=big, steps=args.steps, warmup=args.warmup)
         steps_ms = w.n_beads / cb["value"] * 1e3
-        print(json.dumps({
+        line = {
             "impl": "reference", "metric": "bead-steps/s", "value": cb["value"],
-            "unit": "bead-steps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": steps_ms, "higher_is_better": True,
+            "unit": "bead-steps/s", "n_gpus": args.gpus, "steps": cb["steps"],
+            "warmup": cb["warmup"], "ms_per_step": steps_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "long double (f80/f128)",
             "data": "synthetic (seeded random capsomere states)", "config": config,
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}))
+                    "d2h_bytes_per_step": 0}}
+        if not args.no_cpu_baseline:
+            # context only: the same algorithm with long double replaced by double
+            line["cpu_baseline_fp64_patched"] = cpu_reference(w, big_beads=big, variant="f64",
+                                                              seconds=args.cpu_seconds)
+        print(json.dumps(line))
         return
 
     import numpy as np
@@ -864,6 +912,9 @@ def main():
     s.set_state(w.state.pos, w.state.vel)
     if big is not None:
         s.set_big_beads(big, BIG_BEAD["sigma"], BIG_BEAD["charge"], BIG_BEAD["shc"])
+    parity = None
+    if rank == 0 and not args.profile and not args.no_parity and big is None:
+        parity = oracle_parity(w, s)
     tuning = s.autotune(trials=20) if not args.profile else None
     s.md_begin()
     if args.profile:
@@ -995,8 +1046,14 @@ def main():
                           "bytes_per_bead_step": step_bytes / w.n_beads},
         "clocks": _summarize_clocks(samples),
     }
+    if parity is not None:
+        out["force_rms_rel_error"] = parity["force_rms_rel_error"]
+        out["pairlist_identical"] = parity["pairlist_identical"]
+        out["parity"] = parity
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference(w, seconds=args.cpu_seconds, big_beads=big)
+        out["cpu_baseline_fp64_patched"] = cpu_reference(w, seconds=args.cpu_seconds, big_beads=big,
+                                                         variant="f64")
     if rank == 0 and world == 1 and not args.no_surrogate_batched and not args.big_beads:
         # the replica sweep with the learned surrogate against the plain single-system path
         s.close()

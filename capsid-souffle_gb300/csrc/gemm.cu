@@ -37,7 +37,9 @@ struct GemmTile {
   static constexpr int kStage = kA + kB;
   // a tile's K = 256 in flight (deeper rings measured no faster)
   static constexpr int kStages = 4;
-  static constexpr int kBars = 2 * kStages + 4;  // full[s], empty[s], tmem_full[2], tmem_empty[2]
+  // full[s], empty[s], tmem_full[2], tmem_empty[2], and one barrier the MMA issuer drains its own
+  // MMAs on when it gives up early
+  static constexpr int kBars = 2 * kStages + 5;
   static constexpr int kSmem = 1024 + kStages * kStage + kBars * 8 + 16;
   static constexpr int kTmemCols = 2 * BN;      // two accumulators
   static_assert(kStage % 1024 == 0, "stages stay on 1024-byte boundaries (128-byte swizzle atoms)");
@@ -64,7 +66,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t base = (raw + 1023u) & ~1023u;
   const uint32_t bars = base + G::kStages * G::kStage;
   const uint32_t full0 = bars, empty0 = bars + 8 * G::kStages;
-  const uint32_t tfull0 = bars + 16 * G::kStages, tempty0 = tfull0 + 16;
+  const uint32_t tfull0 = bars + 16 * G::kStages, tempty0 = tfull0 + 16, drain = tempty0 + 16;
   const uint32_t tmem_slot = bars + G::kBars * 8;
   volatile uint32_t* tmem_slot_ptr = reinterpret_cast<volatile uint32_t*>(smem_raw + (tmem_slot - raw));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -88,6 +90,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(tfull0 + 8 * b, 1);
       mbar_init(tempty0 + 8 * b, kEpiWarps);
     }
+    mbar_init(drain, 1);
     mbar_fence_init();
   }
   if (threadIdx.x == 64) {
@@ -154,7 +157,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       umma_commit(tfull0 + 8 * b);  // after every MMA issued above has completed
     }
-    if (!ok) atomicOr(e.err, e.err_bit);
+    if (!ok) {
+      atomicOr(e.err, e.err_bit);
+      // MMAs issued before the timeout may still be writing tensor memory: wait (bounded) for
+      // them before the CTA releases it
+      umma_commit(drain);
+      mbar_wait(drain, 0);
+    }
   } else if (warp >= 4) {
     // ---- epilogue
     const int quarter = warp & 3, half = (warp - 4) >> 2;

@@ -137,6 +137,7 @@ def load() -> C.CDLL:
     lib.souffle_gpu_stream.argtypes = [vp]
     lib.souffle_gpu_md_profile.argtypes = [vp, C.c_int64, C.c_int32, C.POINTER(KernelTimes_)]
     lib.souffle_gpu_autotune.argtypes = [vp, C.c_int32, C.POINTER(Tuning_)]
+    lib.souffle_gpu_kinetic_energy_noalloc.argtypes = [dp, dp, C.c_int64, dp, vp]
     fp = C.POINTER(C.c_float)
     lib.souffle_mlp_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_int32,
                                        C.POINTER(vp)]

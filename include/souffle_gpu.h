@@ -231,9 +231,11 @@ souffle_status souffle_gpu_autotune(souffle_gpu_system* h, int32_t trials, souff
  *   out    device pointer, 4 doubles: sum 1/2 m |v|^2, sum vx, sum vy, sum vz
  *   stream cudaStream_t (NULL = default stream); the call is asynchronous on it
  * At most 4,194,304 beads (SOUFFLE_ERR_BAD_INPUT beyond).  Nothing is allocated or freed.  The
- * first call on a device looks up the scratch address for that device, so make it before any
- * stream capture.  All calls share the scratch: calls that overlap on the GPU race; order them
- * on one stream.  The result is bitwise the same on every call for the same input. */
+ * first call on a device looks up the scratch address for that device and keeps it for the rest
+ * of the process, so make it before any stream capture, and do not reset the device
+ * (cudaDeviceReset) after it: the kept address would then be stale.  All calls share the scratch:
+ * calls that overlap on the GPU race; order them on one stream.  The result is bitwise the same
+ * on every call for the same input. */
 souffle_status souffle_gpu_kinetic_energy_noalloc(const double* vel, const double* mass, int64_t n_beads,
                                                   double* out, void* stream);
 

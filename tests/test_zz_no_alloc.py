@@ -75,3 +75,32 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     assert rc == 1
     assert b"scratch limit" in lib.souffle_gpu_last_error()
     assert torch.count_nonzero(buf).item() == 0
+
+
+@pytest.mark.parametrize("n", [600_001, 4_194_304])
+def test_noalloc_large_inputs_against_float64_sums(n):
+    """Sizes where the 2048-block grid takes several beads per thread, up to the limit itself."""
+    import torch
+    from souffle_gb300 import gpu
+    lib = gpu.load()
+    rng = np.random.default_rng(n)
+    vel = rng.normal(size=(n, 3))
+    mass = rng.uniform(0.5, 2.0, size=n)
+    d_vel = torch.tensor(vel.reshape(-1), dtype=torch.float64, device="cuda")
+    d_mass = torch.tensor(mass, dtype=torch.float64, device="cuda")
+    d_out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    dp = C.POINTER(C.c_double)
+    results = []
+    for _ in range(2):
+        rc = lib.souffle_gpu_kinetic_energy_noalloc(C.cast(d_vel.data_ptr(), dp), C.cast(d_mass.data_ptr(), dp), n,
+                                                    C.cast(d_out.data_ptr(), dp), C.c_void_p(stream))
+        assert rc == 0, lib.souffle_gpu_last_error()
+        torch.cuda.synchronize()
+        results.append(d_out.cpu().numpy().copy())
+    ke = 0.5 * (mass * (vel ** 2).sum(axis=1)).sum()
+    for out in results:
+        assert out[0] == pytest.approx(ke, rel=1e-12)
+        # velocity sums cancel: compare against the scale of the summed magnitudes
+        np.testing.assert_allclose(out[1:], vel.sum(axis=0), rtol=0, atol=1e-12 * np.abs(vel).sum(axis=0).max())
+    assert np.array_equal(results[0], results[1])

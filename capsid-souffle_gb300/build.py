@@ -21,7 +21,7 @@ OUT = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(REPO, "include")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["pairlist.cu", "forces.cu", "energies.cu", "souffle_gpu.cu", "noalloc.cu", "gemm.cu", "mlp.cu", "surrogate.cu",
+CU_SOURCES = ["pairlist.cu", "forces.cu", "energies.cu", "souffle_gpu.cu", "noalloc.cu", "gemm.cu", "mlp.cu", "mlp_fused.cu", "surrogate.cu",
               "analysis.cu"]
 LIB = os.path.join(OUT, "libsouffle_gb300.so")
 DRIVER = os.path.join(OUT, "souffle_gb300")

@@ -25,6 +25,10 @@
 
 namespace souffle {
 void record_error(const std::string& msg);
+bool mlp_fused_supported(int n_in, int width, int out_pad);
+cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const int* m_dyn, int n_in,
+                              const __nv_bfloat16* const w[4], const int ldw[4], int out_pad, const float* const bias[4],
+                              float* y, int ldy, unsigned int* err, unsigned int err_bit, cudaStream_t st);
 }
 
 using namespace souffle;
@@ -302,6 +306,9 @@ namespace souffle {
 
 constexpr unsigned int kErrSurrogateBit = 8u;  // the system's error word: surrogate network timeout
 
+cudaError_t mlp_forward_packed_async(souffle_mlp* h, int m_cap, const int* m_dyn, unsigned int* err, cudaStream_t st,
+                                     const float** y, int* ldy);
+
 // For the surrogate inside a system handle: forward over m_cap rows of x on the caller's stream,
 // rows >= *m_dyn skipped, output left in the network's buffer (*y, row stride *ldy).  Enqueues
 // only, so it can be captured in a CUDA graph.
@@ -312,9 +319,33 @@ cudaError_t mlp_forward_async(souffle_mlp* h, const float* x, int m_cap, const i
       x, m_cap, h->n_in, h->act[0].p, h->in_ld[0], nullptr, h->cap, m_dyn);
   cudaError_t r = cudaGetLastError();
   if (r != cudaSuccess) return r;
-  r = forward_on(h, m_cap, false, st, m_dyn, err, kErrSurrogateBit);
+  return mlp_forward_packed_async(h, m_cap, m_dyn, err, st, y, ldy);
+}
+
+// The network's BF16 input buffer [cap][*ld] (row-major), which mlp_forward_packed_async reads.
+__nv_bfloat16* mlp_input_bf16(souffle_mlp* h, int* ld) {
+  *ld = h->in_ld[0];
+  return h->act[0].p;
+}
+
+// Forward over rows already in the BF16 input buffer: the fused one-kernel forward
+// (mlp_fused.cu) where the shape allows it, else the per-layer GEMMs.  Enqueues only.
+cudaError_t mlp_forward_packed_async(souffle_mlp* h, int m_cap, const int* m_dyn, unsigned int* err, cudaStream_t st,
+                                     const float** y, int* ldy) {
+  if (m_cap < 1 || m_cap > h->cap) return cudaErrorInvalidValue;
+  const int L = kLayers - 1;
+  cudaError_t r;
+  if (mlp_fused_supported(h->n_in, h->width, h->out_pad[L])) {
+    const __nv_bfloat16* w[4] = {h->wb[0].p, h->wb[1].p, h->wb[2].p, h->wb[3].p};
+    const int ldw[4] = {h->in[0], h->in[1], h->in[2], h->in[3]};
+    const float* b[4] = {h->b[0].p, h->b[1].p, h->b[2].p, h->b[3].p};
+    r = mlp_forward_fused(h->act[0].p, h->in_ld[0], m_cap, m_dyn, h->n_in, w, ldw, h->out_pad[L], b, h->y.p,
+                          h->out_pad[L], err, kErrSurrogateBit, st);
+  } else {
+    r = forward_on(h, m_cap, false, st, m_dyn, err, kErrSurrogateBit);
+  }
   *y = h->y.p;
-  *ldy = h->out_pad[kLayers - 1];
+  *ldy = h->out_pad[L];
   return r;
 }
 
@@ -407,6 +438,8 @@ souffle_status souffle_mlp_create(int32_t n_in, int32_t width, int32_t n_out, in
   return SOUFFLE_OK;
 }
 
+void* souffle_mlp_stream(const souffle_mlp* h) { return h ? static_cast<void*>(h->stream) : nullptr; }
+
 souffle_status souffle_mlp_destroy(souffle_mlp* h) {
   if (!h) return SOUFFLE_OK;
   cudaSetDevice(h->device);
@@ -456,6 +489,20 @@ souffle_status souffle_mlp_set_params(souffle_mlp* h, const float* host_in, int6
 }
 
 souffle_status souffle_mlp_forward(souffle_mlp* h, const float* x_dev, int32_t m, float* y_dev) {
+  if (!h || !x_dev || !y_dev || m < 1 || m > h->cap) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  MLP_TRY(cudaSetDevice(h->device));
+  souffle_status s = pack_input(h, x_dev, m, false);
+  if (s != SOUFFLE_OK) return s;
+  const float* y = nullptr;
+  int ldy = 0;
+  MLP_TRY(souffle::mlp_forward_packed_async(h, m, nullptr, h->err.p, h->stream, &y, &ldy));
+  const int L = kLayers - 1;
+  k_unpad<<<blocks((long long)m * h->n_out, 256), 256, 0, h->stream>>>(h->y.p, h->out_pad[L], m, h->n_out, y_dev);
+  MLP_TRY(cudaGetLastError());
+  return check_gemm_err(h);
+}
+
+souffle_status souffle_mlp_forward_layered(souffle_mlp* h, const float* x_dev, int32_t m, float* y_dev) {
   if (!h || !x_dev || !y_dev || m < 1 || m > h->cap) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
   MLP_TRY(cudaSetDevice(h->device));
   souffle_status s = pack_input(h, x_dev, m, false);

@@ -17,6 +17,7 @@
 //                                revert to exact at the next rebuild
 // Training:     k_far_targets    exact forces of far pairs as (F, tau, residuals) in A's frame
 //               souffle_surrogate_fit normalises the data set and trains with mlp.cu's kernels.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,6 +38,9 @@ namespace souffle {
 void record_error(const std::string& msg);
 cudaError_t mlp_forward_async(souffle_mlp* h, const float* x, int m_cap, const int* m_dyn, unsigned int* err,
                               cudaStream_t st, const float** y, int* ldy);
+cudaError_t mlp_forward_packed_async(souffle_mlp* h, int m_cap, const int* m_dyn, unsigned int* err, cudaStream_t st,
+                                     const float** y, int* ldy);
+__nv_bfloat16* mlp_input_bf16(souffle_mlp* h, int* ld);
 void mlp_dims(const souffle_mlp* h, int* n_in, int* n_out, int* cap);
 }  // namespace souffle
 
@@ -66,6 +70,8 @@ struct FarArgs {
   const float* rest;     // [np][3]
   int anchor1, anchor2;
   float* x;              // [far_cap][kDesc]
+  __nv_bfloat16* xb;     // or, for inference: BF16 rows [far_cap][ldxb], the network's input buffer
+  int ldxb;
   const float* x_mean;   // null: raw descriptors
   const float* x_istd;
   const float* y;        // network output [far_cap][ldy], normalised
@@ -429,6 +435,20 @@ __device__ void far_descr_one(const FarArgs& a, int p) {
 #pragma unroll
     for (int k = 0; k < kDesc; k++) x[k] = (x[k] - a.x_mean[k]) * a.x_istd[k];
   }
+  if (a.xb) {  // BF16 rows (128 bytes) straight into the network's input buffer
+    uint4* out = reinterpret_cast<uint4*>(a.xb + (size_t)p * a.ldxb);
+#pragma unroll
+    for (int k = 0; k < kDesc / 8; k++) {
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const __nv_bfloat162 h2 = __floats2bfloat162_rn(x[8 * k + 2 * j], x[8 * k + 2 * j + 1]);
+        w[j] = *reinterpret_cast<const uint32_t*>(&h2);
+      }
+      out[k] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    return;
+  }
   float4* out = reinterpret_cast<float4*>(a.x + (size_t)p * kDesc);  // 256-byte rows
 #pragma unroll
   for (int k = 0; k < kDesc / 4; k++) out[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
@@ -451,25 +471,41 @@ __device__ __forceinline__ void net_body_forces(const FarArgs& a, const float* r
   }
 }
 
+// Forces on each subunit's beads from all its far pairs, warp per subunit.  The force on bead i
+// from one pair is affine in the network's output row (F / np + (J^-1 tau) x d_i + r_i after
+// de-normalisation), so the rows of the subunit's pairs are summed first (in pair order, one
+// output column per lane) and the per-bead forces are formed once from the sum.
 __global__ void __launch_bounds__(128) k_far_apply(FarArgs a) {
+  __shared__ float s_sum[4][256];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.x * 4 + warp;
   if (s >= a.S) return;
   const int lo = a.far_start[s], hi = a.far_start[s + 1];
+  float* sum = s_sum[warp];
+  Frame F{};
   float3 acc[kBeadsPerLane];
 #pragma unroll
   for (int k = 0; k < kBeadsPerLane; k++) acc[k] = f3_(0.f, 0.f, 0.f);
-  Frame F{};
   if (lo < hi) {
+    const float npairs = (float)(hi - lo);
+    for (int c = lane; c < a.n_out; c += 32) {
+      float t = 0.f;
+      for (int q = lo; q < hi; q++) t += a.y[(size_t)q * a.ldy + c];
+      sum[c] = t * a.t_std[c] + npairs * a.t_mean[c];
+    }
+    __syncwarp();
     F = load_frame(a.frame + (size_t)s * kFrame);
     float3 e[kBeadsPerLane];
     int4 p[kBeadsPerLane];
     body_coords(a, s, F, lane, e, p);
-    for (int q = lo; q < hi; q++) {
-      float3 g[kBeadsPerLane];
-      net_body_forces(a, a.y + (size_t)q * a.ldy, F, e, lane, g);
+    const float3 Ft = f3_(sum[0], sum[1], sum[2]);
+    const float3 w = mat3(F.Ji, f3_(sum[3], sum[4], sum[5]));
+    const float inv_np = 1.0f / (float)a.np;
 #pragma unroll
-      for (int k = 0; k < kBeadsPerLane; k++) acc[k] = add3(acc[k], g[k]);
+    for (int k = 0; k < kBeadsPerLane; k++) {
+      const int l = lane + 32 * k;
+      if (l < a.np)
+        acc[k] = add3(add3(mul3(Ft, inv_np), cross3_(w, e[k])), f3_(sum[6 + 3 * l], sum[7 + 3 * l], sum[8 + 3 * l]));
     }
   }
 #pragma unroll
@@ -815,10 +851,12 @@ void surrogate_forces(souffle_gpu_system* h, ForceArgs& fa) {
   FarArgs a = far_args(h);
   const int sb = (h->S + 3) / 4;
   k_sub_frames<<<sb, 128, 0, h->stream>>>(a);
+  // descriptors as BF16 rows straight into the network's input buffer, then the fused forward
+  a.xb = mlp_input_bf16(c.net, &a.ldxb);
   k_far_descr<<<std::min((c.far_cap + 127) / 128, 152 * 8), 128, 0, h->stream>>>(a);
   const float* y = nullptr;
   int ldy = 0;
-  if (mlp_forward_async(c.net, c.x.p, c.far_cap, c.far_total.p, h->err.p, h->stream, &y, &ldy) != cudaSuccess) {
+  if (mlp_forward_packed_async(c.net, c.far_cap, c.far_total.p, h->err.p, h->stream, &y, &ldy) != cudaSuccess) {
     // parameters were validated at attach; a launch failure surfaces through cudaGetLastError
     return;
   }

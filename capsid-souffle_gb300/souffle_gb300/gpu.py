@@ -30,8 +30,8 @@ EXPORTED = [
     "souffle_gpu_synchronize", "souffle_gpu_last_error", "souffle_gpu_stream",
     "souffle_gpu_md_profile", "souffle_gpu_kinetic_energy_noalloc", "souffle_gpu_autotune",
     # include/souffle_surrogate.h
-    "souffle_mlp_create", "souffle_mlp_destroy", "souffle_mlp_param_count", "souffle_mlp_get_params",
-    "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_gradients", "souffle_mlp_train_step",
+    "souffle_mlp_create", "souffle_mlp_destroy", "souffle_mlp_stream", "souffle_mlp_param_count", "souffle_mlp_get_params",
+    "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_forward_layered", "souffle_mlp_gradients", "souffle_mlp_train_step",
     "souffle_gemm_bf16", "souffle_surrogate_attach", "souffle_surrogate_collect", "souffle_surrogate_fit",
     "souffle_surrogate_enable", "souffle_surrogate_get_stats",
     # include/souffle_analysis.h
@@ -142,11 +142,14 @@ def load() -> C.CDLL:
     lib.souffle_mlp_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_int32,
                                        C.POINTER(vp)]
     lib.souffle_mlp_destroy.argtypes = [vp]
+    lib.souffle_mlp_stream.restype = C.c_void_p
+    lib.souffle_mlp_stream.argtypes = [vp]
     lib.souffle_mlp_param_count.restype = C.c_int64
     lib.souffle_mlp_param_count.argtypes = [vp]
     lib.souffle_mlp_get_params.argtypes = [vp, fp, C.c_int64]
     lib.souffle_mlp_set_params.argtypes = [vp, fp, C.c_int64]
     lib.souffle_mlp_forward.argtypes = [vp, vp, C.c_int32, vp]
+    lib.souffle_mlp_forward_layered.argtypes = [vp, vp, C.c_int32, vp]
     lib.souffle_mlp_gradients.argtypes = [vp, vp, vp, C.c_int32, fp, fp]
     lib.souffle_mlp_train_step.argtypes = [vp, vp, vp, C.c_int32, C.c_float, fp]
     lib.souffle_gemm_bf16.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
@@ -158,7 +161,7 @@ def load() -> C.CDLL:
     lib.souffle_surrogate_get_stats.argtypes = [vp, C.POINTER(SurrogateStats_)]
     for name in EXPORTED:
         if name not in ("souffle_gpu_last_error", "souffle_gpu_num_beads", "souffle_gpu_stream",
-                        "souffle_mlp_param_count"):
+                        "souffle_mlp_param_count", "souffle_mlp_stream"):
             getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -340,6 +343,10 @@ class Mlp:
         except Exception:
             pass
 
+    def stream(self) -> int:
+        """The network's cudaStream_t as an integer."""
+        return int(self.lib.souffle_mlp_stream(self.h) or 0)
+
     def get_params(self) -> np.ndarray:
         out = np.empty(self.n_params, dtype=np.float32)
         _check(self.lib.souffle_mlp_get_params(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), self.n_params))
@@ -351,6 +358,10 @@ class Mlp:
 
     def forward(self, x_ptr: int, m: int, y_ptr: int) -> None:
         _check(self.lib.souffle_mlp_forward(self.h, C.c_void_p(x_ptr), m, C.c_void_p(y_ptr)))
+
+    def forward_layered(self, x_ptr: int, m: int, y_ptr: int) -> None:
+        """The per-layer GEMM forward (the training path's forward)."""
+        _check(self.lib.souffle_mlp_forward_layered(self.h, C.c_void_p(x_ptr), m, C.c_void_p(y_ptr)))
 
     def gradients(self, x_ptr: int, t_ptr: int, m: int):
         g = np.empty(self.n_params, dtype=np.float32)

@@ -29,6 +29,9 @@ typedef struct souffle_mlp souffle_mlp;
 souffle_status souffle_mlp_create(int32_t n_in, int32_t width, int32_t n_out, int32_t max_batch, uint64_t seed,
                                   int32_t device, souffle_mlp** out);
 souffle_status souffle_mlp_destroy(souffle_mlp* h);
+/* The network's CUDA stream (cudaStream_t), on which its calls run, for callers that order or
+ * time their own work against it. */
+void* souffle_mlp_stream(const souffle_mlp* h);
 
 /* Number of FP32 parameters, flat layout W1 [width][n_in], b1 [width], W2, b2, W3, b3,
  * W4 [n_out][width], b4 [n_out]. */
@@ -36,8 +39,14 @@ int64_t souffle_mlp_param_count(const souffle_mlp* h);
 souffle_status souffle_mlp_get_params(souffle_mlp* h, float* host_out, int64_t n);
 souffle_status souffle_mlp_set_params(souffle_mlp* h, const float* host_in, int64_t n);
 
-/* y_dev [m][n_out] = network(x_dev [m][n_in]); 1 <= m <= max_batch. */
+/* y_dev [m][n_out] = network(x_dev [m][n_in]); 1 <= m <= max_batch.  For n_in <= 64 and
+ * n_out <= 256 the whole forward pass is one tensor-core kernel that keeps each 128-row tile's
+ * activations on chip (SiLU through a hardware tanh approximation); other shapes run layer by
+ * layer. */
 souffle_status souffle_mlp_forward(souffle_mlp* h, const float* x_dev, int32_t m, float* y_dev);
+/* The same forward pass one GEMM per layer, activations through device memory (the path the
+ * training steps use, with SiLU from an exponential and a division). */
+souffle_status souffle_mlp_forward_layered(souffle_mlp* h, const float* x_dev, int32_t m, float* y_dev);
 
 /* Loss and gradient of the loss with respect to every parameter (flat layout above, host array
  * of souffle_mlp_param_count floats) for one batch; parameters unchanged. */

@@ -578,9 +578,10 @@ def surrogate_batched(args):
 def bench_gemm(args):
     """The surrogate network's forward pass (64 -> 256 -> 256 -> 256 -> 132, BF16 operands, FP32
     accumulation) at several row counts through the C ABI: the fused one-kernel forward
-    (souffle_mlp_forward) and the per-layer GEMMs (souffle_mlp_forward_layered), each timed with
-    CUDA events on the network's stream around the call (input packing, the forward, output
-    unpadding), against the measured BF16 tensor peak."""
+    (souffle_mlp_forward) and the per-layer GEMMs (souffle_mlp_forward_layered).  us_per_call:
+    CUDA events on the network's stream around the C call (input packing, the forward, output
+    unpadding, host gaps between them); us_per_forward: the forward kernels alone, back to back
+    (souffle_mlp_profile_forward), the figure against the measured BF16 tensor peak."""
     import torch
     from souffle_gb300 import gpu
     torch.cuda.set_device(0)
@@ -610,7 +611,9 @@ def bench_gemm(args):
                 e1.record(ext)
             torch.cuda.synchronize()
             us = sum(e0.elapsed_time(e1) for e0, e1 in evs) / len(evs) * 1e3
-            row[name] = {"us_per_forward": us, "tflops": flop / (us * 1e-6) / 1e12}
+            # the forward kernels alone, back to back on pre-packed input
+            kus = net.profile_forward(m, args.steps, fused=(name == "fused"))
+            row[name] = {"us_per_call": us, "us_per_forward": kus, "tflops": flop / (kus * 1e-6) / 1e12}
         rows.append(row)
         net.close()
     best = rows[2]["fused"]

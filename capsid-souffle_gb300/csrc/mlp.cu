@@ -514,6 +514,37 @@ souffle_status souffle_mlp_forward_layered(souffle_mlp* h, const float* x_dev, i
   return check_gemm_err(h);
 }
 
+souffle_status souffle_mlp_profile_forward(souffle_mlp* h, int32_t m, int32_t iters, int32_t fused, double* us) {
+  if (!h || !us || m < 1 || m > h->cap || iters < 1) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  const int L = kLayers - 1;
+  if (fused && !mlp_fused_supported(h->n_in, h->width, h->out_pad[L]))
+    return fail(SOUFFLE_ERR_BAD_INPUT, "network shape has no fused forward");
+  MLP_TRY(cudaSetDevice(h->device));
+  cudaEvent_t e0, e1;
+  MLP_TRY(cudaEventCreate(&e0));
+  MLP_TRY(cudaEventCreate(&e1));
+  const __nv_bfloat16* w[4] = {h->wb[0].p, h->wb[1].p, h->wb[2].p, h->wb[3].p};
+  const int ldw[4] = {h->in[0], h->in[1], h->in[2], h->in[3]};
+  const float* b[4] = {h->b[0].p, h->b[1].p, h->b[2].p, h->b[3].p};
+  auto run = [&]() {
+    return fused ? mlp_forward_fused(h->act[0].p, h->in_ld[0], m, nullptr, h->n_in, w, ldw, h->out_pad[L], b, h->y.p,
+                                     h->out_pad[L], h->err.p, 1u, h->stream)
+                 : forward_on(h, m, false, h->stream, nullptr, h->err.p);
+  };
+  cudaError_t r = run();  // warm-up
+  if (r == cudaSuccess) r = cudaEventRecord(e0, h->stream);
+  for (int i = 0; i < iters && r == cudaSuccess; i++) r = run();
+  if (r == cudaSuccess) r = cudaEventRecord(e1, h->stream);
+  if (r == cudaSuccess) r = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  MLP_TRY(r);
+  *us = 1e3 * ms / iters;
+  return check_gemm_err(h);
+}
+
 souffle_status souffle_mlp_gradients(souffle_mlp* h, const float* x_dev, const float* t_dev, int32_t m, float* loss,
                                      float* grad_host) {
   if (!h || !x_dev || !t_dev || !grad_host || m < 1 || m > h->cap) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");

@@ -31,7 +31,7 @@ EXPORTED = [
     "souffle_gpu_md_profile", "souffle_gpu_kinetic_energy_noalloc", "souffle_gpu_autotune",
     # include/souffle_surrogate.h
     "souffle_mlp_create", "souffle_mlp_destroy", "souffle_mlp_stream", "souffle_mlp_param_count", "souffle_mlp_get_params",
-    "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_forward_layered", "souffle_mlp_gradients", "souffle_mlp_train_step",
+    "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_forward_layered", "souffle_mlp_profile_forward", "souffle_mlp_gradients", "souffle_mlp_train_step",
     "souffle_gemm_bf16", "souffle_surrogate_attach", "souffle_surrogate_collect", "souffle_surrogate_fit",
     "souffle_surrogate_enable", "souffle_surrogate_get_stats",
     # include/souffle_analysis.h
@@ -150,6 +150,7 @@ def load() -> C.CDLL:
     lib.souffle_mlp_set_params.argtypes = [vp, fp, C.c_int64]
     lib.souffle_mlp_forward.argtypes = [vp, vp, C.c_int32, vp]
     lib.souffle_mlp_forward_layered.argtypes = [vp, vp, C.c_int32, vp]
+    lib.souffle_mlp_profile_forward.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
     lib.souffle_mlp_gradients.argtypes = [vp, vp, vp, C.c_int32, fp, fp]
     lib.souffle_mlp_train_step.argtypes = [vp, vp, vp, C.c_int32, C.c_float, fp]
     lib.souffle_gemm_bf16.argtypes = [vp, vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int32]
@@ -346,6 +347,12 @@ class Mlp:
     def stream(self) -> int:
         """The network's cudaStream_t as an integer."""
         return int(self.lib.souffle_mlp_stream(self.h) or 0)
+
+    def profile_forward(self, m: int, iters: int, fused: bool = True) -> float:
+        """Mean device microseconds per forward over the rows of the last forward's input."""
+        us = C.c_double()
+        _check(self.lib.souffle_mlp_profile_forward(self.h, m, iters, 1 if fused else 0, C.byref(us)))
+        return us.value
 
     def get_params(self) -> np.ndarray:
         out = np.empty(self.n_params, dtype=np.float32)

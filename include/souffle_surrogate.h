@@ -48,6 +48,12 @@ souffle_status souffle_mlp_forward(souffle_mlp* h, const float* x_dev, int32_t m
  * training steps use, with SiLU from an exponential and a division). */
 souffle_status souffle_mlp_forward_layered(souffle_mlp* h, const float* x_dev, int32_t m, float* y_dev);
 
+/* Benchmark utility: runs the forward pass over the m rows already in the network's input buffer
+ * (the last souffle_mlp_forward call's input) iters times back to back on the network's stream,
+ * fused (1) or layer by layer (0), and reports the mean device time per pass in *us (CUDA
+ * events around the launches; no input packing or output unpadding). */
+souffle_status souffle_mlp_profile_forward(souffle_mlp* h, int32_t m, int32_t iters, int32_t fused, double* us);
+
 /* Loss and gradient of the loss with respect to every parameter (flat layout above, host array
  * of souffle_mlp_param_count floats) for one batch; parameters unchanged. */
 souffle_status souffle_mlp_gradients(souffle_mlp* h, const float* x_dev, const float* t_dev, int32_t m,

@@ -391,6 +391,39 @@ def bench_surrogate_batched(args):
     print(json.dumps(surrogate_batched(args)))
 
 
+def _series_stats(temps, pots, ext, t_every, e_every, n_beads):
+    """Mean and standard error (8 block means) of temperature and potential energy over the last
+    three quarters of a run, and the extended energy's drift per bead per 10^4 steps (linear
+    fit over the whole run)."""
+    import numpy as np
+
+    def mean_se(x):
+        x = np.asarray(x[len(x) // 4:], dtype=np.float64)
+        blocks = np.array_split(x, 8)
+        bm = np.array([b.mean() for b in blocks if len(b)])
+        return float(x.mean()), float(bm.std(ddof=1) / np.sqrt(len(bm))) if len(bm) > 1 else 0.0
+
+    tm, tse = mean_se(temps)
+    pm, pse = mean_se(pots)
+    steps = e_every * (np.arange(len(ext)) + 1)
+    drift = float(np.polyfit(steps, np.asarray(ext) / n_beads, 1)[0] * 1e4) if len(ext) > 1 else None
+    return {"T_mean": tm, "T_se": tse, "potential_mean": pm, "potential_se": pse,
+            "drift_per_bead_per_1e4_steps": drift, "samples": len(temps)}
+
+
+def _compare_stats(a, b):
+    """Differences between two runs' statistics in units of their combined standard error."""
+    import math
+    out = {}
+    for key in a:
+        x, y = a[key], b[key]
+        zt = (y["T_mean"] - x["T_mean"]) / max(math.hypot(x["T_se"], y["T_se"]), 1e-30)
+        zp = (y["potential_mean"] - x["potential_mean"]) / max(math.hypot(x["potential_se"], y["potential_se"]), 1e-30)
+        out[key] = {"T_z": zt, "potential_z": zp}
+    out["within_2se"] = all(abs(v["T_z"]) <= 2 and abs(v["potential_z"]) <= 2 for k, v in out.items())
+    return out
+
+
 def surrogate_batched(args):
     """Surrogate + batching against the plain GPU path on the replica sweep: 256 independent
     systems of 20-500 bilayer capsomeres with per-system attraction, screening length (0.5-2
@@ -402,8 +435,12 @@ def surrogate_batched(args):
       surrogate all replicas in one handle, far subunit pairs from the network.
     Batched windows run whole rebuild windows as CUDA graphs; their working set is larger than
     L2.  Also reported: total-force RMS error of the surrogate batch against exact forces at the
-    same state, and temperature and potential-energy statistics of the systems with the longest
-    screening lengths, exact against surrogate."""
+    same state, and, for the four systems with the longest screening lengths run in a handle of
+    their own with the same network, temperature, potential energy and extended-energy drift
+    over stat_steps steps, exact against surrogate from the same configuration with independent
+    velocity draws, with standard errors.  (Systems near the
+    short end of the screening range can blow up after ~10^3 steps with the reference's
+    pair-list rule at -L 0.3: its centre prefilter misses contacts between 42-bead patches.)"""
     import numpy as np
     import torch
     from souffle_gb300 import gpu, workloads
@@ -484,29 +521,48 @@ def surrogate_batched(args):
         e1.record(ext)
         s.synchronize()
         ms = e0.elapsed_time(e1)
-        a1 = a0 + k
-        temps = {i: [] for i in watch}
-        pots = {i: [] for i in watch}
-        if args.stat_steps <= 0:  # throughput only
-            st = gpu.surrogate_stats(s) if enabled else None
-            return {"value": n * k / (ms / 1e3), "ms_per_step": ms / k, "T_mean": None, "potential_mean": None,
-                    "potential_std": None,
-                    "judge": {"judged": st["judged"], "classes_off": st["classes_off"],
-                              "last_error": st["last_error"]} if st else None}
-        for q in range(args.stat_steps // 20):
-            s.md_steps(a1, 20)
-            a1 += 20
-            for i in watch:
-                ke, _, _ = s.md_scalars(i)
-                temps[i].append(2 * ke / (3 * reps[i].n_beads))
-                if q % 5 == 0:
-                    e = s.energies(i)
-                    pots[i].append(e["stretching"] + e["bending"] + e["lj"] + e["electrostatic"])
         st = gpu.surrogate_stats(s) if enabled else None
         return {"value": n * k / (ms / 1e3), "ms_per_step": ms / k,
-                "T_mean": {str(i): float(np.mean(temps[i])) for i in watch},
-                "potential_mean": {str(i): float(np.mean(pots[i])) for i in watch},
-                "potential_std": {str(i): float(np.std(pots[i])) for i in watch},
+                "judge": {"judged": st["judged"], "classes_off": st["classes_off"],
+                          "last_error": st["last_error"]} if st else None}
+
+    def run_stats(enabled, vseed):
+        """The watched systems alone in one handle with the same trained network: stat_steps
+        steps from the post-training configuration with Maxwell-Boltzmann velocities drawn from
+        vseed (independent draws for the exact and the surrogate run, so that the two
+        trajectories are independent samples), temperature every 20 steps, potential and
+        extended energy every 40; the first quarter is left out of the means."""
+        sw = gpu.GpuSystem(tpl, [params[i] for i in watch])
+        gpu.surrogate_attach(sw, net, tpl.pos, far_capacity=max(4096, args.far_per_subunit *
+                                                                 sum(int(reps[i].opt.S) for i in watch)))
+        gpu.surrogate_enable(sw, enabled)
+        rng = np.random.default_rng(vseed)
+        vels = []
+        for i in watch:
+            m = np.tile(np.asarray(tpl.mass, dtype=np.float64), int(reps[i].opt.S))
+            v = rng.normal(size=(reps[i].n_beads, 3)) * np.sqrt(reps[i].derived.T_reduced / m)[:, None]
+            vels.append(v - v.mean(axis=0))
+        sw.set_state(np.concatenate([pos[offs[i]:offs[i + 1]] for i in watch]), np.concatenate(vels))
+        sw.md_begin()
+        temps = {i: [] for i in watch}
+        pots = {i: [] for i in watch}
+        e_ext = {i: [] for i in watch}
+        a1 = 0
+        for q in range(args.stat_steps // 20):
+            sw.md_steps(a1, 20)
+            a1 += 20
+            for j, i in enumerate(watch):
+                ke, _, _ = sw.md_scalars(j)
+                temps[i].append(2 * ke / (3 * reps[i].n_beads))
+                if q % 2 == 1:
+                    e = sw.energies(j)
+                    pot = e["stretching"] + e["bending"] + e["lj"] + e["electrostatic"]
+                    pots[i].append(pot)
+                    e_ext[i].append(pot + e["kinetic"] + e["thermo_pe"] + e["thermo_ke"])
+        st = gpu.surrogate_stats(sw) if enabled else None
+        sw.close()
+        return {"statistics": {str(i): _series_stats(temps[i], pots[i], e_ext[i], 20, 40, reps[i].n_beads)
+                               for i in watch},
                 "judge": {"judged": st["judged"], "classes_off": st["classes_off"],
                           "last_error": st["last_error"]} if st else None}
 
@@ -519,6 +575,8 @@ def surrogate_batched(args):
     batched = run_batch(False)
     surr = run_batch(True)
     s.close()
+    stats_exact = run_stats(False, 101) if args.stat_steps > 0 else None
+    stats_surr = run_stats(True, 202) if args.stat_steps > 0 else None
     net.close()
 
     # the plain GPU path: each replica alone, exact
@@ -565,6 +623,10 @@ def surrogate_batched(args):
         "plain": {"value": plain_value, "replicas_timed": len(sample), "beads_timed": plain_beads,
                   "ms_total": plain_ms},
         "batched": batched, "surrogate": surr,
+        "statistics": ({"steps": args.stat_steps, "exact": stats_exact["statistics"],
+                        "surrogate": stats_surr["statistics"], "surrogate_judge": stats_surr["judge"],
+                        "comparison": _compare_stats(stats_exact["statistics"], stats_surr["statistics"])}
+                       if stats_exact else None),
         "force_rms_rel_error": rms, "force_rms_rel_error_worst_system": max(per_sys),
         "far_pairs": far_pairs, "far_capacity": far_cap,
         "watched_systems": {str(i): {"subunits": sizes[i], "debye_length": lam[i],
@@ -1071,7 +1133,7 @@ def main():
         s.close()
         try:
             sb = surrogate_batched(argparse.Namespace(
-                replicas=256, far_per_subunit=16, steps=100, stat_steps=400, plain_sample=64, profile=False,
+                replicas=256, far_per_subunit=16, steps=100, stat_steps=2000, plain_sample=64, profile=False,
                 train_rows=args.train_rows, max_frames=args.max_frames, epochs=args.epochs))
             out["surrogate_batched"] = {k: sb[k] for k in (
                 "metric", "value", "unit", "gain", "gain_batching", "gain_surrogate", "config",
@@ -1079,10 +1141,7 @@ def main():
             out["surrogate_batched"]["plain_value"] = sb["plain"]["value"]
             out["surrogate_batched"]["batched_value"] = sb["batched"]["value"]
             out["surrogate_batched"]["judge"] = sb["surrogate"]["judge"]
-            out["surrogate_batched"]["statistics"] = {
-                "T_mean": {"exact": sb["batched"]["T_mean"], "surrogate": sb["surrogate"]["T_mean"]},
-                "potential_mean": {"exact": sb["batched"]["potential_mean"],
-                                   "surrogate": sb["surrogate"]["potential_mean"]}}
+            out["surrogate_batched"]["statistics"] = sb["statistics"]
         except Exception as ex:  # the main line stands on its own
             out["surrogate_batched"] = {"error": f"{type(ex).__name__}: {ex}"}
     if rank == 0:

@@ -30,6 +30,13 @@ struct GemmEpi {
   unsigned int err_bit = 1u;      // set in *err when a bounded wait ran out
 };
 
+// Device pointers to a network's normalisation of its training data (held by the network, so a
+// trained network brings it to every handle it is attached to); *has is set once trained.
+struct MlpNorm {
+  float *x_mean, *x_istd, *t_mean, *t_std, *t_istd;
+  bool* has;
+};
+
 // Launches on the stream; A/B base addresses 16-byte aligned, lda/ldb multiples of 8 elements.
 cudaError_t gemm_bf16(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, const GemmEpi& e,
                       cudaStream_t stream);

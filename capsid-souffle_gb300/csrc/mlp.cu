@@ -180,6 +180,11 @@ struct souffle_mlp {
   DevBuf<float> y, partial, loss;
   DevBuf<unsigned int> err;
   long long steps = 0;
+  // the normalisation of the data the surrogate was trained on: per input feature mean and
+  // 1/spread, per output mean, spread and 1/spread (set by souffle_surrogate_fit; travels with
+  // the network to any handle it is attached to)
+  DevBuf<float> x_mean, x_istd, t_mean, t_std, t_istd;
+  bool has_norm = false;
 };
 
 namespace {
@@ -349,6 +354,10 @@ cudaError_t mlp_forward_packed_async(souffle_mlp* h, int m_cap, const int* m_dyn
   return r;
 }
 
+MlpNorm mlp_norm(souffle_mlp* h) {
+  return MlpNorm{h->x_mean.p, h->x_istd.p, h->t_mean.p, h->t_std.p, h->t_istd.p, &h->has_norm};
+}
+
 void mlp_dims(const souffle_mlp* h, int* n_in, int* n_out, int* cap) {
   *n_in = h->n_in;
   *n_out = h->n_out;
@@ -426,6 +435,8 @@ souffle_status souffle_mlp_create(int32_t n_in, int32_t width, int32_t n_out, in
     MLP_TRY_C(cudaMemset(h->dz_t[l].p, 0, (size_t)cols * h->cap * 2));
   }
   MLP_TRY_C(h->y.alloc((size_t)h->cap * h->out_pad[kLayers - 1]));
+  for (auto* b : {&h->x_mean, &h->x_istd}) MLP_TRY_C(b->alloc(n_in));
+  for (auto* b : {&h->t_mean, &h->t_std, &h->t_istd}) MLP_TRY_C(b->alloc(n_out));
   MLP_TRY_C(h->partial.alloc(blocks((long long)h->cap * h->out_pad[kLayers - 1], 256)));
   MLP_TRY_C(h->loss.alloc(1));
   MLP_TRY_C(h->err.alloc(1));

@@ -11,9 +11,11 @@
 //               network forward  tcgen05 GEMMs (mlp.cu), rows beyond the far-pair count skipped
 //               k_far_apply      forces on each subunit's beads from its far pairs, summed in
 //                                pair order (warp per subunit), for k_forces to add
-// Judge:        k_far_judge      exact re-evaluation of one far pair in judge_stride against the
+// Judge:        k_force_norms    per system: sum of |F|^2 over its beads (the last step's total forces)
+//               k_far_judge      exact re-evaluation of one far pair in judge_stride against the
 //                                network's output, per distance class
-//               k_judge_decide   relative RMS error per class; classes above the tolerance
+//               k_judge_decide   per class, the worst system's estimated share of the total-force
+//                                RMS relative error; classes above the tolerance
 //                                revert to exact at the next rebuild
 // Training:     k_far_targets    exact forces of far pairs as (F, tau, residuals) in A's frame
 //               souffle_surrogate_fit normalises the data set and trains with mlp.cu's kernels.
@@ -29,6 +31,7 @@
 #include <vector>
 
 #include "devbuf.cuh"
+#include "gemm.cuh"
 #include "kernels.cuh"
 #include "souffle_surrogate.h"
 #include "surrogate.cuh"
@@ -42,6 +45,7 @@ cudaError_t mlp_forward_packed_async(souffle_mlp* h, int m_cap, const int* m_dyn
                                      const float** y, int* ldy);
 __nv_bfloat16* mlp_input_bf16(souffle_mlp* h, int* ld);
 void mlp_dims(const souffle_mlp* h, int* n_in, int* n_out, int* cap);
+MlpNorm mlp_norm(souffle_mlp* h);
 }  // namespace souffle
 
 namespace souffle {
@@ -88,8 +92,13 @@ struct FarArgs {
   // judge
   int judge_stride;
   float judge_tol;
+  int n_sys;
+  const long long* force;  // [3][N] total forces, 2^-32 fixed point
+  long long n_beads;
+  const int* bead_sys;
+  double* judge_fn2;     // [n_sys] sum of |F|^2 over the system's beads
   int* judge_counter;
-  double* judge_acc;     // [kClasses][2]
+  double* judge_acc;     // [kClasses][n_sys] sum of |network - exact|^2 over judged pairs
   int* judge_n;          // [kClasses]
   int* class_off_w;      // [kClasses] written by the decision
   float* judge_err;      // [kClasses]
@@ -601,6 +610,37 @@ __global__ void __launch_bounds__(128) k_far_targets(FarArgs a) {
 }
 
 // ---- judge ---------------------------------------------------------------------------------
+// The judge estimates what each distance class of far pairs adds to a system's total-force RMS
+// relative error, sqrt(sum over beads |F_net - F_exact|^2 / sum over beads |F|^2): the squared
+// force errors of the judged pairs (one in judge_stride), scaled by judge_stride, over the sum of
+// |F|^2 of the system's beads (the last step's total forces).  Pairs are treated as independent
+// contributions.  A class whose estimate exceeds judge_tolerance / 2 in any system reverts, so
+// the four classes together stay within judge_tolerance.
+
+// sum of |F|^2 per system: each thread a contiguous run of beads, one atomic per run of beads
+// of one system
+__global__ void k_force_norms(FarArgs a) {
+  constexpr int kRun = 64;
+  const long long b0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kRun;
+  if (b0 >= a.n_beads) return;
+  const long long b1 = min(a.n_beads, b0 + kRun);
+  const double u = 2.3283064365386963e-10;  // 2^-32
+  int sys = a.bead_sys[b0];
+  double acc = 0.0;
+  for (long long b = b0; b < b1; b++) {
+    const int sb = a.bead_sys[b];
+    if (sb != sys) {
+      atomicAdd(&a.judge_fn2[sys], acc);
+      acc = 0.0;
+      sys = sb;
+    }
+    const double fx = (double)a.force[b] * u, fy = (double)a.force[a.n_beads + b] * u,
+                 fz = (double)a.force[2 * a.n_beads + b] * u;
+    acc += fx * fx + fy * fy + fz * fz;
+  }
+  atomicAdd(&a.judge_fn2[sys], acc);
+}
+
 __global__ void __launch_bounds__(128) k_far_judge(FarArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * 4 + warp;
@@ -613,19 +653,16 @@ __global__ void __launch_bounds__(128) k_far_judge(FarArgs a) {
   body_coords(a, ab.x, F, lane, e, p);
   exact_body_forces(a, ab.x, ab.y, F, p, lane, gx);
   net_body_forces(a, a.y + (size_t)q * a.ldy, F, e, lane, gn);
-  float num = 0.f, den = 0.f;
+  float num = 0.f;
 #pragma unroll
   for (int b = 0; b < kBeadsPerLane; b++) {
     const float3 dd = sub3(gn[b], gx[b]);
     num += dot3_(dd, dd);
-    den += dot3_(gx[b], gx[b]);
   }
   num = wsum(num);
-  den = wsum(den);
   if (lane == 0) {
     const int c = dist_class(a.far_dmin[q], a.r_switch);
-    atomicAdd(&a.judge_acc[2 * c], (double)num);
-    atomicAdd(&a.judge_acc[2 * c + 1], (double)den);
+    atomicAdd(&a.judge_acc[(size_t)c * a.n_sys + a.sub_sys[ab.x]], (double)num);
     atomicAdd(&a.judge_n[c], 1);
   }
 }
@@ -633,17 +670,23 @@ __global__ void __launch_bounds__(128) k_far_judge(FarArgs a) {
 __global__ void k_judge_decide(FarArgs a) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   long long n = 0;
+  const double tol_class = 0.5 * (double)a.judge_tol;  // four classes in quadrature
   for (int c = 0; c < kClasses; c++) {
     const int nc = a.judge_n[c];
     n += nc;
-    if (nc > 0 && a.judge_acc[2 * c + 1] > 0.0) {
-      const double e = sqrt(a.judge_acc[2 * c] / a.judge_acc[2 * c + 1]);
-      a.judge_err[c] = (float)e;
-      if (!(e <= (double)a.judge_tol)) a.class_off_w[c] = 1;
+    double worst = -1.0;
+    for (int k = 0; k < a.n_sys; k++) {
+      double* acc = &a.judge_acc[(size_t)c * a.n_sys + k];
+      if (nc > 0 && a.judge_fn2[k] > 0.0) worst = fmax(worst, sqrt((double)a.judge_stride * *acc / a.judge_fn2[k]));
+      *acc = 0.0;
     }
-    a.judge_acc[2 * c] = a.judge_acc[2 * c + 1] = 0.0;
+    if (nc > 0) {
+      a.judge_err[c] = (float)worst;
+      if (!(worst <= tol_class)) a.class_off_w[c] = 1;
+    }
     a.judge_n[c] = 0;
   }
+  for (int k = 0; k < a.n_sys; k++) a.judge_fn2[k] = 0.0;
   *a.judged += n;
   *a.judge_counter += 1;
 }
@@ -697,14 +740,15 @@ struct SurrogateCtx {
   souffle_surrogate_options opt{};
   int np = 0, n_out = 0, far_cap = 0;
   int anchor1 = 0, anchor2 = 0;
-  bool enabled = false, have_norm = false;
-  DevBuf<float> modes, rest, x_mean, x_istd, t_mean, t_std, t_istd;
+  bool enabled = false;
+  MlpNorm norm{};  // the attached network's normalisation buffers
+  DevBuf<float> modes, rest;
   DevBuf<unsigned char> cand_far;
   DevBuf<float> cand_dmin, far_dmin, frame, x;
   DevBuf<int> far_count, far_start, far_total, class_off, judge_n, judge_counter;
   DevBuf<int2> far_pair;
   DevBuf<float4> sf;
-  DevBuf<double> judge_acc;
+  DevBuf<double> judge_acc, judge_fn2;
   DevBuf<float> judge_err;
   DevBuf<long long> judged;
   const float* y = nullptr;  // network output (inside the network's buffers) of the last forward
@@ -756,12 +800,12 @@ FarArgs far_args(souffle_gpu_system* h) {
   a.anchor1 = c.anchor1;
   a.anchor2 = c.anchor2;
   a.x = c.x.p;
-  a.x_mean = c.x_mean.p;
-  a.x_istd = c.x_istd.p;
+  a.x_mean = c.norm.x_mean;
+  a.x_istd = c.norm.x_istd;
   a.y = c.y;
   a.ldy = c.ldy;
-  a.t_mean = c.t_mean.p;
-  a.t_std = c.t_std.p;
+  a.t_mean = c.norm.t_mean;
+  a.t_std = c.norm.t_std;
   a.sf = c.sf.p;
   a.dh_w = h->dh_w.p;
   a.species = h->tpl_i.p + h->L.o_species;
@@ -769,6 +813,11 @@ FarArgs far_args(souffle_gpu_system* h) {
   a.L = h->L;
   a.judge_stride = c.opt.judge_stride;
   a.judge_tol = (float)c.opt.judge_tolerance;
+  a.n_sys = h->n_sys;
+  a.force = h->force.p;
+  a.n_beads = h->N;
+  a.bead_sys = h->d_bead_sys.p;
+  a.judge_fn2 = c.judge_fn2.p;
   a.judge_counter = c.judge_counter.p;
   a.judge_acc = c.judge_acc.p;
   a.judge_n = c.judge_n.p;
@@ -876,6 +925,7 @@ void surrogate_judge(souffle_gpu_system* h) {
   SurrogateCtx& c = *h->sur;
   FarArgs a = far_args(h);
   const int nj = (c.far_cap + c.opt.judge_stride - 1) / c.opt.judge_stride;
+  k_force_norms<<<(int)((h->N + 64 * 128 - 1) / (64 * 128)), 128, 0, h->stream>>>(a);
   k_far_judge<<<(nj + 3) / 4, 128, 0, h->stream>>>(a);
   k_judge_decide<<<1, 32, 0, h->stream>>>(a);
 }
@@ -897,7 +947,7 @@ souffle_status souffle_surrogate_attach(souffle_gpu_system* h, souffle_mlp* net,
   if (o.switch_radius <= 0) o.switch_radius = 3.5;
   if (o.judge_every <= 0) o.judge_every = 100;
   if (o.judge_stride <= 0) o.judge_stride = 100;
-  if (o.judge_tolerance <= 0) o.judge_tolerance = 0.2;
+  if (o.judge_tolerance <= 0) o.judge_tolerance = 1e-3;
   if (o.far_capacity <= 0) o.far_capacity = std::max(1024, 2 * h->S);
   if (cap < o.far_capacity) return sfail(SOUFFLE_ERR_BAD_INPUT, "network max_batch is below far_capacity");
   // body frame of the rest shape: centre bead, the bead farthest from it, the bead farthest
@@ -1044,8 +1094,7 @@ souffle_status souffle_surrogate_attach(souffle_gpu_system* h, souffle_mlp* net,
   S_TRY_C(cudaMemcpy(c->modes.p, modes.data(), modes.size() * 4, cudaMemcpyHostToDevice));
   S_TRY_C(c->rest.alloc(restf.size()));
   S_TRY_C(cudaMemcpy(c->rest.p, restf.data(), restf.size() * 4, cudaMemcpyHostToDevice));
-  for (auto* b : {&c->x_mean, &c->x_istd}) S_TRY_C(b->alloc(kDesc));
-  for (auto* b : {&c->t_mean, &c->t_std, &c->t_istd}) S_TRY_C(b->alloc(n_out));
+  c->norm = mlp_norm(net);
   S_TRY_C(c->cand_far.alloc((size_t)h->S * h->cand_cap));
   S_TRY_C(c->cand_dmin.alloc((size_t)h->S * h->cand_cap));
   S_TRY_C(c->far_count.alloc(h->S));
@@ -1065,8 +1114,10 @@ souffle_status souffle_surrogate_attach(souffle_gpu_system* h, souffle_mlp* net,
   S_TRY_C(cudaMemset(c->judge_n.p, 0, kClasses * sizeof(int)));
   S_TRY_C(c->judge_counter.alloc(1));
   S_TRY_C(cudaMemset(c->judge_counter.p, 0, sizeof(int)));
-  S_TRY_C(c->judge_acc.alloc(2 * kClasses));
-  S_TRY_C(cudaMemset(c->judge_acc.p, 0, 2 * kClasses * sizeof(double)));
+  S_TRY_C(c->judge_acc.alloc((size_t)kClasses * h->n_sys));
+  S_TRY_C(cudaMemset(c->judge_acc.p, 0, (size_t)kClasses * h->n_sys * sizeof(double)));
+  S_TRY_C(c->judge_fn2.alloc(h->n_sys));
+  S_TRY_C(cudaMemset(c->judge_fn2.p, 0, h->n_sys * sizeof(double)));
   S_TRY_C(c->judge_err.alloc(kClasses));
   {
     const float neg[kClasses] = {-1.f, -1.f, -1.f, -1.f};
@@ -1140,16 +1191,16 @@ souffle_status souffle_surrogate_fit(souffle_gpu_system* h, const float* x_dev, 
   if (batch > cap) return sfail(SOUFFLE_ERR_BAD_INPUT, "batch exceeds the network's max_batch");
   S_TRY(cudaSetDevice(h->opt.device));
   cudaStream_t st = h->stream;
-  k_col_stats<<<kDesc, 256, 0, st>>>(x_dev, n, kDesc, c.x_mean.p, c.x_istd.p, nullptr);
-  k_col_stats<<<n_out, 256, 0, st>>>(t_dev, n, n_out, c.t_mean.p, c.t_istd.p, c.t_std.p);
+  k_col_stats<<<kDesc, 256, 0, st>>>(x_dev, n, kDesc, c.norm.x_mean, c.norm.x_istd, nullptr);
+  k_col_stats<<<n_out, 256, 0, st>>>(t_dev, n, n_out, c.norm.t_mean, c.norm.t_istd, c.norm.t_std);
   S_TRY(cudaGetLastError());
   // targets are scaled by 1/std (constant columns kept at scale 1)
   {
     std::vector<float> sd(n_out), is(n_out);
-    S_TRY(cudaMemcpyAsync(sd.data(), c.t_std.p, n_out * 4, cudaMemcpyDeviceToHost, st));
+    S_TRY(cudaMemcpyAsync(sd.data(), c.norm.t_std, n_out * 4, cudaMemcpyDeviceToHost, st));
     S_TRY(cudaStreamSynchronize(st));
     for (int k = 0; k < n_out; k++) is[k] = 1.0f / sd[k];
-    S_TRY(cudaMemcpy(c.t_istd.p, is.data(), n_out * 4, cudaMemcpyHostToDevice));
+    S_TRY(cudaMemcpy(c.norm.t_istd, is.data(), n_out * 4, cudaMemcpyHostToDevice));
   }
   std::vector<int> perm(n);
   std::iota(perm.begin(), perm.end(), 0);
@@ -1161,10 +1212,10 @@ souffle_status souffle_surrogate_fit(souffle_gpu_system* h, const float* x_dev, 
   S_TRY(xn.alloc((size_t)n * kDesc));
   S_TRY(tn.alloc((size_t)n * n_out));
   S_TRY(cudaMemcpy(dperm.p, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-  k_normalise_rows<<<(int)(((long long)n * kDesc + 255) / 256), 256, 0, st>>>(x_dev, dperm.p, n, kDesc, c.x_mean.p,
-                                                                              c.x_istd.p, xn.p);
-  k_normalise_rows<<<(int)(((long long)n * n_out + 255) / 256), 256, 0, st>>>(t_dev, dperm.p, n, n_out, c.t_mean.p,
-                                                                              c.t_istd.p, tn.p);
+  k_normalise_rows<<<(int)(((long long)n * kDesc + 255) / 256), 256, 0, st>>>(x_dev, dperm.p, n, kDesc, c.norm.x_mean,
+                                                                              c.norm.x_istd, xn.p);
+  k_normalise_rows<<<(int)(((long long)n * n_out + 255) / 256), 256, 0, st>>>(t_dev, dperm.p, n, n_out, c.norm.t_mean,
+                                                                              c.norm.t_istd, tn.p);
   S_TRY(cudaGetLastError());
   S_TRY(cudaStreamSynchronize(st));
   const int nb = (n + batch - 1) / batch;
@@ -1183,14 +1234,14 @@ souffle_status souffle_surrogate_fit(souffle_gpu_system* h, const float* x_dev, 
     }
     last = sum / n;
   }
-  c.have_norm = true;
+  *c.norm.has = true;
   if (final_loss) *final_loss = (float)last;
   return SOUFFLE_OK;
 }
 
 souffle_status souffle_surrogate_enable(souffle_gpu_system* h, int32_t on) {
   if (!h || !h->sur) return sfail(SOUFFLE_ERR_BAD_INPUT, "no surrogate attached");
-  if (on && !h->sur->have_norm) return sfail(SOUFFLE_ERR_STATE, "the surrogate has not been trained");
+  if (on && !*h->sur->norm.has) return sfail(SOUFFLE_ERR_STATE, "the surrogate has not been trained");
   if ((bool)on != h->sur->enabled) {
     h->sur->enabled = on != 0;
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.second);

@@ -390,7 +390,7 @@ def gemm_bf16(a_ptr: int, b_ptr: int, m: int, n: int, k: int, c_ptr: int, device
 
 def surrogate_attach(system: "GpuSystem", net: Mlp, rest_pos: np.ndarray, switch_radius: float = 3.5,
                      far_capacity: int = 0, judge_every: int = 100, judge_stride: int = 100,
-                     judge_tolerance: float = 0.2) -> None:
+                     judge_tolerance: float = 1e-3) -> None:
     """Attach a trained-or-not network to a system (include/souffle_surrogate.h)."""
     rp = np.ascontiguousarray(rest_pos, dtype=np.float64).reshape(-1)
     o = SurrogateOptions_(switch_radius, far_capacity, judge_every, judge_stride, judge_tolerance)

@@ -81,14 +81,17 @@ souffle_status souffle_mlp_train_step(souffle_mlp* h, const float* x_dev, const 
  *
  * Judge: every judge_every steps one far pair in judge_stride is re-evaluated exactly; pairs are
  * binned in four classes by closest distance (switch_radius + [0, 0.5), [0.5, 1), [1, 1.5),
- * [1.5, inf)); a class whose relative RMS force error exceeds judge_tolerance reverts to exact
- * from the next rebuild on. */
+ * [1.5, inf)).  For each class and system the judge estimates the class's share of the
+ * system's total-force RMS relative error, sqrt(judge_stride x sum over judged pairs of
+ * |network - exact|^2 / sum over the system's beads of |F|^2), pairs taken as independent; a
+ * class whose estimate exceeds judge_tolerance / 2 in any system reverts to exact from the next
+ * rebuild on, so the four classes together stay within judge_tolerance. */
 typedef struct souffle_surrogate_options {
   double switch_radius;    /* default 3.5 */
   int32_t far_capacity;    /* most far pairs (0 = max(1024, 2 x subunits)); beyond it all stay exact */
   int32_t judge_every;     /* default 100 */
   int32_t judge_stride;    /* default 100 (1 % of the far pairs) */
-  double judge_tolerance;  /* default 0.2 */
+  double judge_tolerance;  /* bound on a system's total-force RMS relative error from the network, default 1e-3 */
 } souffle_surrogate_options;
 
 typedef struct souffle_surrogate_stats {
@@ -97,11 +100,14 @@ typedef struct souffle_surrogate_stats {
   int32_t far_found;       /* far pairs found at the last rebuild (> far_pairs on overflow) */
   int32_t classes_off;     /* bit c set: class c reverted to exact */
   int64_t judged;          /* pairs re-evaluated so far */
-  double last_error[4];    /* per class: relative RMS error at the last judgement, -1 = none */
+  double last_error[4];    /* per class: the estimated share of the total-force RMS relative error at
+                              the last judgement (worst system), -1 = none */
 } souffle_surrogate_stats;
 
 /* Attach a network (n_in 64, n_out 6 + 3 np, max_batch >= far_capacity) to a handle whose
- * template rest shape is rest_pos [np][3]. */
+ * template rest shape is rest_pos [np][3].  A network trained by souffle_surrogate_fit keeps the
+ * normalisation of its training data, so it can be attached to other handles of the same
+ * template and switched on there without training again. */
 souffle_status souffle_surrogate_attach(souffle_gpu_system* h, souffle_mlp* net, const double* rest_pos,
                                         const souffle_surrogate_options* opt);
 /* Training data at the current state (surrogate switched off): classifies the far pairs and

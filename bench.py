@@ -101,6 +101,19 @@ def _profile_traffic():
     return None
 
 
+def _profile_instructions():
+    """Warp instructions issued per k_forces launch (smsp__inst_executed.sum) from the committed
+    ncu summary, if present."""
+    try:
+        for line in open(PROFILE_SUMMARY):
+            if line.startswith("smsp__inst_executed.sum"):
+                v, unit = line.split()[1:3]
+                return float(v) * {"M": 1e6, "K": 1e3, "G": 1e9}.get(unit, 1.0)
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
 def rank_aggregate(total_ms: float, beads_per_rank: int, steps: int, world: int, dist=None):
     """Whole-job figures of a weak-scaling run (every rank an independent replica of the
     workload): the slowest rank's timed region (max over ranks, ms) and the total bead-steps/s
@@ -419,8 +432,11 @@ def _compare_stats(a, b):
         x, y = a[key], b[key]
         zt = (y["T_mean"] - x["T_mean"]) / max(math.hypot(x["T_se"], y["T_se"]), 1e-30)
         zp = (y["potential_mean"] - x["potential_mean"]) / max(math.hypot(x["potential_se"], y["potential_se"]), 1e-30)
-        out[key] = {"T_z": zt, "potential_z": zp}
-    out["within_2se"] = all(abs(v["T_z"]) <= 2 and abs(v["potential_z"]) <= 2 for k, v in out.items())
+        zd = (y["drift_per_bead_per_1e4_steps"] - x["drift_per_bead_per_1e4_steps"]) / max(
+            math.hypot(x.get("drift_se", 0.0), y.get("drift_se", 0.0)), 1e-30)
+        out[key] = {"T_z": zt, "potential_z": zp, "drift_z": zd}
+    out["within_2se"] = all(abs(v["T_z"]) <= 2 and abs(v["potential_z"]) <= 2 and abs(v["drift_z"]) <= 2
+                            for k, v in out.items())
     return out
 
 
@@ -435,10 +451,10 @@ def surrogate_batched(args):
       surrogate all replicas in one handle, far subunit pairs from the network.
     Batched windows run whole rebuild windows as CUDA graphs; their working set is larger than
     L2.  Also reported: total-force RMS error of the surrogate batch against exact forces at the
-    same state, and, for the four systems with the longest screening lengths run in a handle of
-    their own with the same network, temperature, potential energy and extended-energy drift
-    over stat_steps steps, exact against surrogate from the same configuration with independent
-    velocity draws, with standard errors.  (Systems near the
+    same state, and, for the four systems with the longest screening lengths in a handle of their
+    own with the same network, temperature, potential energy and extended-energy drift over
+    stat_steps steps, exact against surrogate, each from six independent velocity draws, with
+    standard errors from the run-to-run spread.  (Systems near the
     short end of the screening range can blow up after ~10^3 steps with the reference's
     pair-list rule at -L 0.3: its centre prefilter misses contacts between 42-bead patches.)"""
     import numpy as np
@@ -526,43 +542,56 @@ def surrogate_batched(args):
                 "judge": {"judged": st["judged"], "classes_off": st["classes_off"],
                           "last_error": st["last_error"]} if st else None}
 
-    def run_stats(enabled, vseed):
-        """The watched systems alone in one handle with the same trained network: stat_steps
-        steps from the post-training configuration with Maxwell-Boltzmann velocities drawn from
-        vseed (independent draws for the exact and the surrogate run, so that the two
-        trajectories are independent samples), temperature every 20 steps, potential and
-        extended energy every 40; the first quarter is left out of the means."""
-        sw = gpu.GpuSystem(tpl, [params[i] for i in watch])
+    def run_stats(enabled, seed0, n_seeds=6):
+        """The watched systems in a handle of their own with the same trained network, each run
+        n_seeds times from the post-training configuration with independent Maxwell-Boltzmann
+        velocity draws (seeds seed0 ..; other draws for the exact and the surrogate run):
+        stat_steps steps, temperature every 20 steps, potential and extended energy every 40.
+        Per run the means over the last three quarters; per watched system their mean over the
+        runs with the standard error from the run-to-run spread (the runs are independent
+        trajectories, so slow relaxation of the potential is in the spread)."""
+        sysl = [i for i in watch for _ in range(n_seeds)]
+        sw = gpu.GpuSystem(tpl, [params[i] for i in sysl])
         gpu.surrogate_attach(sw, net, tpl.pos, far_capacity=max(4096, args.far_per_subunit *
-                                                                 sum(int(reps[i].opt.S) for i in watch)))
+                                                                 sum(int(reps[i].opt.S) for i in sysl)))
         gpu.surrogate_enable(sw, enabled)
-        rng = np.random.default_rng(vseed)
+        rng = np.random.default_rng(seed0)
         vels = []
-        for i in watch:
+        for i in sysl:
             m = np.tile(np.asarray(tpl.mass, dtype=np.float64), int(reps[i].opt.S))
             v = rng.normal(size=(reps[i].n_beads, 3)) * np.sqrt(reps[i].derived.T_reduced / m)[:, None]
             vels.append(v - v.mean(axis=0))
-        sw.set_state(np.concatenate([pos[offs[i]:offs[i + 1]] for i in watch]), np.concatenate(vels))
+        sw.set_state(np.concatenate([pos[offs[i]:offs[i + 1]] for i in sysl]), np.concatenate(vels))
         sw.md_begin()
-        temps = {i: [] for i in watch}
-        pots = {i: [] for i in watch}
-        e_ext = {i: [] for i in watch}
+        temps = [[] for _ in sysl]
+        pots = [[] for _ in sysl]
+        e_ext = [[] for _ in sysl]
         a1 = 0
         for q in range(args.stat_steps // 20):
             sw.md_steps(a1, 20)
             a1 += 20
-            for j, i in enumerate(watch):
+            for j, i in enumerate(sysl):
                 ke, _, _ = sw.md_scalars(j)
-                temps[i].append(2 * ke / (3 * reps[i].n_beads))
+                temps[j].append(2 * ke / (3 * reps[i].n_beads))
                 if q % 2 == 1:
                     e = sw.energies(j)
                     pot = e["stretching"] + e["bending"] + e["lj"] + e["electrostatic"]
-                    pots[i].append(pot)
-                    e_ext[i].append(pot + e["kinetic"] + e["thermo_pe"] + e["thermo_ke"])
+                    pots[j].append(pot)
+                    e_ext[j].append(pot + e["kinetic"] + e["thermo_pe"] + e["thermo_ke"])
         st = gpu.surrogate_stats(sw) if enabled else None
         sw.close()
-        return {"statistics": {str(i): _series_stats(temps[i], pots[i], e_ext[i], 20, 40, reps[i].n_beads)
-                               for i in watch},
+        runs = [_series_stats(temps[j], pots[j], e_ext[j], 20, 40, reps[i].n_beads) for j, i in enumerate(sysl)]
+        out = {}
+        for i in watch:
+            rs = [r for r, k in zip(runs, sysl) if k == i]
+            tm = np.array([r["T_mean"] for r in rs])
+            pm = np.array([r["potential_mean"] for r in rs])
+            dr = np.array([r["drift_per_bead_per_1e4_steps"] for r in rs])
+            out[str(i)] = {"T_mean": float(tm.mean()), "T_se": float(tm.std(ddof=1) / np.sqrt(len(tm))),
+                           "potential_mean": float(pm.mean()), "potential_se": float(pm.std(ddof=1) / np.sqrt(len(pm))),
+                           "drift_per_bead_per_1e4_steps": float(dr.mean()),
+                           "drift_se": float(dr.std(ddof=1) / np.sqrt(len(dr))), "runs": len(rs)}
+        return {"statistics": out,
                 "judge": {"judged": st["judged"], "classes_off": st["classes_off"],
                           "last_error": st["last_error"]} if st else None}
 
@@ -700,11 +729,11 @@ def bench_drift(args):
     w = workloads.plain_large(args.subunits, debye_length=args.debye_length, conc_um=args.concentration,
                               nhc_mass=args.nhc_mass)
     p = gpu.system_params(w.opt, w.derived, int(w.opt.S), w.center_local)
-    s = gpu.GpuSystem(w.template, [p])
+    s = gpu.GpuSystem(w.template, [p], chain_fp64=args.chain_fp64)
     s.set_state(w.state.pos, w.state.vel)
     s.md_begin()
     n, np_, L = w.n_beads, w.template.n_beads, float(w.derived.box)
-    every = 500
+    every, t_every = 500, 50
 
     def rg():
         pos, _ = s.get_state()
@@ -714,11 +743,13 @@ def bench_drift(args):
         c = d.mean(axis=1, keepdims=True)
         return float(np.sqrt(((d - c) ** 2).sum(axis=2).mean(axis=1)).mean())
 
-    rows = []
+    rows, temps = [], []
     t0 = time.perf_counter()
     for a in range(0, args.drift_steps + 1, every):
         if a:
-            s.md_steps(a - every + 1, every)
+            for b in range(a - every, a, t_every):
+                s.md_steps(b + 1, t_every)
+                temps.append((b + t_every, 2 * s.md_scalars()[0] / (3 * n)))
         e = s.energies()
         pot = e["stretching"] + e["bending"] + e["lj"] + e["electrostatic"]
         rows.append((a, e["temperature"], pot / n, (pot + e["kinetic"] + e["thermo_pe"] + e["thermo_ke"]) / n, rg()))
@@ -726,13 +757,18 @@ def bench_drift(args):
     r = np.array(rows)
     half = len(r) // 2
     slope = float(np.polyfit(r[:, 0], r[:, 3], 1)[0] * 1e4)
+    tt = np.array([t for step, t in temps if step > args.drift_steps // 2])
+    tb = np.array([b.mean() for b in np.array_split(tt, 8)]) if len(tt) >= 8 else tt
     print(json.dumps({
         "metric": "extended-energy drift per bead per 1e4 steps", "value": slope, "unit": "kT per bead",
         "n_gpus": 1, "steps": args.drift_steps, "higher_is_better": False, "dtype": "f32+i64 fixed / f64",
         "data": "synthetic", "config": {"workload": f"plain_large: {args.subunits} bilayer capsomeres x 42 "
                                                     f"beads = {n} beads, {w.opt.C:g} uM, -e 5 -L 0.3 -B 10 "
                                                     f"-t 0.005 -q 5 -Q {w.opt.Q:g}", "sample_every": every},
-        "T_mean_second_half": float(r[half:, 1].mean()), "T_std_second_half": float(r[half:, 1].std()),
+        "chain": "fp64 (validation variant)" if args.chain_fp64 else "double-float",
+        "T_mean_second_half": float(tt.mean()) if len(tt) else None,
+        "T_std_second_half": float(tt.std()) if len(tt) else None,
+        "T_se_second_half": float(tb.std(ddof=1) / np.sqrt(len(tb))) if len(tb) > 1 else None,
         "potential_per_bead_mean_second_half": float(r[half:, 2].mean()),
         "rg_mean_second_half": float(r[half:, 4].mean()),
         "extended_energy_per_bead_first_last": [float(r[0, 3]), float(r[-1, 3])],
@@ -909,6 +945,8 @@ def main():
     ap.add_argument("--big-beads", type=int, default=0,
                     help="encapsulation: this many big beads (-a 3 -G -78 -H 3.5) in the workload")
     ap.add_argument("--nhc-mass", type=float, default=0.0, help="-Q for --drift-steps (default 10)")
+    ap.add_argument("--chain-fp64", action="store_true",
+                    help="--drift-steps with the thermostat chain in FP64 (validation variant)")
     ap.add_argument("--drift-steps", type=int, default=0,
                     help="long-run statistics: extended-energy drift, T, potential, Rg over this many steps")
     ap.add_argument("--gemm", action="store_true",
@@ -1078,6 +1116,14 @@ def main():
            "note": "set_state from pinned host + md_begin + steps in rebuild windows with the "
                    "thermostat scalars read after each window + get_state, wall clock"}
 
+    # one energy block (souffle_gpu_energies: every pair j > i in FP64, as the reference's
+    # update_LJ_ES_energies_simplified), wall clock around synchronous calls
+    s.energies()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        s.energies()
+    energies_ms = (time.perf_counter() - t0) / 3 * 1e3
+
     # roofline of the dominant kernel (k_forces): its share of the algorithmic bytes per bead
     # step: pos32 tile 16 B + neighbour-index stream 4 n_bar + force write 24 B + velocity
     # read/write 48 B + per-bead constants 16 B
@@ -1093,6 +1139,9 @@ def main():
     # the committed ncu figure is for the default workload only
     default_workload = args.subunits == 2000 and not args.debye_length and not args.concentration
     traffic = _profile_traffic() if default_workload else None
+    inst = _profile_instructions() if default_workload else None
+    clk = _summarize_clocks(samples)
+    sm_ghz = (clk["sm_mhz"] or 2070.0) / 1e3
     out = {
         "metric": "bead-steps/s", "value": value, "unit": "bead-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -1115,10 +1164,19 @@ def main():
                           "peak": 152 * 128 * 2 * 2.07e9 / 1e12, "unit": "TFLOP/s",
                           "frac": 40.0 * n_bar * w.n_beads / (forces_ms / 1e3) / (152 * 128 * 2 * 2.07e9),
                           "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz"},
+        # the bound the kernel actually meets at this size: instruction issue (the working set
+        # stays in L2, so HBM is not the limit); instructions per launch from the ncu summary
+        "roofline_issue": ({"achieved": inst / (forces_ms / 1e3) / 1e9, "peak": 152 * 4 * sm_ghz,
+                            "unit": "G warp instructions/s", "frac": inst / (forces_ms / 1e3) / 1e9 / (152 * 4 * sm_ghz),
+                            "instructions_per_launch": inst,
+                            "source": "ncu smsp__inst_executed.sum (profiles/k_forces_plain_large.txt); peak 152 SMs x "
+                                      "4 schedulers x 1 instruction per cycle at the sampled SM clock"}
+                           if inst else None),
+        "energies_ms": energies_ms,
         "roofline_step": {"achieved": step_bytes * value / w.n_beads / 1e9, "peak": peak,
                           "unit": "GB/s", "frac": step_bytes * value / w.n_beads / 1e9 / peak,
                           "bytes_per_bead_step": step_bytes / w.n_beads},
-        "clocks": _summarize_clocks(samples),
+        "clocks": clk,
     }
     if parity is not None:
         out["force_rms_rel_error"] = parity["force_rms_rel_error"]
@@ -1133,7 +1191,7 @@ def main():
         s.close()
         try:
             sb = surrogate_batched(argparse.Namespace(
-                replicas=256, far_per_subunit=16, steps=100, stat_steps=2000, plain_sample=64, profile=False,
+                replicas=256, far_per_subunit=16, steps=100, stat_steps=3000, plain_sample=64, profile=False,
                 train_rows=args.train_rows, max_frames=args.max_frames, epochs=args.epochs))
             out["surrogate_batched"] = {k: sb[k] for k in (
                 "metric", "value", "unit", "gain", "gain_batching", "gain_surrogate", "config",

@@ -594,8 +594,18 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       }
     }
     __syncwarp();
-    if (a.mode == 1) nhc_forward_warp(S, lane, chain_scratch);
-    if (!nhc_backward_warp(S, lane, chain_scratch + 2 * kMaxChain)) atomicOr(a.err, kErrNonFinite);
+    if (a.chain64) {  // FP64 validation variant, one thread
+      if (lane == 0) {
+        Chain64& c = a.chain64[w.sys];
+        const double ke = (double)s_red[0] * 2.3283064365386963e-10;  // 2^-32
+        if (a.mode == 1) chain64_forward(c, ke, S);
+        if (!chain64_backward(c, ke, S)) atomicOr(a.err, kErrNonFinite);
+      }
+      __syncwarp();
+    } else {
+      if (a.mode == 1) nhc_forward_warp(S, lane, chain_scratch);
+      if (!nhc_backward_warp(S, lane, chain_scratch + 2 * kMaxChain)) atomicOr(a.err, kErrNonFinite);
+    }
   }
   if (wid == vcom_warp && lane == 0) {
     const long long x = s_red[1], y = s_red[2], z = s_red[3];

@@ -69,6 +69,7 @@ struct ForceArgs {
   const long long* fdrag = nullptr;  // Brownian: [3][N] drag and random force of the step
   const long long* fran = nullptr;
   const int4* bb_pos32 = nullptr;  // encapsulation big beads: high words of their positions
+  Chain64* chain64 = nullptr;      // [n_sys] the chain in FP64 (souffle_options.chain_fp64), or null
   const int* inter_count;
   int inter_cap;
   const float* dh_w;         // [n_sys * np] q * exp(kappa sigma/2)/(1 + kappa sigma/2) * sqrt(lb)

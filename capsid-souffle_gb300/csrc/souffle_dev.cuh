@@ -118,6 +118,17 @@ struct __align__(16) SysState {
   unsigned int lcg;      // Brownian: minstd_rand0 state before this step's draws
 };
 
+// The chain in FP64 (souffle_options.chain_fp64): the link variables and constants of one system
+// in the reference's double arithmetic.  xi / eta are the current chain (after the backward half
+// of the next step, between launches); SysState's double-float xi / eta and xi_b / eta_b mirror
+// them for the energy output.
+struct Chain64 {
+  int m;
+  double dt;
+  double q[kMaxChain], t[kMaxChain], dof[kMaxChain];
+  double xi[kMaxChain], eta[kMaxChain];
+};
+
 // Lengths of the force kernel's per-bead fixed-point force limbs (3 components x 3 32-bit limbs
 // per bead, padded to keep 16-byte alignment) and of its prefix-sum array (nbead + 1 ints,
 // padded to a multiple of 4).

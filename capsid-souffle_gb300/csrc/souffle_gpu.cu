@@ -406,6 +406,7 @@ ForceArgs force_args(souffle_gpu_system* h, int mode, bool want_parts) {
   a.fdrag = h->bd_fdrag.p;
   a.fran = h->bd_fran.p;
   a.bb_pos32 = h->bb_pos32.p;
+  a.chain64 = h->opt.chain_fp64 ? h->chain64.p : nullptr;
   a.max_sub = h->subs_per_cta;
   a.mode = mode;
   return a;
@@ -1137,6 +1138,24 @@ souffle_status souffle_gpu_md_begin(souffle_gpu_system* h) {
     S.inv_n = 1.0 / S.n_beads;
   }
   CUDA_TRY(cudaMemcpyAsync(h->d_state.p, st.data(), sizeof(SysState) * h->n_sys, cudaMemcpyHostToDevice, h->stream));
+  if (h->opt.chain_fp64) {
+    std::vector<Chain64> c64(h->n_sys);
+    for (int k = 0; k < h->n_sys; k++) {
+      Chain64& c = c64[k];
+      std::memset(&c, 0, sizeof(c));
+      c.m = st[k].m;
+      c.dt = h->prm[k].dt;
+      for (int j = 0; j < c.m; j++) {
+        c.q[j] = st[k].q[j];
+        c.t[j] = st[k].t[j];
+        c.dof[j] = st[k].dof[j];
+      }
+    }
+    if (h->chain64.n != (size_t)h->n_sys) CUDA_TRY(h->chain64.alloc(h->n_sys));  // kept: graphs hold the pointer
+    CUDA_TRY(cudaMemcpyAsync(h->chain64.p, c64.data(), sizeof(Chain64) * h->n_sys, cudaMemcpyHostToDevice,
+                             h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+  }
   // initial forces with a rebuild (src/md.cpp:241) and particle_ke (src/md.cpp:258); the last
   // CTA then applies the backward half of the first step
   launch_rebuild(h);

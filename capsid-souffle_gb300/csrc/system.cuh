@@ -60,6 +60,7 @@ struct souffle_gpu_system {
   DevBuf<float> tpl_f;
   DevBuf<SysParams> d_sys;
   DevBuf<SysState> d_state;
+  DevBuf<Chain64> chain64;  // souffle_options.chain_fp64: the chain in FP64
   DevBuf<WorkItem> d_work;
   DevBuf<int2> d_slots;
   DevBuf<int> d_sub_sys, d_bead_sys;

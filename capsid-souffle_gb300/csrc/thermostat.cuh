@@ -110,6 +110,46 @@ __host__ __device__ inline bool nhc_backward(SysState& s) {
 }
 
 #ifdef __CUDACC__
+// ---- the chain in FP64 on one thread (souffle_options.chain_fp64), a validation variant -----
+// update_chain_xi (src/functions.cpp:33-58) and THERMOSTAT::update_eta (src/thermostat.h:35-40)
+// in the reference's double arithmetic and link order.
+__device__ inline void chain64_xi(Chain64& c, int j, double ke) {
+  if (c.q[j] == 0) return;
+  const double xn = j + 1 < kMaxChain ? c.xi[j + 1] : 0.0;
+  const double g = j == 0 ? 2 * ke - c.dof[0] * c.t[0] : c.q[j - 1] * c.xi[j - 1] * c.xi[j - 1] - c.dof[j] * c.t[j];
+  c.xi[j] = c.xi[j] * exp(-0.5 * c.dt * xn) + 0.5 * c.dt * (1.0 / c.q[j]) * g * exp(-0.25 * c.dt * xn);
+}
+__device__ inline void chain64_eta(Chain64& c) {
+  for (int j = 0; j < c.m; j++)
+    if (c.q[j] != 0) c.eta[j] = c.eta[j] + 0.5 * c.dt * c.xi[j];
+}
+// forward half at the end of a step (src/md.cpp:457-460); mirrors xi / eta for the energy output
+__device__ inline void chain64_forward(Chain64& c, double ke, SysState& S) {
+  chain64_eta(c);
+  for (int j = 0; j < c.m; j++) chain64_xi(c, j, ke);
+  for (int j = 0; j < c.m; j++) {
+    S.xi[j] = df_from(c.xi[j]);
+    S.eta[j] = df_from(c.eta[j]);
+  }
+}
+// backward half at the start of the next step (src/md.cpp:401-406) and its kick factors:
+// expfac = exp(-dt xi_0 / 2), 1 - expfac = -(e^h - 1)(e^h + 1) with h = -dt xi_0 / 4,
+// kick_c0 = dt e^h / 2.  False when they leave the fixed-point kick's range.
+__device__ inline bool chain64_backward(Chain64& c, double ke, SysState& S) {
+  for (int j = c.m - 1; j > -1; j--) chain64_xi(c, j, ke);
+  chain64_eta(c);
+  for (int j = 0; j < c.m; j++) {
+    S.xi_b[j] = df_from(c.xi[j]);
+    S.eta_b[j] = df_from(c.eta[j]);
+  }
+  const double u = expm1(-0.25 * c.dt * c.xi[0]);
+  const double one_minus = -u * (u + 2.0), kc0 = 0.5 * c.dt * (u + 1.0);
+  if (!(fabs(one_minus) < 1.9) || !(fabs(kc0) < 1.0e6)) return false;
+  S.delta_fx = __double2ll_rn(one_minus * 4611686018427387904.0);  // 2^62
+  S.kick_c0 = df_from(kc0);
+  return true;
+}
+
 static_assert(kMaxChain <= 32, "one lane per chain link");
 
 // Forward half on one warp: lane j evaluates link j's exponential, A_j, B_j and eta_j at once;

@@ -79,7 +79,7 @@ class Params_(C.Structure):
 class Options_(C.Structure):
     _fields_ = [("inter_capacity", C.c_int32), ("cand_capacity", C.c_int32),
                 ("compat_quirks", C.c_int32), ("device", C.c_int32),
-                ("threads_per_cta", C.c_int32), ("subunits_per_cta", C.c_int32)]
+                ("threads_per_cta", C.c_int32), ("subunits_per_cta", C.c_int32), ("chain_fp64", C.c_int32)]
 
 
 class Tuning_(C.Structure):
@@ -194,7 +194,7 @@ class GpuSystem:
 
     def __init__(self, t: Template, params: Sequence[Params_], inter_capacity: int = 0,
                  cand_capacity: int = 0, quirks: bool = True, device: int = 0, threads_per_cta: int = 0,
-                 subunits_per_cta: int = 0):
+                 subunits_per_cta: int = 0, chain_fp64: bool = False):
         self.lib = load()
         self.t = t
         self._arrs = dict(
@@ -219,7 +219,7 @@ class GpuSystem:
         self.params = list(params)
         arr = (Params_ * len(self.params))(*self.params)
         opts = Options_(inter_capacity, cand_capacity, 1 if quirks else -1, device, threads_per_cta,
-                        subunits_per_cta)
+                        subunits_per_cta, 1 if chain_fp64 else 0)
         h = C.c_void_p()
         _check(self.lib.souffle_gpu_create(C.byref(tpl), arr, len(self.params), C.byref(opts),
                                            C.byref(h)))

@@ -98,6 +98,10 @@ typedef struct souffle_options {
   int32_t threads_per_cta;/* force-kernel block size, 64..256 in steps of 32 (0 = default 256;
                              souffle_gpu_autotune chooses it by measurement) */
   int32_t subunits_per_cta;/* subunits per force-kernel CTA (0 = default: up to 128 beads) */
+  int32_t chain_fp64;     /* 1: run the Nose-Hoover chain in FP64 on one thread (the reference's
+                             double arithmetic, src/functions.cpp:33-58), a validation variant of
+                             the default double-float chain; slower by several microseconds per
+                             step on GB300's FP64 latency.  0 = double-float (default) */
 } souffle_options;
 
 typedef struct souffle_energies {

@@ -263,3 +263,33 @@ def test_brownian_steps_match_reference_run(name):
     e = s.energies()
     assert e["temperature"] == pytest.approx(g["bd_energy_rows"][-1, 8], rel=2e-5)
     assert e["thermo_pe"] == 0 and e["thermo_ke"] == 0      # no thermostat in Brownian runs
+
+
+def test_fp64_chain_variant_tracks_oracle_and_double_float_chain():
+    """The FP64 thermostat chain (souffle_options.chain_fp64, one thread, the reference's double
+    arithmetic) against the oracle over 100 steps, and against the default double-float chain at
+    the same step: the two chains differ by their rounding (2^-53 against ~2^-46 per operation),
+    which the trajectory amplifies about a hundredfold per hundred steps on this system."""
+    import pyoracle
+    g = load_golden("plain_small")
+    s64, t, opt, d = _gpu(g, chain_fp64=True)
+    o = pyoracle.Oracle(t, int(g["n_sub"]), d, opt.s, opt.b, opt.E, int(g["center"]))
+    o.set_state(g["pos"], g["vel"])
+    o.forces(True)
+    ke_o = o.kinetic_energy()
+    o.nhc_init(int(opt.q), opt.Q, opt.K)
+    s64.md_begin()
+    for a in range(100):
+        ke_o, _, _ = o.md_step(a, opt.t, int(opt.B), ke_o)
+        s64.md_steps(a, 1)
+        ke_g, xi_g, _ = s64.md_scalars()
+        assert ke_g == pytest.approx(ke_o, rel=1e-5), a
+    assert xi_g == pytest.approx(o.nhc.xi[0], rel=1e-5, abs=1e-9)
+    sdf, *_ = _gpu(g)
+    sdf.md_begin()
+    sdf.md_steps(0, 100)
+    k64, x64, _ = s64.md_scalars()
+    kdf, xdf, _ = sdf.md_scalars()
+    assert k64 == pytest.approx(kdf, rel=1e-9) and x64 == pytest.approx(xdf, rel=1e-9, abs=1e-12)
+    e64, edf = s64.energies(), sdf.energies()
+    assert e64["thermo_pe"] == pytest.approx(edf["thermo_pe"], rel=1e-9, abs=1e-9)

@@ -127,6 +127,9 @@ __device__ __noinline__ void bigbead_mask(const ForceArgs& a, const SysParams& P
 
 // 5 CTAs of 256 threads per SM (<= 51 registers) so 3-subunit work items fit one wave of
 // 152 x 5 CTAs at the 2000-subunit workload.
+// kChain64: the tail runs the FP64 validation chain (souffle_options.chain_fp64) instead of the
+// double-float one; a separate instantiation, so that the default kernel's code is untouched.
+template <bool kChain64>
 __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const TplLayout& L = a.L;
@@ -594,12 +597,11 @@ __global__ void __launch_bounds__(256, 5) k_forces(ForceArgs a) {
       }
     }
     __syncwarp();
-    if (a.chain64) {  // FP64 validation variant, one thread
+    if constexpr (kChain64) {  // FP64 validation variant, one thread
       if (lane == 0) {
         Chain64& c = a.chain64[w.sys];
-        const double ke = (double)s_red[0] * 2.3283064365386963e-10;  // 2^-32
-        if (a.mode == 1) chain64_forward(c, ke, S);
-        if (!chain64_backward(c, ke, S)) atomicOr(a.err, kErrNonFinite);
+        if (!chain64_tail(c, (double)s_red[0] * 2.3283064365386963e-10, a.mode == 1, S))  // KE: 2^-32 units
+          atomicOr(a.err, kErrNonFinite);
       }
       __syncwarp();
     } else {
@@ -789,7 +791,10 @@ __global__ void k_state_out(StateArgs a) {
 
 namespace souffle {
 void launch_forces(const ForceArgs& a, int grid, int block, size_t smem, cudaStream_t s) {
-  k_forces<<<grid, block, smem, s>>>(a);
+  if (a.chain64)
+    k_forces<true><<<grid, block, smem, s>>>(a);
+  else
+    k_forces<false><<<grid, block, smem, s>>>(a);
 }
 void launch_drift(const DriftArgs& a, int grid, int block, cudaStream_t s) {
   k_drift<<<grid, block, 0, s>>>(a);
@@ -801,12 +806,14 @@ void launch_state_out(const StateArgs& a, int grid, int block, cudaStream_t s) {
   k_state_out<<<grid, block, 0, s>>>(a);
 }
 cudaError_t set_kernel_smem(size_t force_smem, int force_threads, size_t pair_smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_forces, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_smem);
+  cudaError_t e = cudaFuncSetAttribute(k_forces<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_forces<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_smem);
   if (e != cudaSuccess) return e;
   // Ask for a shared-memory carveout that holds as many force CTAs as the registers allow (the
   // default may be smaller, which splits a one-wave grid into two waves).
   cudaFuncAttributes fa{};
-  if ((e = cudaFuncGetAttributes(&fa, k_forces)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&fa, k_forces<false>)) != cudaSuccess) return e;
   int dev = 0, regs_sm = 0, smem_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess) return e;
@@ -815,14 +822,15 @@ cudaError_t set_kernel_smem(size_t force_smem, int force_threads, size_t pair_sm
   const int ctas = regs_sm / (warp_regs * ((force_threads + 31) / 32));
   const size_t need = (size_t)ctas * (force_smem + fa.sharedSizeBytes + 1024);
   const int percent = (int)std::min<size_t>(100, (need * 100 + smem_sm - 1) / (size_t)smem_sm);
-  if ((e = cudaFuncSetAttribute(k_forces, cudaFuncAttributePreferredSharedMemoryCarveout, percent)) != cudaSuccess)
+  if ((e = cudaFuncSetAttribute(k_forces<false>, cudaFuncAttributePreferredSharedMemoryCarveout, percent)) != cudaSuccess ||
+      (e = cudaFuncSetAttribute(k_forces<true>, cudaFuncAttributePreferredSharedMemoryCarveout, percent)) != cudaSuccess)
     return e;
   return set_pairs_smem(pair_smem);
 }
 
 cudaError_t force_wave_ctas(int threads, size_t smem, int* ctas) {
   int per_sm = 0, dev = 0, sms = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces, threads, smem);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces<false>, threads, smem);
   if (e != cudaSuccess) return e;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;

@@ -155,6 +155,16 @@ struct EnergyArgs {
   int n0, n;               // first bead of the system, beads in it
   double* se; double* be; double* ne; double* ce; double* ke;  // [n] (system-local)
   double* totals;          // [8] per call
+  double* pair_tab;        // [3][np * np] per template bead pair (i, j): the Yukawa size factor,
+                           // sbar^6, the attractive LJ shift at ecut (k_energy_tables)
+  unsigned char* att_tab;  // [np * np] 1 = attractive by the directed LJ table
+  // cell grid of the pair pass (nc cells per axis, nc >= 3; nc = 0: every pair j > i is visited)
+  int nc;
+  int* cell_count;         // [nc^3] (zeroed before the count)
+  int* cell_start;         // [nc^3 + 1]
+  int* cell_fill;          // [nc^3] (zeroed before the scatter)
+  int* cell_beads;         // [n] system-local bead indices, ascending within each cell
+  int* bead_cell;          // [n]
   // encapsulation big beads of the system: fixed-point positions [3][total], the big-bead parts
   // of ne and ce per subunit bead [n] and their sums ([2]: lj, electrostatic)
   const long long* bb_fx = nullptr;

@@ -1052,6 +1052,28 @@ souffle_status souffle_gpu_energies(souffle_gpu_system* h, int32_t system, souff
     a.ce_bb = h->e_bead.p + 6 * (size_t)n;
     a.bb_totals = h->e_tot.p + 5;
   }
+  {
+    const size_t np2 = (size_t)h->tpl.np * h->tpl.np;
+    if (h->e_pair_tab.n != 3 * np2) CUDA_TRY(h->e_pair_tab.alloc(3 * np2));
+    if (h->e_att_tab.n != np2) CUDA_TRY(h->e_att_tab.alloc(np2));
+    a.pair_tab = h->e_pair_tab.p;
+    a.att_tab = h->e_att_tab.p;
+    // cell grid for the pair pass: cells at least the reach of every pair term wide (with a
+    // margin), at most 128 per axis; none without a DH cut-off (every pair then counts)
+    const double reach = std::max(std::max(p.ecut, p.ecut_el), 1.12246205 * a.sigma_max) * 1.01;
+    const int nc = p.ecut_el > 0 ? (int)std::min(128.0, std::floor(p.box / reach)) : 0;
+    a.nc = nc >= 3 ? nc : 0;
+    if (a.nc) {
+      const size_t ncell = (size_t)a.nc * a.nc * a.nc;
+      const size_t need = 3 * ncell + 1 + 2 * (size_t)n;
+      if (h->e_cells.n < need) CUDA_TRY(h->e_cells.alloc(need));
+      a.cell_count = h->e_cells.p;
+      a.cell_fill = h->e_cells.p + ncell;
+      a.cell_start = h->e_cells.p + 2 * ncell;
+      a.cell_beads = h->e_cells.p + 3 * ncell + 1;
+      a.bead_cell = a.cell_beads + n;
+    }
+  }
   launch_energies(a, n, h->stream);
   CUDA_TRY(cudaGetLastError());
   double tot[8];

@@ -78,7 +78,9 @@ struct souffle_gpu_system {
   DevBuf<dfloat> inv_mass;
   DevBuf<double> mass_d, q_d, sigma_d, len0_d;
   DevBuf<int> type_d, lj_d;
-  DevBuf<double> e_bead, e_tot;
+  DevBuf<double> e_bead, e_tot, e_pair_tab;
+  DevBuf<unsigned char> e_att_tab;
+  DevBuf<int> e_cells;  // the energy pass's cell grid: count, start, fill (3 nc^3 + 1), beads, bead cells (2 n)
   DevBuf<unsigned int> err;
   unsigned int* err_host = nullptr;  // pinned landing word for the error flag's read-back
   // Brownian systems: per system and template bead drag (2^40 units) and noise scale, the

@@ -150,6 +150,13 @@ __device__ inline bool chain64_backward(Chain64& c, double ke, SysState& S) {
   return true;
 }
 
+// Both halves as the force kernel's tail runs them (forward only after an MD step); out of line so
+// that the FP64 code does not weigh on the force kernel's registers.
+static __device__ __noinline__ bool chain64_tail(Chain64& c, double ke, bool forward, SysState& S) {
+  if (forward) chain64_forward(c, ke, S);
+  return chain64_backward(c, ke, S);
+}
+
 static_assert(kMaxChain <= 32, "one lane per chain link");
 
 // Forward half on one warp: lane j evaluates link j's exponential, A_j, B_j and eta_j at once;

@@ -28,7 +28,8 @@ void record_error(const std::string& msg);
 bool mlp_fused_supported(int n_in, int width, int out_pad);
 cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const int* m_dyn, int n_in,
                               const __nv_bfloat16* const w[4], const int ldw[4], int out_pad, const float* const bias[4],
-                              float* y, int ldy, unsigned int* err, unsigned int err_bit, cudaStream_t st);
+                              float* y, int ldy, unsigned int* err, unsigned int err_bit, cudaStream_t st,
+                              __nv_bfloat16* yb = nullptr);
 }
 
 using namespace souffle;
@@ -178,6 +179,7 @@ struct souffle_mlp {
   DevBuf<float> z[kLayers];                            // z_1 .. z_3 (index l for layer l output)
   DevBuf<__nv_bfloat16> dz[kLayers + 1], dz_t[kLayers + 1];  // dZ_l for l = 1..4 (4 = dY)
   DevBuf<float> y, partial, loss;
+  DevBuf<__nv_bfloat16> yb;  // BF16 copy of the output rows (fused forward for the surrogate)
   DevBuf<unsigned int> err;
   long long steps = 0;
   // the normalisation of the data the surrogate was trained on: per input feature mean and
@@ -327,6 +329,22 @@ cudaError_t mlp_forward_async(souffle_mlp* h, const float* x, int m_cap, const i
   return mlp_forward_packed_async(h, m_cap, m_dyn, err, st, y, ldy);
 }
 
+// The fused forward over rows already in the BF16 input buffer, output rows in BF16 (*yb, row
+// stride *ldy) -- the form the surrogate step reads; false when the shape has no fused forward.
+bool mlp_forward_packed_bf16_async(souffle_mlp* h, int m_cap, const int* m_dyn, unsigned int* err, cudaStream_t st,
+                                   const __nv_bfloat16** yb, int* ldy, cudaError_t* r) {
+  const int L = kLayers - 1;
+  if (m_cap < 1 || m_cap > h->cap || !mlp_fused_supported(h->n_in, h->width, h->out_pad[L])) return false;
+  const __nv_bfloat16* w[4] = {h->wb[0].p, h->wb[1].p, h->wb[2].p, h->wb[3].p};
+  const int ldw[4] = {h->in[0], h->in[1], h->in[2], h->in[3]};
+  const float* b[4] = {h->b[0].p, h->b[1].p, h->b[2].p, h->b[3].p};
+  *r = mlp_forward_fused(h->act[0].p, h->in_ld[0], m_cap, m_dyn, h->n_in, w, ldw, h->out_pad[L], b, nullptr,
+                         h->out_pad[L], err, kErrSurrogateBit, st, h->yb.p);
+  *yb = h->yb.p;
+  *ldy = h->out_pad[L];
+  return true;
+}
+
 // The network's BF16 input buffer [cap][*ld] (row-major), which mlp_forward_packed_async reads.
 __nv_bfloat16* mlp_input_bf16(souffle_mlp* h, int* ld) {
   *ld = h->in_ld[0];
@@ -435,6 +453,7 @@ souffle_status souffle_mlp_create(int32_t n_in, int32_t width, int32_t n_out, in
     MLP_TRY_C(cudaMemset(h->dz_t[l].p, 0, (size_t)cols * h->cap * 2));
   }
   MLP_TRY_C(h->y.alloc((size_t)h->cap * h->out_pad[kLayers - 1]));
+  MLP_TRY_C(h->yb.alloc((size_t)h->cap * h->out_pad[kLayers - 1]));
   for (auto* b : {&h->x_mean, &h->x_istd}) MLP_TRY_C(b->alloc(n_in));
   for (auto* b : {&h->t_mean, &h->t_std, &h->t_istd}) MLP_TRY_C(b->alloc(n_out));
   MLP_TRY_C(h->partial.alloc(blocks((long long)h->cap * h->out_pad[kLayers - 1], 256)));

@@ -60,7 +60,8 @@ struct FusedArgs {
   int n_in;             // <= 64
   int out_pad;          // output columns computed and stored (multiple of 16, <= 256)
   const float* bias[4];  // [256] x 3, [out_pad]
-  float* y;             // [m_cap][ldy] FP32
+  float* y;             // [m_cap][ldy] FP32, or
+  __nv_bfloat16* yb;    // [m_cap][ldy] BF16 (when set, instead of y)
   int ldy;
   unsigned int* err;
   unsigned int err_bit;
@@ -319,14 +320,29 @@ __global__ void __launch_bounds__(kFThreads, 1)
             const float* ob = s_bias + 3 * kFWidth;
             const int nh = a.out_pad >> 1;
             const int cb = half * nh, ce = cb + nh;
-            float* yrow = a.y + (size_t)row * a.ldy;
+            float* yrow = a.y ? a.y + (size_t)row * a.ldy : nullptr;
+            __nv_bfloat16* ybrow = a.yb ? a.yb + (size_t)row * a.ldy : nullptr;
             const bool vec = ((a.ldy & 3) == 0) && ((reinterpret_cast<uintptr_t>(a.y) & 15) == 0);
+            const bool vecb = ((a.ldy & 7) == 0) && ((reinterpret_cast<uintptr_t>(a.yb) & 15) == 0);
             int c0 = cb;
 #pragma unroll 1
             for (; c0 + 32 <= ce; c0 += 32) {
               float v[32];
               tmem_ld32(t_row + (uint32_t)c0, v);
-              if (row_ok) {
+              if (row_ok && ybrow) {  // BF16 rows: 16-byte stores of 8 values
+                if (vecb && (c0 & 7) == 0) {
+#pragma unroll
+                  for (int k = 0; k < 4; k++)
+                    *reinterpret_cast<uint4*>(ybrow + c0 + 8 * k) =
+                        make_uint4(pack2_bf16(v[8 * k] + ob[c0 + 8 * k], v[8 * k + 1] + ob[c0 + 8 * k + 1]),
+                                   pack2_bf16(v[8 * k + 2] + ob[c0 + 8 * k + 2], v[8 * k + 3] + ob[c0 + 8 * k + 3]),
+                                   pack2_bf16(v[8 * k + 4] + ob[c0 + 8 * k + 4], v[8 * k + 5] + ob[c0 + 8 * k + 5]),
+                                   pack2_bf16(v[8 * k + 6] + ob[c0 + 8 * k + 6], v[8 * k + 7] + ob[c0 + 8 * k + 7]));
+                } else {
+#pragma unroll
+                  for (int k = 0; k < 32; k++) ybrow[c0 + k] = __float2bfloat16_rn(v[k] + ob[c0 + k]);
+                }
+              } else if (row_ok) {
                 if (vec && (c0 & 3) == 0) {
 #pragma unroll
                   for (int k = 0; k < 8; k++)
@@ -343,7 +359,10 @@ __global__ void __launch_bounds__(kFThreads, 1)
             for (; c0 < ce; c0 += 8) {
               float v[8];
               tmem_ld8(t_row + (uint32_t)c0, v);
-              if (row_ok) {
+              if (row_ok && ybrow) {
+#pragma unroll
+                for (int k = 0; k < 8; k++) ybrow[c0 + k] = __float2bfloat16_rn(v[k] + ob[c0 + k]);
+              } else if (row_ok) {
 #pragma unroll
                 for (int k = 0; k < 8; k++) yrow[c0 + k] = v[k] + ob[c0 + k];
               }
@@ -405,8 +424,9 @@ bool mlp_fused_supported(int n_in, int width, int out_pad) {
 
 cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const int* m_dyn, int n_in,
                               const __nv_bfloat16* const w[4], const int ldw[4], int out_pad, const float* const bias[4],
-                              float* y, int ldy, unsigned int* err, unsigned int err_bit, cudaStream_t st) {
-  if (!mlp_fused_supported(n_in, kFWidth, out_pad) || m_cap < 1 || !x || !y || !err || ldx < n_in || ldx % 8 ||
+                              float* y, int ldy, unsigned int* err, unsigned int err_bit, cudaStream_t st,
+                              __nv_bfloat16* yb) {
+  if (!mlp_fused_supported(n_in, kFWidth, out_pad) || m_cap < 1 || !x || !(y || yb) || !err || ldx < n_in || ldx % 8 ||
       ldy < out_pad || (reinterpret_cast<uintptr_t>(x) & 15) || ldw[0] < n_in || ldw[1] < kFWidth ||
       ldw[2] < kFWidth || ldw[3] < kFWidth)
     return cudaErrorInvalidValue;
@@ -436,7 +456,8 @@ cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const 
   a.n_in = n_in;
   a.out_pad = out_pad;
   for (int l = 0; l < 4; l++) a.bias[l] = bias[l];
-  a.y = y;
+  a.y = yb ? nullptr : y;
+  a.yb = yb;
   a.ldy = ldy;
   a.err = err;
   a.err_bit = err_bit;

@@ -44,6 +44,8 @@ cudaError_t mlp_forward_async(souffle_mlp* h, const float* x, int m_cap, const i
 cudaError_t mlp_forward_packed_async(souffle_mlp* h, int m_cap, const int* m_dyn, unsigned int* err, cudaStream_t st,
                                      const float** y, int* ldy);
 __nv_bfloat16* mlp_input_bf16(souffle_mlp* h, int* ld);
+bool mlp_forward_packed_bf16_async(souffle_mlp* h, int m_cap, const int* m_dyn, unsigned int* err, cudaStream_t st,
+                                   const __nv_bfloat16** yb, int* ldy, cudaError_t* r);
 void mlp_dims(const souffle_mlp* h, int* n_in, int* n_out, int* cap);
 MlpNorm mlp_norm(souffle_mlp* h);
 }  // namespace souffle
@@ -78,7 +80,8 @@ struct FarArgs {
   int ldxb;
   const float* x_mean;   // null: raw descriptors
   const float* x_istd;
-  const float* y;        // network output [far_cap][ldy], normalised
+  const float* y;        // network output [far_cap][ldy], normalised, FP32, or
+  const __nv_bfloat16* yb;  // the same rows in BF16 (when set)
   int ldy;
   const float* t_mean;
   const float* t_std;
@@ -464,9 +467,13 @@ __device__ void far_descr_one(const FarArgs& a, int p) {
 }
 
 // force on this lane's beads of subunit A (body frame) from the network output row of one pair
-__device__ __forceinline__ void net_body_forces(const FarArgs& a, const float* row, const Frame& F,
+__device__ __forceinline__ float net_out(const FarArgs& a, size_t i) {
+  return a.yb ? __bfloat162float(a.yb[i]) : a.y[i];
+}
+
+__device__ __forceinline__ void net_body_forces(const FarArgs& a, size_t row, const Frame& F,
                                                 const float3 (&e)[kBeadsPerLane], int lane, float3 (&g)[kBeadsPerLane]) {
-  auto out = [&](int k) { return row[k] * a.t_std[k] + a.t_mean[k]; };
+  auto out = [&](int k) { return net_out(a, row + k) * a.t_std[k] + a.t_mean[k]; };
   const float3 Ft = f3_(out(0), out(1), out(2));
   const float3 tau = f3_(out(3), out(4), out(5));
   const float3 w = mat3(F.Ji, tau);
@@ -499,7 +506,7 @@ __global__ void __launch_bounds__(128) k_far_apply(FarArgs a) {
     const float npairs = (float)(hi - lo);
     for (int c = lane; c < a.n_out; c += 32) {
       float t = 0.f;
-      for (int q = lo; q < hi; q++) t += a.y[(size_t)q * a.ldy + c];
+      for (int q = lo; q < hi; q++) t += net_out(a, (size_t)q * a.ldy + c);
       sum[c] = t * a.t_std[c] + npairs * a.t_mean[c];
     }
     __syncwarp();
@@ -652,7 +659,7 @@ __global__ void __launch_bounds__(128) k_far_judge(FarArgs a) {
   int4 p[kBeadsPerLane];
   body_coords(a, ab.x, F, lane, e, p);
   exact_body_forces(a, ab.x, ab.y, F, p, lane, gx);
-  net_body_forces(a, a.y + (size_t)q * a.ldy, F, e, lane, gn);
+  net_body_forces(a, (size_t)q * a.ldy, F, e, lane, gn);
   float num = 0.f;
 #pragma unroll
   for (int b = 0; b < kBeadsPerLane; b++) {
@@ -752,6 +759,7 @@ struct SurrogateCtx {
   DevBuf<float> judge_err;
   DevBuf<long long> judged;
   const float* y = nullptr;  // network output (inside the network's buffers) of the last forward
+  const __nv_bfloat16* yb = nullptr;  // or its BF16 rows
   int ldy = 0;
 };
 
@@ -803,6 +811,7 @@ FarArgs far_args(souffle_gpu_system* h) {
   a.x_mean = c.norm.x_mean;
   a.x_istd = c.norm.x_istd;
   a.y = c.y;
+  a.yb = c.yb;
   a.ldy = c.ldy;
   a.t_mean = c.norm.t_mean;
   a.t_std = c.norm.t_std;
@@ -904,14 +913,19 @@ void surrogate_forces(souffle_gpu_system* h, ForceArgs& fa) {
   a.xb = mlp_input_bf16(c.net, &a.ldxb);
   k_far_descr<<<std::min((c.far_cap + 127) / 128, 152 * 8), 128, 0, h->stream>>>(a);
   const float* y = nullptr;
+  const __nv_bfloat16* yb = nullptr;
   int ldy = 0;
-  if (mlp_forward_packed_async(c.net, c.far_cap, c.far_total.p, h->err.p, h->stream, &y, &ldy) != cudaSuccess) {
-    // parameters were validated at attach; a launch failure surfaces through cudaGetLastError
-    return;
-  }
+  cudaError_t r = cudaSuccess;
+  // the fused forward with BF16 output rows (half the bytes for k_far_apply and the judge to
+  // read); the per-layer forward with FP32 rows for shapes the fused kernel does not cover
+  if (!mlp_forward_packed_bf16_async(c.net, c.far_cap, c.far_total.p, h->err.p, h->stream, &yb, &ldy, &r))
+    r = mlp_forward_packed_async(c.net, c.far_cap, c.far_total.p, h->err.p, h->stream, &y, &ldy);
+  if (r != cudaSuccess) return;  // parameters were validated at attach; launch failures surface later
   c.y = y;
+  c.yb = yb;
   c.ldy = ldy;
   a.y = y;
+  a.yb = yb;
   a.ldy = ldy;
   k_far_apply<<<sb, 128, 0, h->stream>>>(a);
   fa.surr_f = c.sf.p;

@@ -489,8 +489,9 @@ __device__ __forceinline__ void net_body_forces(const FarArgs& a, size_t row, co
 
 // Forces on each subunit's beads from all its far pairs, warp per subunit.  The force on bead i
 // from one pair is affine in the network's output row (F / np + (J^-1 tau) x d_i + r_i after
-// de-normalisation), so the rows of the subunit's pairs are summed first (in pair order, one
-// output column per lane) and the per-bead forces are formed once from the sum.
+// de-normalisation), so the rows of the subunit's pairs are summed first (in pair order; eight
+// BF16 columns per lane from one 16-byte load, or one FP32 column per lane) and the per-bead
+// forces are formed once from the sum.
 __global__ void __launch_bounds__(128) k_far_apply(FarArgs a) {
   __shared__ float s_sum[4][256];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -504,10 +505,42 @@ __global__ void __launch_bounds__(128) k_far_apply(FarArgs a) {
   for (int k = 0; k < kBeadsPerLane; k++) acc[k] = f3_(0.f, 0.f, 0.f);
   if (lo < hi) {
     const float npairs = (float)(hi - lo);
-    for (int c = lane; c < a.n_out; c += 32) {
-      float t = 0.f;
-      for (int q = lo; q < hi; q++) t += net_out(a, (size_t)q * a.ldy + c);
-      sum[c] = t * a.t_std[c] + npairs * a.t_mean[c];
+    if (a.yb && (a.ldy & 7) == 0) {
+      // BF16 rows: one 16-byte load (8 columns) per lane per pair, pairs two at a time, summed in
+      // pair order
+      const int c0 = 8 * lane;
+      if (c0 < a.n_out) {
+        float t[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) t[j] = 0.f;
+        auto add_row = [&](const uint4 v) {
+          const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[j]));
+            t[2 * j] += f.x;
+            t[2 * j + 1] += f.y;
+          }
+        };
+        const uint4* row = reinterpret_cast<const uint4*>(a.yb + (size_t)lo * a.ldy + c0);
+        const size_t step = (size_t)(a.ldy >> 3);
+        int q = lo;
+        for (; q + 1 < hi; q += 2, row += 2 * step) {
+          const uint4 v0 = __ldg(row), v1 = __ldg(row + step);
+          add_row(v0);
+          add_row(v1);
+        }
+        if (q < hi) add_row(__ldg(row));
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          if (c0 + j < a.n_out) sum[c0 + j] = t[j] * a.t_std[c0 + j] + npairs * a.t_mean[c0 + j];
+      }
+    } else {
+      for (int c = lane; c < a.n_out; c += 32) {
+        float t = 0.f;
+        for (int q = lo; q < hi; q++) t += net_out(a, (size_t)q * a.ldy + c);
+        sum[c] = t * a.t_std[c] + npairs * a.t_mean[c];
+      }
     }
     __syncwarp();
     F = load_frame(a.frame + (size_t)s * kFrame);

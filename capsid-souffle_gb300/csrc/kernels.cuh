@@ -51,6 +51,7 @@ struct PairArgs {
   const int* far_ok = nullptr;              // the far flags apply (no far-list overflow)
   int* ref_len;              // [N] reference list length (intra + inter)
   int inter_cap;
+  int chunk;                 // candidates staged together (1 .. kPairChunkMax)
   unsigned int* err;
 };
 
@@ -178,6 +179,10 @@ void launch_cells_scan(const CellArgs& a, cudaStream_t s);
 void launch_cells_scatter(const CellArgs& a, int grid, int block, cudaStream_t s);
 void launch_candidates(const CandArgs& a, int grid, int block, cudaStream_t s);
 void launch_pairs(const PairArgs& a, int n_sub, size_t smem, cudaStream_t s);
+// k_pairs' chunk of candidates staged together, and its dynamic shared memory
+constexpr int kPairChunkMax = 32;
+int pair_chunk(int np, int words);
+size_t pair_smem_bytes(int np, int words, int chunk);
 void launch_forces(const ForceArgs& a, int grid, int block, size_t smem, cudaStream_t s);
 void launch_drift(const DriftArgs& a, int grid, int block, cudaStream_t s);
 void launch_state_in(const StateArgs& a, int grid, int block, cudaStream_t s);

@@ -179,8 +179,12 @@ __global__ void __launch_bounds__(128) k_candidates(CandArgs a) {
 
 // One CTA per subunit i; thread t owns bead rows t, t + blockDim, ... (at most two: blockDim is
 // np rounded up to whole warps, at most 128, so that a one-wave grid holds every subunit).
-// Candidate subunit j's positions are staged in shared memory, in ascending j, so each row's
-// entries come out in ascending global id.
+// Candidates are taken in ascending j, so each row's entries come out in ascending global id.
+// Runs of ordinary candidates are staged together (a chunk): their high words load in one round,
+// every (candidate, row) item computes its partner mask in parallel, and each row then appends
+// the chunk's partners in order -- a handful of barriers per chunk instead of per candidate.
+// Subunit i's own block (intra bits, each unordered pair once) and blocks with the stale-r2
+// semantics of the system's subunit 0 take the per-block path, one candidate at a time.
 __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int4* s32 = reinterpret_cast<int4*>(smem_raw);                   // [np] 16-byte entries first
@@ -221,9 +225,129 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
   for (int t = threadIdx.x; t < np * a.words; t += blockDim.x) s_imask[t] = 0u;
 
   const bool skip_far = a.cand_far && *a.far_ok;
-  for (int c = 0; c < ncand; c++) {
-    const int j = cand[c];
-    if (skip_far && a.cand_far[(size_t)i * a.cand_cap + c]) continue;  // uniform over the CTA
+  // chunk staging (after the per-block area, 16-byte aligned): the own rows' high words, the
+  // chunk's candidates' high words, and a mask of partners per (candidate, row)
+  const size_t blk_bytes = (size_t)np * (sizeof(int4) + 3 * sizeof(long long) + sizeof(double) + sizeof(int) +
+                                         sizeof(float)) + sizeof(unsigned int) * (size_t)np * a.words;
+  int4* s_own = reinterpret_cast<int4*>(smem_raw + ((blk_bytes + 15) & ~(size_t)15));
+  int4* c32 = s_own + np;
+  unsigned int* cmask = reinterpret_cast<unsigned int*>(c32 + (size_t)a.chunk * np);
+  __shared__ int s_cj[kPairChunkMax];
+  __shared__ unsigned char s_cfar[kPairChunkMax];
+  __shared__ float s_cR[kPairChunkMax];
+  for (int t = threadIdx.x; t < np; t += blockDim.x) s_own[t] = a.pos32[(size_t)i * np + t];
+  const bool cta_quirk = p.quirks && i_local == 0;  // every block of the system's subunit 0
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int c = 0;
+  while (c < ncand) {
+    __syncthreads();  // the previous chunk's readers are done
+    if (threadIdx.x < a.chunk) {
+      const int cc = c + threadIdx.x;
+      int j = -1;
+      unsigned char fl = 0;
+      if (cc < ncand) {
+        j = cand[cc];
+        fl = skip_far ? a.cand_far[(size_t)i * a.cand_cap + cc] : 0;
+      }
+      s_cj[threadIdx.x] = j;
+      s_cfar[threadIdx.x] = fl;
+    }
+    __syncthreads();
+    // The chunk runs up to the first candidate that takes the per-block path below: subunit i
+    // itself (intra bits) or a block with the stale-r2 semantics.  Far candidates (left to the
+    // surrogate or beyond every cut-off) stay in the chunk with empty masks.
+    int nk = 0;
+    for (; nk < a.chunk; nk++) {
+      const int j = s_cj[nk];
+      if (j < 0) break;
+      if (!s_cfar[nk] && (j == i || cta_quirk || (p.quirks && j == p.sub0))) break;
+    }
+    if (nk > 0) {
+      c += nk;
+      for (int t = threadIdx.x; t < nk * np; t += blockDim.x) {
+        const int k = t / np;
+        if (!s_cfar[k]) c32[t] = a.pos32[(size_t)s_cj[k] * np + (t - k * np)];
+      }
+      __syncthreads();
+      // each candidate's radius about its centre bead, warp per candidate
+      for (int k = wid; k < nk; k += nw) {
+        if (s_cfar[k]) continue;
+        const int4 pc = c32[k * np + p.center_local];
+        float m = 0.0f;
+        for (int t = lane; t < np; t += 32) {
+          const int4 pt = c32[k * np + t];
+          const float dx = hi_diff(pt.x, pc.x, unit), dy = hi_diff(pt.y, pc.y, unit), dz = hi_diff(pt.z, pc.z, unit);
+          m = fmaxf(m, sqrtf(dx * dx + dy * dy + dz * dz));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) s_cR[k] = m;
+      }
+      __syncthreads();
+      // partner masks of every (candidate, row) item: the same float test with its margin and
+      // exact fallback, and the same reach shortcut, as the per-block path
+      for (int t = threadIdx.x; t < nk * np; t += blockDim.x) {
+        const int k = t / np, ii = t - k * np;
+        unsigned int* mk = cmask + (size_t)t * a.words;
+        const int4* cj32 = c32 + k * np;
+        bool skip = s_cfar[k] != 0;
+        const int4 pi = s_own[ii];
+        if (!skip) {
+          const int4 pc = cj32[p.center_local];
+          const float reach = s_cR[k] + r_list + eps;
+          const float dx = hi_diff(pi.x, pc.x, unit), dy = hi_diff(pi.y, pc.y, unit), dz = hi_diff(pi.z, pc.z, unit);
+          skip = dx * dx + dy * dy + dz * dz > reach * reach;
+        }
+        const int gi = i * np + ii, jbase = s_cj[k] * np;
+        for (int w0 = 0; w0 < np; w0 += 32) {
+          unsigned int bits = 0;
+          if (!skip) {
+            const int w1 = min(np, w0 + 32);
+            for (int jj = w0; jj < w1; jj++) {
+              const int4 pj = cj32[jj];
+              const float dx = hi_diff(pi.x, pj.x, unit), dy = hi_diff(pi.y, pj.y, unit), dz = hi_diff(pi.z, pj.z, unit);
+              const float r2f = dx * dx + dy * dy + dz * dz;
+              bool in;
+              if (fabsf(r2f - nl2f) > margin) {
+                in = r2f < nl2f;
+              } else {
+                const int gj = jbase + jj;
+                const double ex = fixed_diff(a.px[gi], a.px[gj], p.fx_to_len);
+                const double ey = fixed_diff(a.py[gi], a.py[gj], p.fx_to_len);
+                const double ez = fixed_diff(a.pz[gi], a.pz[gj], p.fx_to_len);
+                in = ex * ex + ey * ey + ez * ez < p.nl2;
+              }
+              if (in) bits |= 1u << (jj - w0);
+            }
+          }
+          mk[w0 >> 5] = bits;
+        }
+      }
+      __syncthreads();
+      // ids in ascending global order: candidates in order, partners in bead order
+      for (int r = 0, ii = threadIdx.x; ii < np; ii += blockDim.x, r++) {
+        const int gi = i * np + ii;
+        int n = inter_n[r];
+        for (int k = 0; k < nk; k++) {
+          const unsigned int* mk = cmask + (size_t)(k * np + ii) * a.words;
+          const int jbase = s_cj[k] * np;
+          for (int w = 0; w < a.words; w++) {
+            unsigned int bits = mk[w];
+            while (bits) {
+              const int b = __ffs(bits) - 1;
+              bits &= bits - 1;
+              if (n < a.inter_cap) a.inter_ids[(size_t)gi * a.inter_cap + n] = jbase + (w << 5) + b;
+              n++;
+            }
+          }
+        }
+        inter_n[r] = n;
+      }
+      continue;
+    }
+    // per-block path for candidate s_cj[0]
+    const int j = s_cj[0];
+    c += 1;
     __syncthreads();
     if (threadIdx.x == 0) s_Rj = 0.0f;
     for (int t = threadIdx.x; t < np; t += blockDim.x) {
@@ -397,6 +521,18 @@ void launch_candidates(const CandArgs& a, int grid, int block, cudaStream_t s) {
   const int warps_per_block = 4;
   const int g = (a.c.n_sub_total + warps_per_block - 1) / warps_per_block;
   k_candidates<<<g, 32 * warps_per_block, sizeof(int) * warps_per_block * a.cap, s>>>(a);
+}
+// About 8 KB of staging per CTA (8 candidates of 42 beads), so that a one-wave grid of 64-thread
+// CTAs still fits the shared memory of an SM.
+int pair_chunk(int np, int words) {
+  const int per = np * (int)(sizeof(int4) + sizeof(unsigned int) * words);
+  return std::max(1, std::min(kPairChunkMax, 8192 / per));
+}
+size_t pair_smem_bytes(int np, int words, int chunk) {
+  const size_t blk = (size_t)np * (sizeof(int4) + 3 * sizeof(long long) + sizeof(double) + sizeof(int) + sizeof(float)) +
+                     sizeof(unsigned int) * (size_t)np * words;
+  return ((blk + 15) & ~(size_t)15) + sizeof(int4) * (size_t)np * (1 + chunk) +
+         sizeof(unsigned int) * (size_t)chunk * np * words;
 }
 void launch_pairs(const PairArgs& a, int n_sub, size_t smem, cudaStream_t s) {
   const int block = std::min(128, 32 * ((a.np + 31) / 32));

@@ -361,6 +361,7 @@ void launch_rebuild(souffle_gpu_system* h) {
   pa.inter_count = h->inter_count.p;
   pa.ref_len = h->ref_len.p;
   pa.inter_cap = h->inter_cap;
+  pa.chunk = h->pair_chunk;
   pa.err = h->err.p;
   if (surrogate_enabled(h)) surrogate_classify(h, pa);
   launch_pairs(pa, h->S, h->pair_smem, st);
@@ -729,8 +730,8 @@ souffle_status souffle_gpu_create(const souffle_template* tpl, const souffle_par
   CUDA_TRY(cudaMemset(h->inter_count.p, 0, sizeof(int) * N));
   CUDA_TRY(cudaMemset(h->force.p, 0, sizeof(long long) * 3 * N));
 
-  h->pair_smem = np * (3 * sizeof(long long) + sizeof(int4) + sizeof(double) + sizeof(int) + sizeof(float)) +
-                 sizeof(unsigned int) * np * ((np + 31) / 32);
+  h->pair_chunk = pair_chunk(np, L.words);
+  h->pair_smem = pair_smem_bytes(np, L.words, h->pair_chunk);
   s = plan_work(h.get(), h->subs_per_cta, h->threads);
   if (s != SOUFFLE_OK) return s;
   *out = h.release();

@@ -53,6 +53,7 @@ struct souffle_gpu_system {
   std::vector<int2> slots;
   int inter_cap = 96, cand_cap = 128;
   size_t force_smem = 0, pair_smem = 0;
+  int pair_chunk = 1;
   cudaStream_t stream = nullptr;
   bool began = false, have_state = false;
   // device

@@ -71,7 +71,9 @@ void create_handle(vector<SUBUNIT>& protein, vector<BEAD>& beads, double lb, dou
   p.nlist_cutoff = NListCutoff;
   p.nlist_capacity = (int)beads[0].itsN.size();
   p.center_local = (int)(s0.centerBead->id - base);
-  p.dt = 1;                 // unused by forces
+  // forceCalculation receives no time step and the forces do not use one; the handle still
+  // checks that dt / (2 m) fits its fixed-point kick, so give it the reference's default -t
+  p.dt = 0.005;
   p.chain_length = 1;
   p.temperature = 1;
   p.build_freq = 1;

@@ -1,14 +1,16 @@
 // Learned far-field surrogate inside a system handle (include/souffle_surrogate.h).
 //
-// Per rebuild:  k_far_classify   closest bead distance of every candidate subunit pair (warp per
-//                                pair, FP32 from the exact integer position differences); far
-//                                pairs are flagged so k_pairs leaves them out of the pair list
+// Per rebuild:  k_far_classify   closest bead distance of every candidate subunit pair j > i (warp
+//                                per pair, FP32 from the exact integer position differences)
+//               k_far_decide     the same distance for j < i from j's side; far / inert / near
+//                                flags, so k_pairs leaves far pairs out of the pair list
 //               k_far_scan       per-subunit far counts -> offsets (one CTA), overflow check
 //               k_far_write      the far-pair list (A, B) in candidate order, grouped by A
 // Per step:     k_sub_frames     per subunit: centre of mass, body frame, 12 elastic-mode
 //                                amplitudes, inverse of J = sum |d|^2 I - d d^T (warp per subunit)
 //               k_far_descr      64-float descriptors of the far pairs, normalised
-//               network forward  tcgen05 GEMMs (mlp.cu), rows beyond the far-pair count skipped
+//               network forward  one persistent tcgen05 kernel (mlp_fused.cu), BF16 output rows;
+//                                rows beyond the far-pair count skipped
 //               k_far_apply      forces on each subunit's beads from its far pairs, summed in
 //                                pair order (warp per subunit), for k_forces to add
 // Judge:        k_force_norms    per system: sum of |F|^2 over its beads (the last step's total forces)
@@ -64,7 +66,7 @@ struct FarArgs {
   const int* cand;
   const int* cand_count;
   unsigned char* cand_far;
-  float* cand_dmin;
+  float* cand_dmin;       // [S][cand_cap] squared closest bead distance of each candidate pair
   int* far_count;
   int* far_start;   // [S + 1]
   int* far_total;   // [0] pairs in the list, [1] pairs found, [2] list valid (1) or overflowed (0)
@@ -72,8 +74,8 @@ struct FarArgs {
   float* far_dmin;
   const int* class_off;  // [kClasses] or null (collect: every class)
   float* frame;          // [S][kFrame]
-  const float* modes;    // [kModes][np][3]
-  const float* rest;     // [np][3]
+  const float4* modes;   // [kModes][np] (x, y, z, 0)
+  const float4* rest;    // [np] (x, y, z, 0)
   int anchor1, anchor2;
   float* x;              // [far_cap][kDesc]
   __nv_bfloat16* xb;     // or, for inference: BF16 rows [far_cap][ldxb], the network's input buffer
@@ -127,6 +129,21 @@ __device__ __forceinline__ float wsum(float v) {
   return v;
 }
 __device__ __forceinline__ float3 wsum3(float3 v) { return f3_(wsum(v.x), wsum(v.y), wsum(v.z)); }
+// 32 warp-wide sums at once by recursive halving: afterwards lane L holds the sum over the warp
+// of v[L] (v[0] on return); 31 shuffles instead of 5 per sum.
+__device__ __forceinline__ float wsum_scatter32(float (&v)[32], int lane) {
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool up = (lane & h) != 0;
+#pragma unroll
+    for (int k = 0; k < h; k++) {
+      const float send = up ? v[k] : v[k + h];
+      const float keep = up ? v[k + h] : v[k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+    }
+  }
+  return v[0];
+}
 __device__ __forceinline__ int dist_class(float d, float r_sw) {
   return min(kClasses - 1, max(0, (int)((d - r_sw) * 2.0f)));
 }
@@ -175,55 +192,83 @@ __device__ __forceinline__ void body_coords(const FarArgs& a, int s, const Frame
 
 // ---- rebuild -------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_far_classify(FarArgs a) {
+  // closest bead pair of every candidate j > i (warp per candidate); the pairs with j < i are
+  // the same pairs seen from the other side and take their distance in k_far_decide
   extern __shared__ int4 s_pa[];  // [np]
-  __shared__ int s_cnt;
-  __shared__ float s_reach2;
   const int i = blockIdx.x, np = a.np;
   for (int t = threadIdx.x; t < np; t += blockDim.x) s_pa[t] = a.pos32[(size_t)i * np + t];
-  const SysParams& P = a.sys[a.sub_sys[i]];
-  if (threadIdx.x == 0) {
-    s_cnt = 0;
-    // reach of every pair term: the DH cut-off (+inf without one) and the LJ/WCA cut-offs
-    float r2 = P.ecut_el2;
-    for (int k = 0; k < kMaxSpecies * kMaxSpecies; k++) r2 = fmaxf(r2, a.pt->cut2[k]);
-    s_reach2 = r2 * 1.0001f;
-  }
   __syncthreads();
-  const float unit = P.unit32;
+  const float unit = a.sys[a.sub_sys[i]].unit32;
   const int ncand = a.cand_count[i];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  int my_far = 0;
   for (int c = warp; c < ncand; c += nw) {
     const int j = a.cand[(size_t)i * a.cand_cap + c];
-    float d2 = 3.0e38f;
-    const bool near = j == i;
-    if (j != i) {  // closest bead pair (an early exit at the switch radius measured slower)
-      for (int jj = lane; jj < np; jj += 32) {
-        const int4 pj = a.pos32[(size_t)j * np + jj];
-        for (int ii = 0; ii < np; ii++) {
-          const float3 d = dpos(s_pa[ii], pj, unit);
-          d2 = fminf(d2, dot3_(d, d));
-        }
+    if (j <= i) continue;  // uniform per warp
+    float d2 = 3.0e38f;  // full scan (an early exit at the switch radius measured slower)
+    for (int jj = lane; jj < np; jj += 32) {
+      const int4 pj = a.pos32[(size_t)j * np + jj];
+      for (int ii = 0; ii < np; ii++) {
+        const float3 d = dpos(s_pa[ii], pj, unit);
+        d2 = fminf(d2, dot3_(d, d));
       }
+    }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) d2 = fminf(d2, __shfl_xor_sync(0xffffffffu, d2, o));
-    }
-    if (lane == 0) {
-      const float dmin = sqrtf(d2);
-      bool far = !near && dmin >= a.r_switch;
-      // a far pair with every bead pair beyond every cut-off exerts no force: it is left out of
-      // both the pair list and the far list (2)
-      const bool inert = far && d2 > s_reach2;
-      if (far && a.class_off && a.class_off[dist_class(dmin, a.r_switch)]) far = false;
-      far = far && !inert;
-      a.cand_far[(size_t)i * a.cand_cap + c] = inert ? 2 : (far ? 1 : 0);
-      a.cand_dmin[(size_t)i * a.cand_cap + c] = dmin;
-      my_far += far ? 1 : 0;
-    }
+    for (int o = 16; o > 0; o >>= 1) d2 = fminf(d2, __shfl_xor_sync(0xffffffffu, d2, o));
+    if (lane == 0) a.cand_dmin[(size_t)i * a.cand_cap + c] = d2;  // squared until k_far_decide
   }
-  if (lane == 0) atomicAdd(&s_cnt, my_far);
-  __syncthreads();
-  if (threadIdx.x == 0) a.far_count[i] = s_cnt;
+}
+
+// Warp per subunit i, lane per candidate: the squared closest distance of each candidate pair
+// (from i's own scan for j > i; for j < i from j's scan of i, found by binary search in j's
+// ascending candidate list -- the candidate relation is symmetric), then the decisions: far
+// (closest pair at least the switch radius apart, class not reverted), inert (far with every
+// bead pair beyond every cut-off: in neither list), or near; and i's far-pair count.  dpos is
+// sign-symmetric, so both sides' scans give the same minimum.  A pair missing from j's list
+// (possible only after a candidate-list overflow, which the rebuild repeats) is kept near.
+__global__ void __launch_bounds__(128) k_far_decide(FarArgs a) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 4 + warp;
+  if (i >= a.S) return;
+  const SysParams& P = a.sys[a.sub_sys[i]];
+  // reach of every pair term: the DH cut-off (+inf without one) and the LJ/WCA cut-offs
+  float r2 = P.ecut_el2;
+  for (int k = lane; k < kMaxSpecies * kMaxSpecies; k += 32) r2 = fmaxf(r2, a.pt->cut2[k]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+  const float reach2 = r2 * 1.0001f;
+  const int ncand = a.cand_count[i];
+  int my_far = 0;
+  for (int c = lane; c < ncand; c += 32) {
+    const size_t e = (size_t)i * a.cand_cap + c;
+    const int j = a.cand[e];
+    float d2 = 0.0f;  // i itself: near
+    if (j > i) {
+      d2 = a.cand_dmin[e];
+    } else if (j < i) {
+      const int* cj = a.cand + (size_t)j * a.cand_cap;
+      int lo = 0, hi = a.cand_count[j];
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cj[mid] < i) lo = mid + 1; else hi = mid;
+      }
+      if (lo < a.cand_count[j] && cj[lo] == i) d2 = a.cand_dmin[(size_t)j * a.cand_cap + lo];
+    }
+    const float dmin = sqrtf(d2);
+    bool far = j != i && dmin >= a.r_switch;
+    // a far pair with every bead pair beyond every cut-off exerts no force: it is left out of
+    // both the pair list and the far list (2)
+    const bool inert = far && d2 > reach2;
+    if (far && a.class_off && a.class_off[dist_class(dmin, a.r_switch)]) far = false;
+    far = far && !inert;
+    a.cand_far[e] = inert ? 2 : (far ? 1 : 0);
+    // entries with j <= i take their squared distance here: only entries with j > i are read by
+    // other warps, so the writes and the reads never meet
+    if (j <= i) a.cand_dmin[e] = d2;
+    my_far += far ? 1 : 0;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) my_far += __shfl_xor_sync(0xffffffffu, my_far, o);
+  if (lane == 0) a.far_count[i] = my_far;
 }
 
 // exclusive scan of far_count over all subunits in one CTA of 1024 threads: chunks of 8192
@@ -298,7 +343,7 @@ __global__ void k_far_write(FarArgs a) {
     const size_t e = (size_t)i * a.cand_cap + c;
     if (a.cand_far[e] != 1) continue;
     a.far_pair[k] = make_int2(i, a.cand[e]);
-    a.far_dmin[k] = a.cand_dmin[e];
+    a.far_dmin[k] = sqrtf(a.cand_dmin[e]);  // squared closest distance -> distance
     k++;
   }
 }
@@ -339,42 +384,40 @@ __global__ void __launch_bounds__(128) k_sub_frames(FarArgs a) {
   F.e3 = norm3(cross3_(F.e1, b2));
   F.e2 = cross3_(F.e3, F.e1);
   F.m = m;
-  float alpha[kModes];
+  // per-lane partial sums: v[0..11] the mode amplitudes, v[12..17] the inertia tensor
+  // (xx, yy, zz, xy, xz, yz, off-diagonals negated), the rest zero
+  float v[32];
 #pragma unroll
-  for (int q = 0; q < kModes; q++) alpha[q] = 0.f;
-  float jxx = 0.f, jyy = 0.f, jzz = 0.f, jxy = 0.f, jxz = 0.f, jyz = 0.f;
+  for (int q = 0; q < 32; q++) v[q] = 0.f;
 #pragma unroll
   for (int k = 0; k < kBeadsPerLane; k++) {
     const int l = lane + 32 * k;
     if (l >= np) continue;
     const float3 e = to_body(F, sub3(d[k], m));
-    const float3 u = sub3(e, f3_(a.rest[3 * l], a.rest[3 * l + 1], a.rest[3 * l + 2]));
+    const float4 rl = __ldg(a.rest + l);
+    const float3 u = sub3(e, f3_(rl.x, rl.y, rl.z));
 #pragma unroll
     for (int q = 0; q < kModes; q++) {
-      const float* ph = a.modes + ((size_t)q * np + l) * 3;
-      alpha[q] += ph[0] * u.x + ph[1] * u.y + ph[2] * u.z;
+      const float4 ph = __ldg(a.modes + (size_t)q * np + l);
+      v[q] += ph.x * u.x + ph.y * u.y + ph.z * u.z;
     }
-    jxx += e.y * e.y + e.z * e.z;
-    jyy += e.x * e.x + e.z * e.z;
-    jzz += e.x * e.x + e.y * e.y;
-    jxy -= e.x * e.y;
-    jxz -= e.x * e.z;
-    jyz -= e.y * e.z;
+    v[12] += e.y * e.y + e.z * e.z;
+    v[13] += e.x * e.x + e.z * e.z;
+    v[14] += e.x * e.x + e.y * e.y;
+    v[15] -= e.x * e.y;
+    v[16] -= e.x * e.z;
+    v[17] -= e.y * e.z;
   }
-#pragma unroll
-  for (int q = 0; q < kModes; q++) alpha[q] = wsum(alpha[q]);
-  jxx = wsum(jxx);
-  jyy = wsum(jyy);
-  jzz = wsum(jzz);
-  jxy = wsum(jxy);
-  jxz = wsum(jxz);
-  jyz = wsum(jyz);
+  const float tot = wsum_scatter32(v, lane);  // lane q: sum q
+  float* f = a.frame + (size_t)s * kFrame;
+  if (lane < kModes) f[9 + lane] = tot;
+  const float jxx = __shfl_sync(0xffffffffu, tot, 12), jyy = __shfl_sync(0xffffffffu, tot, 13),
+              jzz = __shfl_sync(0xffffffffu, tot, 14), jxy = __shfl_sync(0xffffffffu, tot, 15),
+              jxz = __shfl_sync(0xffffffffu, tot, 16), jyz = __shfl_sync(0xffffffffu, tot, 17);
   if (lane == 0) {
-    float* f = a.frame + (size_t)s * kFrame;
     f[0] = F.e1.x; f[1] = F.e1.y; f[2] = F.e1.z;
     f[3] = F.e2.x; f[4] = F.e2.y; f[5] = F.e2.z;
     f[6] = F.e3.x; f[7] = F.e3.y; f[8] = F.e3.z;
-    for (int q = 0; q < kModes; q++) f[9 + q] = alpha[q];
     // inverse of the symmetric J by cofactors
     const float c00 = jyy * jzz - jyz * jyz, c01 = jxz * jyz - jxy * jzz, c02 = jxy * jyz - jxz * jyy;
     const float c11 = jxx * jzz - jxz * jxz, c12 = jxy * jxz - jxx * jyz, c22 = jxx * jyy - jxy * jxy;
@@ -782,7 +825,7 @@ struct SurrogateCtx {
   int anchor1 = 0, anchor2 = 0;
   bool enabled = false;
   MlpNorm norm{};  // the attached network's normalisation buffers
-  DevBuf<float> modes, rest;
+  DevBuf<float4> modes, rest;
   DevBuf<unsigned char> cand_far;
   DevBuf<float> cand_dmin, far_dmin, frame, x;
   DevBuf<int> far_count, far_start, far_total, class_off, judge_n, judge_counter;
@@ -873,6 +916,7 @@ FarArgs far_args(souffle_gpu_system* h) {
 void launch_classify(souffle_gpu_system* h, const FarArgs& a) {
   const int np = h->tpl.np;
   k_far_classify<<<h->S, 128, sizeof(int4) * np, h->stream>>>(a);
+  k_far_decide<<<(h->S + 3) / 4, 128, 0, h->stream>>>(a);
   k_far_scan<<<1, 1024, 0, h->stream>>>(a);
 }
 
@@ -1135,12 +1179,17 @@ souffle_status souffle_surrogate_attach(souffle_gpu_system* h, souffle_mlp* net,
   c->far_cap = o.far_capacity;
   c->anchor1 = b1;
   c->anchor2 = b2;
-  std::vector<float> restf(body.begin(), body.end());
+  // one 16-byte entry per (mode, bead) and per bead
+  std::vector<float4> modes4((size_t)kModes * np), rest4(np);
+  for (size_t k = 0; k < modes4.size(); k++)
+    modes4[k] = make_float4(modes[3 * k], modes[3 * k + 1], modes[3 * k + 2], 0.0f);
+  for (int l = 0; l < np; l++)
+    rest4[l] = make_float4((float)body[3 * l], (float)body[3 * l + 1], (float)body[3 * l + 2], 0.0f);
   S_TRY_C(cudaSetDevice(h->opt.device));
-  S_TRY_C(c->modes.alloc(modes.size()));
-  S_TRY_C(cudaMemcpy(c->modes.p, modes.data(), modes.size() * 4, cudaMemcpyHostToDevice));
-  S_TRY_C(c->rest.alloc(restf.size()));
-  S_TRY_C(cudaMemcpy(c->rest.p, restf.data(), restf.size() * 4, cudaMemcpyHostToDevice));
+  S_TRY_C(c->modes.alloc(modes4.size()));
+  S_TRY_C(cudaMemcpy(c->modes.p, modes4.data(), modes4.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  S_TRY_C(c->rest.alloc(rest4.size()));
+  S_TRY_C(cudaMemcpy(c->rest.p, rest4.data(), rest4.size() * sizeof(float4), cudaMemcpyHostToDevice));
   c->norm = mlp_norm(net);
   S_TRY_C(c->cand_far.alloc((size_t)h->S * h->cand_cap));
   S_TRY_C(c->cand_dmin.alloc((size_t)h->S * h->cand_cap));

@@ -233,45 +233,64 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
   int4* c32 = s_own + np;
   unsigned int* cmask = reinterpret_cast<unsigned int*>(c32 + (size_t)a.chunk * np);
   __shared__ int s_cj[kPairChunkMax];
-  __shared__ unsigned char s_cfar[kPairChunkMax];
   __shared__ float s_cR[kPairChunkMax];
   for (int t = threadIdx.x; t < np; t += blockDim.x) s_own[t] = a.pos32[(size_t)i * np + t];
   const bool cta_quirk = p.quirks && i_local == 0;  // every block of the system's subunit 0
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ int s_ctl[3];  // candidates consumed, chunk size, candidate for the per-block path (-1: none)
   int c = 0;
   while (c < ncand) {
     __syncthreads();  // the previous chunk's readers are done
-    if (threadIdx.x < a.chunk) {
-      const int cc = c + threadIdx.x;
+    // Warp 0 looks at the next 32 candidates: far ones (left to the surrogate, or beyond every
+    // cut-off) are skipped; the chunk takes up to a.chunk ordinary candidates before the first
+    // one that needs the per-block path (subunit i itself, or a block with the stale-r2
+    // semantics); with no ordinary candidate before it, that one goes to the per-block path.
+    if (wid == 0) {
+      const int cc = c + lane;
+      const bool valid = cc < ncand;
       int j = -1;
-      unsigned char fl = 0;
-      if (cc < ncand) {
+      bool far = false;
+      if (valid) {
         j = cand[cc];
-        fl = skip_far ? a.cand_far[(size_t)i * a.cand_cap + cc] : 0;
+        far = skip_far && a.cand_far[(size_t)i * a.cand_cap + cc];
       }
-      s_cj[threadIdx.x] = j;
-      s_cfar[threadIdx.x] = fl;
+      const bool slow = valid && !far && (j == i || cta_quirk || (p.quirks && j == p.sub0));
+      const unsigned int sb = __ballot_sync(0xffffffffu, slow);
+      const unsigned int nb = __ballot_sync(0xffffffffu, valid && !far && !slow);
+      const int fs = sb ? __ffs(sb) - 1 : 32;  // first slow lane
+      const unsigned int take = fs < 32 ? nb & ((1u << fs) - 1u) : nb;
+      const int rank = __popc(take & ((1u << lane) - 1u));
+      const bool mine = ((take >> lane) & 1u) && rank < a.chunk;
+      if (mine) s_cj[rank] = j;
+      const int nk = min(__popc(take), a.chunk);
+      int consumed, slow_j = -1;
+      if (__popc(take) > a.chunk) {  // full chunk: up to and including its last candidate
+        const unsigned int last = __ballot_sync(0xffffffffu, mine && rank == a.chunk - 1);
+        consumed = __ffs(last);
+      } else if (fs < 32) {
+        consumed = nk > 0 ? fs : fs + 1;
+        if (nk == 0) slow_j = __shfl_sync(0xffffffffu, j, fs);
+      } else {
+        consumed = min(32, ncand - c);
+      }
+      if (lane == 0) {
+        s_ctl[0] = consumed;
+        s_ctl[1] = nk;
+        s_ctl[2] = slow_j;
+      }
     }
     __syncthreads();
-    // The chunk runs up to the first candidate that takes the per-block path below: subunit i
-    // itself (intra bits) or a block with the stale-r2 semantics.  Far candidates (left to the
-    // surrogate or beyond every cut-off) stay in the chunk with empty masks.
-    int nk = 0;
-    for (; nk < a.chunk; nk++) {
-      const int j = s_cj[nk];
-      if (j < 0) break;
-      if (!s_cfar[nk] && (j == i || cta_quirk || (p.quirks && j == p.sub0))) break;
-    }
+    const int nk = s_ctl[1];
+    const int slow_j = s_ctl[2];
+    c += s_ctl[0];
     if (nk > 0) {
-      c += nk;
       for (int t = threadIdx.x; t < nk * np; t += blockDim.x) {
         const int k = t / np;
-        if (!s_cfar[k]) c32[t] = a.pos32[(size_t)s_cj[k] * np + (t - k * np)];
+        c32[t] = a.pos32[(size_t)s_cj[k] * np + (t - k * np)];
       }
       __syncthreads();
       // each candidate's radius about its centre bead, warp per candidate
       for (int k = wid; k < nk; k += nw) {
-        if (s_cfar[k]) continue;
         const int4 pc = c32[k * np + p.center_local];
         float m = 0.0f;
         for (int t = lane; t < np; t += 32) {
@@ -290,14 +309,11 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
         const int k = t / np, ii = t - k * np;
         unsigned int* mk = cmask + (size_t)t * a.words;
         const int4* cj32 = c32 + k * np;
-        bool skip = s_cfar[k] != 0;
         const int4 pi = s_own[ii];
-        if (!skip) {
-          const int4 pc = cj32[p.center_local];
-          const float reach = s_cR[k] + r_list + eps;
-          const float dx = hi_diff(pi.x, pc.x, unit), dy = hi_diff(pi.y, pc.y, unit), dz = hi_diff(pi.z, pc.z, unit);
-          skip = dx * dx + dy * dy + dz * dz > reach * reach;
-        }
+        const int4 pc = cj32[p.center_local];
+        const float reach = s_cR[k] + r_list + eps;
+        const float ex = hi_diff(pi.x, pc.x, unit), ey = hi_diff(pi.y, pc.y, unit), ez = hi_diff(pi.z, pc.z, unit);
+        const bool skip = ex * ex + ey * ey + ez * ez > reach * reach;
         const int gi = i * np + ii, jbase = s_cj[k] * np;
         for (int w0 = 0; w0 < np; w0 += 32) {
           unsigned int bits = 0;
@@ -345,9 +361,9 @@ __global__ void __launch_bounds__(128) k_pairs(PairArgs a) {
       }
       continue;
     }
-    // per-block path for candidate s_cj[0]
-    const int j = s_cj[0];
-    c += 1;
+    if (slow_j < 0) continue;  // only far candidates in this window
+    // per-block path for candidate slow_j
+    const int j = slow_j;
     __syncthreads();
     if (threadIdx.x == 0) s_Rj = 0.0f;
     for (int t = threadIdx.x; t < np; t += blockDim.x) {

@@ -431,7 +431,12 @@ DriftArgs drift_args(souffle_gpu_system* h) {
   a.py = h->pos_fx.p + N;
   a.pz = h->pos_fx.p + 2 * N;
   a.pos32 = h->pos32.p;
-  a.inter_ids = h->inter_ids.p;
+  // The idle half of each drift CTA brings the force kernel's pair rows into L2 only when the
+  // step's working set (state, forces and about 64 list entries per bead) fits three quarters of
+  // the 129 MB L2; in larger runs the rows would be evicted before the force kernel reads them
+  // and the prefetch only adds DRAM traffic to the drift.
+  const double step_bytes = (double)N * (200.0 + 4.0 * std::min(h->inter_cap, 64));
+  a.inter_ids = step_bytes <= 96.0 * 1024 * 1024 ? h->inter_ids.p : nullptr;
   a.inter_count = h->inter_count.p;
   a.inter_cap = h->inter_cap;
   a.intra_mask = h->intra_mask.p;

@@ -443,7 +443,20 @@ __device__ void far_descr_one(const FarArgs& a, int p) {
   const int2 ab = a.far_pair[p];
   const int np = a.np;
   const SysParams& P = a.sys[a.sub_sys[ab.x]];
-  const Frame FA = load_frame(a.frame + (size_t)ab.x * kFrame), FB = load_frame(a.frame + (size_t)ab.y * kFrame);
+  // both frames with 16-byte loads (36 floats = 9 float4 per subunit, 144-byte aligned rows)
+  float4 ra[kFrame / 4], rb[kFrame / 4];
+  {
+    const float4* pa = reinterpret_cast<const float4*>(a.frame + (size_t)ab.x * kFrame);
+    const float4* pb = reinterpret_cast<const float4*>(a.frame + (size_t)ab.y * kFrame);
+#pragma unroll
+    for (int k = 0; k < kFrame / 4; k++) {
+      ra[k] = __ldg(pa + k);
+      rb[k] = __ldg(pb + k);
+    }
+  }
+  const float* fa = reinterpret_cast<const float*>(ra);
+  const float* fb = reinterpret_cast<const float*>(rb);
+  const Frame FA = load_frame(fa), FB = load_frame(fb);
   const float3 R = add3(dpos(a.pos32[(size_t)ab.y * np + P.center_local], a.pos32[(size_t)ab.x * np + P.center_local],
                              P.unit32),
                         sub3(FB.m, FA.m));
@@ -476,8 +489,6 @@ __device__ void far_descr_one(const FarArgs& a, int p) {
   x[3] = r; x[4] = 1.0f / r; x[5] = expf(-P.kappa * (r - 8.0f)) / r;
   x[6] = qw; x[7] = qx; x[8] = qy; x[9] = qz;
   x[10] = RB.x; x[11] = RB.y; x[12] = RB.z;
-  const float* fa = a.frame + (size_t)ab.x * kFrame;
-  const float* fb = a.frame + (size_t)ab.y * kFrame;
 #pragma unroll
   for (int q = 0; q < kModes; q++) {
     x[13 + q] = fa[9 + q];

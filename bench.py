@@ -302,7 +302,7 @@ def bench_surrogate(args):
     n_out = 6 + 3 * np_
     far_cap = max(4096, args.far_per_subunit * int(w.opt.S))
     batch = 4096
-    net = gpu.Mlp(64, n_out, max_batch=max(far_cap, batch), seed=7)
+    net = gpu.Mlp(64, n_out, max_batch=max(far_cap, batch), seed=7, width=getattr(args, "net_width", 128))
     gpu.surrogate_attach(s, net, w.template.pos, far_capacity=far_cap)
     B = int(w.opt.B)
     # training data: exact far-pair forces along the plain trajectory, one frame per rebuild window
@@ -482,7 +482,7 @@ def surrogate_batched(args):
     n_out = 6 + 3 * np_
     far_cap = max(4096, args.far_per_subunit * S_tot)
     batch = 4096
-    net = gpu.Mlp(64, n_out, max_batch=max(far_cap, batch), seed=7)
+    net = gpu.Mlp(64, n_out, max_batch=max(far_cap, batch), seed=7, width=getattr(args, "net_width", 128))
     gpu.surrogate_attach(s, net, tpl.pos, far_capacity=far_cap)
     ext = torch.cuda.ExternalStream(s.stream())
 
@@ -651,6 +651,7 @@ def surrogate_batched(args):
         "gain": surr["value"] / plain_value,
         "gain_batching": batched["value"] / plain_value,
         "gain_surrogate": surr["value"] / batched["value"],
+        "net_width": getattr(args, "net_width", 128),
         "plain": {"value": plain_value, "replicas_timed": len(sample), "beads_timed": plain_beads,
                   "ms_total": plain_ms},
         "batched": batched, "surrogate": surr,
@@ -669,8 +670,8 @@ def surrogate_batched(args):
 
 
 def bench_gemm(args):
-    """The surrogate network's forward pass (64 -> 256 -> 256 -> 256 -> 132, BF16 operands, FP32
-    accumulation) at several row counts through the C ABI: the fused one-kernel forward
+    """The surrogate network's forward pass (64 -> w -> w -> w -> 132, w = --net-width, BF16
+    operands, FP32 accumulation) at several row counts through the C ABI: the fused one-kernel forward
     (souffle_mlp_forward) and the per-layer GEMMs (souffle_mlp_forward_layered).  us_per_call:
     CUDA events on the network's stream around the C call (input packing, the forward, output
     unpadding, host gaps between them); us_per_forward: the forward kernels alone, back to back
@@ -685,12 +686,13 @@ def bench_gemm(args):
         pass
     peak = float(peaks.get("bf16_tflops", 1900.0))
     rows = []
+    w = args.net_width
     for m in (8192, 32768, 118016, 524288):
-        net = gpu.Mlp(64, 132, max_batch=m, seed=1)
+        net = gpu.Mlp(64, 132, max_batch=m, seed=1, width=w)
         ext = torch.cuda.ExternalStream(net.stream())
         x = torch.randn(m, 64, device="cuda")
         y = torch.empty(m, 132, device="cuda")
-        flop = 2.0 * m * (64 * 256 + 2 * 256 * 256 + 256 * 144)
+        flop = 2.0 * m * (64 * w + 2 * w * w + w * 144)
         row = {"rows": m}
         for name, fn in (("fused", net.forward), ("layered", net.forward_layered)):
             for _ in range(3):
@@ -714,7 +716,7 @@ def bench_gemm(args):
         "metric": "surrogate network forward TFLOP/s", "value": best["tflops"], "unit": "TFLOP/s",
         "n_gpus": 1, "steps": args.steps, "warmup": 3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic",
-        "config": {"workload": "surrogate MLP 64-256-256-256-132 forward at 118,016 rows, padded output 144"},
+        "config": {"workload": f"surrogate MLP 64-{w}-{w}-{w}-132 forward at 118,016 rows, padded output 144"},
         "per_rows": rows,
         "roofline": {"bound": "tensor", "achieved": best["tflops"], "peak": peak, "unit": "TFLOP/s",
                      "frac": best["tflops"] / peak,
@@ -959,6 +961,9 @@ def main():
                     help="with --replicas --surrogate: replicas timed alone for the plain path")
     ap.add_argument("--far-per-subunit", type=int, default=4,
                     help="surrogate far-pair list capacity per subunit")
+    ap.add_argument("--net-width", type=int, default=128, choices=(128, 256),
+                    help="hidden width of the surrogate network (128: 65 us per 118k-row forward at a "
+                         "force error of ~1.2e-5; 256: 100 us at ~1.1e-5)")
     args = ap.parse_args()
     if args.gemm:
         return bench_gemm(args)
@@ -1194,13 +1199,15 @@ def main():
         try:
             sb = surrogate_batched(argparse.Namespace(
                 replicas=256, far_per_subunit=16, steps=100, stat_steps=3000, plain_sample=64, profile=False,
-                train_rows=args.train_rows, max_frames=args.max_frames, epochs=args.epochs))
+                train_rows=args.train_rows, max_frames=args.max_frames, epochs=args.epochs,
+                net_width=args.net_width))
             out["surrogate_batched"] = {k: sb[k] for k in (
                 "metric", "value", "unit", "gain", "gain_batching", "gain_surrogate", "config",
                 "force_rms_rel_error", "force_rms_rel_error_worst_system", "far_pairs")}
             out["surrogate_batched"]["plain_value"] = sb["plain"]["value"]
             out["surrogate_batched"]["batched_value"] = sb["batched"]["value"]
             out["surrogate_batched"]["judge"] = sb["surrogate"]["judge"]
+            out["surrogate_batched"]["net_width"] = args.net_width
             out["surrogate_batched"]["statistics"] = sb["statistics"]
         except Exception as ex:  # the main line stands on its own
             out["surrogate_batched"] = {"error": f"{type(ex).__name__}: {ex}"}

@@ -1,4 +1,4 @@
-// The surrogate network: n_in -> 256 -> 256 -> 256 -> n_out with SiLU, trained and evaluated with
+// The surrogate network: n_in -> w -> w -> w -> n_out (w = 128 or 256) with SiLU, trained and evaluated with
 // the tcgen05 GEMM (gemm.cu).  Parameters live as FP32 masters plus BF16 copies W [out][in] (the
 // forward B operand) and W^T [in][out] (the backward B operand); activations are BF16, kept both
 // row-major (next forward A operand) and transposed (A/B operands of the weight-gradient GEMMs,
@@ -26,7 +26,7 @@
 namespace souffle {
 void record_error(const std::string& msg);
 bool mlp_fused_supported(int n_in, int width, int out_pad);
-cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const int* m_dyn, int n_in,
+cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const int* m_dyn, int n_in, int width,
                               const __nv_bfloat16* const w[4], const int ldw[4], int out_pad, const float* const bias[4],
                               float* y, int ldy, unsigned int* err, unsigned int err_bit, cudaStream_t st,
                               __nv_bfloat16* yb = nullptr);
@@ -338,7 +338,7 @@ bool mlp_forward_packed_bf16_async(souffle_mlp* h, int m_cap, const int* m_dyn, 
   const __nv_bfloat16* w[4] = {h->wb[0].p, h->wb[1].p, h->wb[2].p, h->wb[3].p};
   const int ldw[4] = {h->in[0], h->in[1], h->in[2], h->in[3]};
   const float* b[4] = {h->b[0].p, h->b[1].p, h->b[2].p, h->b[3].p};
-  *r = mlp_forward_fused(h->act[0].p, h->in_ld[0], m_cap, m_dyn, h->n_in, w, ldw, h->out_pad[L], b, nullptr,
+  *r = mlp_forward_fused(h->act[0].p, h->in_ld[0], m_cap, m_dyn, h->n_in, h->width, w, ldw, h->out_pad[L], b, nullptr,
                          h->out_pad[L], err, kErrSurrogateBit, st, h->yb.p);
   *yb = h->yb.p;
   *ldy = h->out_pad[L];
@@ -362,7 +362,7 @@ cudaError_t mlp_forward_packed_async(souffle_mlp* h, int m_cap, const int* m_dyn
     const __nv_bfloat16* w[4] = {h->wb[0].p, h->wb[1].p, h->wb[2].p, h->wb[3].p};
     const int ldw[4] = {h->in[0], h->in[1], h->in[2], h->in[3]};
     const float* b[4] = {h->b[0].p, h->b[1].p, h->b[2].p, h->b[3].p};
-    r = mlp_forward_fused(h->act[0].p, h->in_ld[0], m_cap, m_dyn, h->n_in, w, ldw, h->out_pad[L], b, h->y.p,
+    r = mlp_forward_fused(h->act[0].p, h->in_ld[0], m_cap, m_dyn, h->n_in, h->width, w, ldw, h->out_pad[L], b, h->y.p,
                           h->out_pad[L], err, kErrSurrogateBit, st);
   } else {
     r = forward_on(h, m_cap, false, st, m_dyn, err, kErrSurrogateBit);
@@ -390,10 +390,10 @@ souffle_status souffle_mlp_create(int32_t n_in, int32_t width, int32_t n_out, in
                                   int32_t device, souffle_mlp** out) {
   if (!out) return fail(SOUFFLE_ERR_BAD_INPUT, "null output");
   *out = nullptr;
-  if (n_in < 8 || n_in > 256 || n_in % 8 || width != 256 || n_out < 1 || n_out > 256 || max_batch < 1 ||
+  if (n_in < 8 || n_in > 256 || n_in % 8 || (width != 128 && width != 256) || n_out < 1 || n_out > 256 || max_batch < 1 ||
       max_batch > (1 << 22))
     return fail(SOUFFLE_ERR_BAD_INPUT,
-                "mlp shape: n_in a multiple of 8 up to 256, 1 <= n_out <= 256, width 256, 1 <= max_batch <= 2^22");
+                "mlp shape: n_in a multiple of 8 up to 256, 1 <= n_out <= 256, width 128 or 256, 1 <= max_batch <= 2^22");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SOUFFLE_ERR_NO_DEVICE, "no CUDA device");
   if (device < 0 || device >= ndev) return fail(SOUFFLE_ERR_BAD_INPUT, "bad device");
@@ -557,7 +557,7 @@ souffle_status souffle_mlp_profile_forward(souffle_mlp* h, int32_t m, int32_t it
   const int ldw[4] = {h->in[0], h->in[1], h->in[2], h->in[3]};
   const float* b[4] = {h->b[0].p, h->b[1].p, h->b[2].p, h->b[3].p};
   auto run = [&]() {
-    return fused ? mlp_forward_fused(h->act[0].p, h->in_ld[0], m, nullptr, h->n_in, w, ldw, h->out_pad[L], b, h->y.p,
+    return fused ? mlp_forward_fused(h->act[0].p, h->in_ld[0], m, nullptr, h->n_in, h->width, w, ldw, h->out_pad[L], b, h->y.p,
                                      h->out_pad[L], h->err.p, 1u, h->stream)
                  : forward_on(h, m, false, h->stream, nullptr, h->err.p);
   };

@@ -1,5 +1,5 @@
-// The surrogate network's whole forward pass (n_in <= 64 -> 256 -> 256 -> 256 -> out_pad, SiLU on
-// the hidden layers) in one persistent tcgen05 kernel: a 128-row tile's activations never leave
+// The surrogate network's whole forward pass (n_in <= 64 -> w -> w -> w -> out_pad, w = 128 or
+// 256, SiLU on the hidden layers) in one persistent tcgen05 kernel: a 128-row tile's activations never leave
 // the SM between layers.
 //
 // One CTA per SM (320 threads, 10 warps), looping over 128-row tiles.  Two tiles are in flight
@@ -41,7 +41,7 @@ namespace {
 
 constexpr int kFRows = 128;                   // tile rows = MMA M
 constexpr int kFK = 64;                       // K per chunk / stage (128 bytes of BF16)
-constexpr int kFWidth = 256;                  // hidden width
+constexpr int kFWidth = 256;                  // largest hidden width (buffers and bias slots are sized for it)
 constexpr int kFChunk = kFRows * kFK * 2;     // 16 KB: one K-chunk of a tile, or one weight stage
 constexpr int kFAct = kFWidth / kFK * kFChunk;  // 64 KB activation buffer per slot
 constexpr int kFStages = 5;
@@ -58,6 +58,7 @@ struct FusedArgs {
   int m_cap;            // rows of the input / output buffers
   const int* m_dyn;     // live rows (device), or null = m_cap
   int n_in;             // <= 64
+  int width;            // hidden width: 128 or 256
   int out_pad;          // output columns computed and stored (multiple of 16, <= 256)
   const float* bias[4];  // [256] x 3, [out_pad]
   float* y;             // [m_cap][ldy] FP32, or
@@ -93,8 +94,10 @@ __device__ __forceinline__ bool fwait(uint32_t bar, uint32_t parity, volatile in
 }
 
 // output columns of the layer: stage parts of up to 128 rows (the last may be narrower)
-__device__ __forceinline__ int layer_n(int l, int out_pad) { return l == 3 ? out_pad : kFWidth; }
-__device__ __forceinline__ int layer_k_chunks(int l, int n_in) { return l == 0 ? (n_in + kFK - 1) / kFK : kFWidth / kFK; }
+__device__ __forceinline__ int layer_n(int l, int out_pad, int width) { return l == 3 ? out_pad : width; }
+__device__ __forceinline__ int layer_k_chunks(int l, int n_in, int width) {
+  return l == 0 ? (n_in + kFK - 1) / kFK : width / kFK;
+}
 
 }  // namespace
 
@@ -154,7 +157,9 @@ __global__ void __launch_bounds__(kFThreads, 1)
   // biases: half of each hidden bias (SiLU works on z / 2), the output bias as it is
   for (int t = threadIdx.x; t < kFBias; t += blockDim.x) {
     float v = 0.f;
-    if (t < 3 * kFWidth) v = 0.5f * a.bias[t / kFWidth][t % kFWidth];
+    if (t < 3 * kFWidth) {
+      if (t % kFWidth < a.width) v = 0.5f * a.bias[t / kFWidth][t % kFWidth];
+    }
     else if (t - 3 * kFWidth < a.out_pad) v = a.bias[3][t - 3 * kFWidth];
     s_bias[t] = v;
   }
@@ -186,7 +191,7 @@ __global__ void __launch_bounds__(kFThreads, 1)
               tma_load_2d(act0 + s * kFAct, &tx, 0, tile * kFRows, xfull0 + 8 * s);
               xs[s]++;
             }
-            const int nk = layer_k_chunks(l, a.n_in), parts = (layer_n(l, a.out_pad) + 127) / 128;
+            const int nk = layer_k_chunks(l, a.n_in, a.width), parts = (layer_n(l, a.out_pad, a.width) + 127) / 128;
             for (int kc = 0; kc < nk && ok; kc++) {
               for (int part = 0; part < parts; part++, g++) {
                 const int st = g % kFStages;
@@ -234,8 +239,8 @@ __global__ void __launch_bounds__(kFThreads, 1)
               break;
             }
             tc_fence_after();
-            const int n = layer_n(l, a.out_pad);
-            const int nk = layer_k_chunks(l, a.n_in), parts = (n + 127) / 128;
+            const int n = layer_n(l, a.out_pad, a.width);
+            const int nk = layer_k_chunks(l, a.n_in, a.width), parts = (n + 127) / 128;
             const uint32_t acc = tmem + (uint32_t)(s * kFWidth);
             const uint32_t abuf = act0 + s * kFAct;
             for (int kc = 0; kc < nk && ok; kc++) {
@@ -289,12 +294,12 @@ __global__ void __launch_bounds__(kFThreads, 1)
           tc_fence_after();
           const uint32_t t_row = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(s * kFWidth);
           if (l < 3) {
-            // hidden layer: columns [128 half, 128 half + 128) -> SiLU -> BF16 into the buffer
+            // hidden layer: columns [half w/2, (half + 1) w/2) -> SiLU -> BF16 into the buffer
             const float* hb = s_bias + l * kFWidth;
             const uint32_t abuf = act0 + s * kFAct;
             const uint32_t rsw = (uint32_t)(r_local & 7);
 #pragma unroll 1
-            for (int c0 = half * 128; c0 < half * 128 + 128; c0 += 32) {
+            for (int c0 = half * (a.width >> 1); c0 < (half + 1) * (a.width >> 1); c0 += 32) {
               float v[32];
               tmem_ld32(t_row + (uint32_t)c0, v);
               uint32_t pk[16];
@@ -418,17 +423,17 @@ bool fused_map(CUtensorMap* m, const void* p, int rows, int cols, int ld) {
 }  // namespace
 
 bool mlp_fused_supported(int n_in, int width, int out_pad) {
-  return n_in >= 8 && n_in <= kFK && n_in % 8 == 0 && width == kFWidth && out_pad >= 16 && out_pad <= kFMaxOut &&
-         out_pad % 16 == 0;
+  return n_in >= 8 && n_in <= kFK && n_in % 8 == 0 && (width == 128 || width == kFWidth) && out_pad >= 16 &&
+         out_pad <= kFMaxOut && out_pad % 16 == 0;
 }
 
-cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const int* m_dyn, int n_in,
+cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const int* m_dyn, int n_in, int width,
                               const __nv_bfloat16* const w[4], const int ldw[4], int out_pad, const float* const bias[4],
                               float* y, int ldy, unsigned int* err, unsigned int err_bit, cudaStream_t st,
                               __nv_bfloat16* yb) {
-  if (!mlp_fused_supported(n_in, kFWidth, out_pad) || m_cap < 1 || !x || !(y || yb) || !err || ldx < n_in || ldx % 8 ||
-      ldy < out_pad || (reinterpret_cast<uintptr_t>(x) & 15) || ldw[0] < n_in || ldw[1] < kFWidth ||
-      ldw[2] < kFWidth || ldw[3] < kFWidth)
+  if (!mlp_fused_supported(n_in, width, out_pad) || m_cap < 1 || !x || !(y || yb) || !err || ldx < n_in || ldx % 8 ||
+      ldy < out_pad || (reinterpret_cast<uintptr_t>(x) & 15) || ldw[0] < n_in || ldw[1] < width ||
+      ldw[2] < width || ldw[3] < width)
     return cudaErrorInvalidValue;
   for (int l = 0; l < 4; l++)
     if (!w[l] || !bias[l] || ldw[l] % 8 || (reinterpret_cast<uintptr_t>(w[l]) & 15)) return cudaErrorInvalidValue;
@@ -439,9 +444,9 @@ cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const 
   });
   if (attr != cudaSuccess) return attr;
   CUtensorMap tx, tw[4];
-  if (!fused_map(&tx, x, m_cap, n_in, ldx) || !fused_map(&tw[0], w[0], kFWidth, n_in, ldw[0]) ||
-      !fused_map(&tw[1], w[1], kFWidth, kFWidth, ldw[1]) || !fused_map(&tw[2], w[2], kFWidth, kFWidth, ldw[2]) ||
-      !fused_map(&tw[3], w[3], out_pad, kFWidth, ldw[3]))
+  if (!fused_map(&tx, x, m_cap, n_in, ldx) || !fused_map(&tw[0], w[0], width, n_in, ldw[0]) ||
+      !fused_map(&tw[1], w[1], width, width, ldw[1]) || !fused_map(&tw[2], w[2], width, width, ldw[2]) ||
+      !fused_map(&tw[3], w[3], out_pad, width, ldw[3]))
     return cudaErrorInvalidValue;
   static int sms = 0;
   static std::once_flag once_sm;
@@ -454,6 +459,7 @@ cudaError_t mlp_forward_fused(const __nv_bfloat16* x, int ldx, int m_cap, const 
   a.m_cap = m_cap;
   a.m_dyn = m_dyn;
   a.n_in = n_in;
+  a.width = width;
   a.out_pad = out_pad;
   for (int l = 0; l < 4; l++) a.bias[l] = bias[l];
   a.y = yb ? nullptr : y;

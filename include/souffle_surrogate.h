@@ -23,8 +23,8 @@ extern "C" {
 
 typedef struct souffle_mlp souffle_mlp;
 
-/* n_in a multiple of 8 up to 256, n_out at most 256, width 256 (the hidden layers are one 256-wide tensor-core tile),
- * max_batch rows per call (rounded up to 128 internally).  Weights are initialised from seed
+/* n_in a multiple of 8 up to 256, n_out at most 256, width 128 or 256 (a hidden layer is one or two 128-wide
+ * tensor-core tiles), max_batch rows per call (rounded up to 128 internally).  Weights are initialised from seed
  * (uniform, +-sqrt(3 / fan_in)), biases zero. */
 souffle_status souffle_mlp_create(int32_t n_in, int32_t width, int32_t n_out, int32_t max_batch, uint64_t seed,
                                   int32_t device, souffle_mlp** out);

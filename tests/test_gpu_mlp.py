@@ -38,39 +38,41 @@ def test_gemm_matches_numpy(m, n, k):
     assert np.all(err <= (k * 1.2e-7 + 1e-6) * scale + 1e-30), err.max()
 
 
-def _setup(m, seed):
+def _setup(m, seed, width=WIDTH):
     torch = _torch()
     from souffle_gb300 import gpu
-    net = gpu.Mlp(N_IN, N_OUT, max_batch=1024, seed=seed)
+    net = gpu.Mlp(N_IN, N_OUT, max_batch=1024, seed=seed, width=width)
     rng = np.random.default_rng(seed)
     x = rng.normal(0, 1, (m, N_IN)).astype(np.float32)
     t = rng.normal(0, 0.5, (m, N_OUT)).astype(np.float32)
     return torch, net, x, t
 
 
+@pytest.mark.parametrize("width", [128, 256])
 @pytest.mark.parametrize("m", [128, 300])
-def test_forward_matches_oracle(m):
-    torch, net, x, _ = _setup(m, 3)
+def test_forward_matches_oracle(m, width):
+    torch, net, x, _ = _setup(m, 3, width)
     p = net.get_params()
     xd = torch.from_numpy(x).cuda()
     y = torch.empty(m, N_OUT, device="cuda")
     net.forward(xd.data_ptr(), m, y.data_ptr())
     torch.cuda.synchronize()
-    ref = M.forward(p, x, N_IN, WIDTH, N_OUT, emulate=True)
+    ref = M.forward(p, x, N_IN, width, N_OUT, emulate=True)
     err = np.abs(y.cpu().numpy() - ref).max()
     assert err <= 2e-2 * np.abs(ref).max(), err
 
 
+@pytest.mark.parametrize("width", [128, 256])
 @pytest.mark.parametrize("m", [128, 300])
-def test_gradients_match_oracle(m):
-    torch, net, x, t = _setup(m, 5)
+def test_gradients_match_oracle(m, width):
+    torch, net, x, t = _setup(m, 5, width)
     p = net.get_params()
     xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
     loss, g = net.gradients(xd.data_ptr(), td.data_ptr(), m)
-    ref_loss, ref_g = M.loss_and_grads(p, x, t, N_IN, WIDTH, N_OUT, emulate=True)
+    ref_loss, ref_g = M.loss_and_grads(p, x, t, N_IN, width, N_OUT, emulate=True)
     assert loss == pytest.approx(ref_loss, rel=1e-4)
     k = 0
-    for (ws, bs) in M.shapes(N_IN, WIDTH, N_OUT):
+    for (ws, bs) in M.shapes(N_IN, width, N_OUT):
         for size in (ws[0] * ws[1], bs[0]):
             a, b = g[k:k + size], ref_g[k:k + size]
             assert np.linalg.norm(a - b) <= 1e-2 * np.linalg.norm(b) + 1e-12, (k, size)
@@ -95,15 +97,17 @@ def test_training_fits_a_smooth_map():
     assert np.mean((y.cpu().numpy() - t) ** 2) == pytest.approx(last, rel=0.3)
 
 
+@pytest.mark.parametrize("width", [128, 256])
 @pytest.mark.parametrize("m", [1, 129, 300, 152 * 128 * 3 + 77])
-def test_fused_forward_matches_oracle_and_layered(m):
+def test_fused_forward_matches_oracle_and_layered(m, width):
     """The one-kernel forward (activations on chip, SiLU from a hardware tanh) against the CPU
     restatement, and against the per-layer GEMMs: both round to BF16 at the same points, so they
     differ only where the SiLU approximations put a value on the other side of a BF16 rounding
-    boundary.  The largest case gives every CTA several tiles and an odd tile count."""
+    boundary.  The largest case gives every CTA several tiles and an odd tile count; both hidden
+    widths the kernel supports."""
     torch = _torch()
     from souffle_gb300 import gpu
-    gpu_net = gpu.Mlp(N_IN, N_OUT, max_batch=max(m, 1024), seed=11)
+    gpu_net = gpu.Mlp(N_IN, N_OUT, max_batch=max(m, 1024), seed=11, width=width)
     rng = np.random.default_rng(m)
     x = rng.normal(0, 1, (m, N_IN)).astype(np.float32)
     p = gpu_net.get_params()
@@ -116,7 +120,7 @@ def test_fused_forward_matches_oracle_and_layered(m):
     yf, yl = y.cpu().numpy(), yl.cpu().numpy()
     assert np.all(np.isfinite(yf))
     rows = np.arange(m) if m <= 2048 else np.random.default_rng(1).choice(m, 2048, replace=False)
-    ref = M.forward(p, x[rows], N_IN, WIDTH, N_OUT, emulate=True)
+    ref = M.forward(p, x[rows], N_IN, width, N_OUT, emulate=True)
     assert np.abs(yf[rows] - ref).max() <= 2e-2 * np.abs(ref).max()
     # fused against layered: RMS of the difference within 1 % of the RMS output
     assert np.sqrt(np.mean((yf - yl) ** 2)) <= 1e-2 * np.sqrt(np.mean(yl ** 2))

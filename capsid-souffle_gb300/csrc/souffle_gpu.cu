@@ -881,6 +881,65 @@ souffle_status souffle_gpu_get_state(souffle_gpu_system* h, double* pos, double*
   return SOUFFLE_OK;
 }
 
+souffle_status souffle_gpu_snapshot_enqueue(souffle_gpu_system* h, int32_t slot, double* pos, double* vel) {
+  if (!h || slot < 0 || slot > 1) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  if (!h->have_state) return fail(SOUFFLE_ERR_STATE, "no state set");
+  if (h->snap_pending[slot]) return fail(SOUFFLE_ERR_STATE, "snapshot slot still pending: wait for it first");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  const int64_t N = h->N;
+  if (!h->snap[slot].p) CUDA_TRY(h->snap[slot].alloc(6 * N));
+  if (!h->snap_err) {
+    CUDA_TRY(cudaMallocHost(&h->snap_err, 2 * sizeof(unsigned int)));
+    h->snap_err[0] = h->snap_err[1] = 0;
+  }
+  if (!h->snap_ev[slot]) CUDA_TRY(cudaEventCreateWithFlags(&h->snap_ev[slot], cudaEventDisableTiming));
+  StateArgs a{};
+  a.sys = h->d_sys.p;
+  a.state = h->d_state.p;
+  a.bead_sys = h->d_bead_sys.p;
+  a.np = h->tpl.np;
+  a.n = (int)N;
+  a.px = h->pos_fx.p;
+  a.py = h->pos_fx.p + N;
+  a.pz = h->pos_fx.p + 2 * N;
+  a.vx = h->vel.p;
+  a.vy = h->vel.p + N;
+  a.vz = h->vel.p + 2 * N;
+  a.pos_out = pos ? h->snap[slot].p : nullptr;
+  a.vel_out = vel ? h->snap[slot].p + 3 * N : nullptr;
+  launch_state_out(a, (int)((N + 255) / 256), 256, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  if (pos) CUDA_TRY(cudaMemcpyAsync(pos, h->snap[slot].p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->stream));
+  if (vel)
+    CUDA_TRY(cudaMemcpyAsync(vel, h->snap[slot].p + 3 * N, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost,
+                             h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->snap_err + slot, h->err.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaEventRecord(h->snap_ev[slot], h->stream));
+  h->snap_pending[slot] = true;
+  return SOUFFLE_OK;
+}
+
+souffle_status souffle_gpu_snapshot_wait(souffle_gpu_system* h, int32_t slot) {
+  if (!h || slot < 0 || slot > 1) return fail(SOUFFLE_ERR_BAD_INPUT, "bad argument");
+  if (!h->snap_pending[slot]) return fail(SOUFFLE_ERR_STATE, "no snapshot queued in this slot");
+  CUDA_TRY(cudaSetDevice(h->opt.device));
+  h->snap_pending[slot] = false;
+  CUDA_TRY(cudaEventSynchronize(h->snap_ev[slot]));
+  // errors of the work queued before the snapshot: the full check (it also clears the flag)
+  if (h->snap_err[slot]) return check_err(h);
+  return SOUFFLE_OK;
+}
+
+void* souffle_gpu_host_alloc(int64_t bytes) {
+  void* p = nullptr;
+  if (bytes <= 0 || cudaMallocHost(&p, (size_t)bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void souffle_gpu_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
 static souffle_status copy_force_out(souffle_gpu_system* h, const float* dev3, double* host) {
   // device float SoA [3][N] -> host double xyz interleaved
   const int64_t N = h->N;

@@ -84,6 +84,12 @@ struct souffle_gpu_system {
   DevBuf<int> e_cells;  // the energy pass's cell grid: count, start, fill (3 nc^3 + 1), beads, bead cells (2 n)
   DevBuf<unsigned int> err;
   unsigned int* err_host = nullptr;  // pinned landing word for the error flag's read-back
+  // asynchronous snapshots (souffle_gpu_snapshot_enqueue / _wait): per slot a device copy of the
+  // state in double, the error flag as it was behind the copy, and the event that marks it
+  DevBuf<double> snap[2];
+  unsigned int* snap_err = nullptr;  // pinned [2]
+  cudaEvent_t snap_ev[2] = {nullptr, nullptr};
+  bool snap_pending[2] = {false, false};
   // Brownian systems: per system and template bead drag (2^40 units) and noise scale, the
   // generator skip-ahead table, the step's drag and random forces
   bool any_brownian = false;
@@ -104,6 +110,9 @@ struct souffle_gpu_system {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
     souffle::surrogate_free(sur);
     if (err_host) cudaFreeHost(err_host);
+    if (snap_err) cudaFreeHost(snap_err);
+    for (auto& e : snap_ev)
+      if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
   }
 };

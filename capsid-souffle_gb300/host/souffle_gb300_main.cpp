@@ -522,27 +522,38 @@ int run_simulation(const Options& o) {
   energy_row(0, false);  // row 0 before the loop (src/md.cpp:339-346)
 
   ofstream rs;  // one stream object for every restart file, as src/md.cpp:104
-  const double loop_end = (totaltime / o.t) + 1;  // src/md.cpp:387
-  long a = loopStart;
-  double pre = -1;
-  while (a < loop_end) {
-    // advance to the next step that writes anything (inclusive)
-    long next = a;
-    while (next + 1 < loop_end && !(next % o.w == 0 || next % o.W == 0 || next % o.M == 0)) next++;
-    check(souffle_gpu_md_steps(h, a, (int)(next - a + 1)), "souffle_gpu_md_steps");
-    a = next;
-    if (a % o.w == 0 || a % o.M == 0) check(souffle_gpu_get_state(h, pos.data(), vel.data()), "souffle_gpu_get_state");
-    if (a % o.w == 0) {
-      rs.open(("outfiles/restart_" + to_string(a) + ".out").c_str(), ios::out);
-      rs << "Velocities & Positions for " << a << endl;
+  // Output pipeline: the state of an output step is read back asynchronously into one of two
+  // page-locked buffers while the next window of steps is already queued behind it, and its
+  // restart and movie files are written while the GPU runs that window.  Energy rows are computed
+  // at their step (a blocking call) after the previous step's files are written; the movie's
+  // per-bead bending energies are those of the last energy row, as in the reference.
+  double* snap_pos[2] = {nullptr, nullptr};
+  double* snap_vel[2] = {nullptr, nullptr};
+  for (int k = 0; k < 2; k++) {
+    snap_pos[k] = static_cast<double*>(souffle_gpu_host_alloc((int64_t)sizeof(double) * 3 * N));
+    snap_vel[k] = static_cast<double*>(souffle_gpu_host_alloc((int64_t)sizeof(double) * 3 * N));
+    if (!snap_pos[k] || !snap_vel[k]) {
+      cerr << "souffle_gb300: page-locked host buffers for the output could not be allocated" << endl;
+      exit(1);
+    }
+  }
+  struct Pending {
+    bool active = false;
+    long a = 0;
+    int slot = 0;
+  } pending;
+  auto write_outputs = [&](long at, const double* P, const double* V) {
+    if (at % o.w == 0) {
+      rs.open(("outfiles/restart_" + to_string(at) + ".out").c_str(), ios::out);
+      rs << "Velocities & Positions for " << at << endl;
       for (long i = 0; i < N; i++)
-        rs << i << "  " << vel[3 * i] << setw(25) << setprecision(12) << vel[3 * i + 1] << setw(25)
-           << setprecision(12) << vel[3 * i + 2] << setw(25) << setprecision(12) << pos[3 * i] << setw(25)
-           << setprecision(12) << pos[3 * i + 1] << setw(25) << setprecision(12) << pos[3 * i + 2] << setw(25)
+        rs << i << "  " << V[3 * i] << setw(25) << setprecision(12) << V[3 * i + 1] << setw(25)
+           << setprecision(12) << V[3 * i + 2] << setw(25) << setprecision(12) << P[3 * i] << setw(25)
+           << setprecision(12) << P[3 * i + 1] << setw(25) << setprecision(12) << P[3 * i + 2] << setw(25)
            << setprecision(12) << endl;
       rs.close();
       if (o.p) {
-        rs.open(("outfiles/rb_" + to_string(a) + ".out").c_str(), ios::out);
+        rs.open(("outfiles/rb_" + to_string(at) + ".out").c_str(), ios::out);
         for (int i = 0; i < n_big; i++)
           rs << big_vel[3 * i] << setw(25) << setprecision(12) << big_vel[3 * i + 1] << setw(25) << setprecision(12)
              << big_vel[3 * i + 2] << setw(25) << setprecision(12) << big_pos[3 * i] << setw(25) << setprecision(12)
@@ -551,18 +562,44 @@ int run_simulation(const Options& o) {
         rs.close();
       }
     }
-    if (a % o.W == 0) energy_row(a, true);
-    if (a % o.M == 0) {
-      ofile << "ITEM: TIMESTEP" << endl << a << endl << "ITEM: NUMBER OF ATOMS" << endl << N + n_big << endl
+    if (at % o.M == 0) {
+      ofile << "ITEM: TIMESTEP" << endl << at << endl << "ITEM: NUMBER OF ATOMS" << endl << N + n_big << endl
             << "ITEM: BOX BOUNDS" << endl << -box_x / 2 << setw(15) << box_x / 2 << endl << -box_x / 2
             << setw(15) << box_x / 2 << endl << -box_x / 2 << setw(15) << box_x / 2 << endl
             << "ITEM: ATOMS index type x y z b charge" << endl;
       for (long g = 0; g < N; g++)
-        ofile << g + 1 << setw(15) << in.type[g % np] << setw(15) << pos[3 * g] << setw(15) << pos[3 * g + 1]
-              << setw(15) << pos[3 * g + 2] << setw(15) << be[g] << setw(15) << in.q[g % np] << endl;
+        ofile << g + 1 << setw(15) << in.type[g % np] << setw(15) << P[3 * g] << setw(15) << P[3 * g + 1]
+              << setw(15) << P[3 * g + 2] << setw(15) << be[g] << setw(15) << in.q[g % np] << endl;
       for (int bb = 0; bb < n_big; bb++)  // type 3, no bending energy (src/md.cpp:670-675)
         ofile << N + bb + 1 << setw(15) << 3 << setw(15) << big_pos[3 * bb] << setw(15) << big_pos[3 * bb + 1]
               << setw(15) << big_pos[3 * bb + 2] << setw(15) << 0 << setw(15) << o.G << endl;
+    }
+  };
+  auto flush_pending = [&]() {
+    if (!pending.active) return;
+    check(souffle_gpu_snapshot_wait(h, pending.slot), "souffle_gpu_snapshot_wait");
+    write_outputs(pending.a, snap_pos[pending.slot], snap_vel[pending.slot]);
+    pending.active = false;
+  };
+  const double loop_end = (totaltime / o.t) + 1;  // src/md.cpp:387
+  long a = loopStart;
+  double pre = -1;
+  int slot = 0;
+  while (a < loop_end) {
+    // advance to the next step that writes anything (inclusive)
+    long next = a;
+    while (next + 1 < loop_end && !(next % o.w == 0 || next % o.W == 0 || next % o.M == 0)) next++;
+    check(souffle_gpu_md_enqueue(h, a, (int)(next - a + 1)), "souffle_gpu_md_enqueue");
+    a = next;
+    const bool state_out = a % o.w == 0 || a % o.M == 0;
+    if (state_out) check(souffle_gpu_snapshot_enqueue(h, slot, snap_pos[slot], snap_vel[slot]), "souffle_gpu_snapshot_enqueue");
+    flush_pending();  // the previous output step's files, while this window runs
+    if (a % o.W == 0) energy_row(a, true);
+    if (state_out) {
+      pending.active = true;
+      pending.a = a;
+      pending.slot = slot;
+      slot ^= 1;
     }
     double pct = roundf(a / (totaltime / o.t) * 100 * 10) / 10;
     if (pct != pre) {
@@ -570,6 +607,12 @@ int run_simulation(const Options& o) {
       pre = pct;
     }
     a++;
+  }
+  flush_pending();
+  check(souffle_gpu_synchronize(h), "souffle_gpu_synchronize");
+  for (int k = 0; k < 2; k++) {
+    souffle_gpu_host_free(snap_pos[k]);
+    souffle_gpu_host_free(snap_vel[k]);
   }
   printf("\n");
   souffle_gpu_destroy(h);

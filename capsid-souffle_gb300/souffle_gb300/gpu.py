@@ -29,6 +29,7 @@ EXPORTED = [
     "souffle_gpu_md_begin", "souffle_gpu_md_steps", "souffle_gpu_md_enqueue", "souffle_gpu_md_scalars",
     "souffle_gpu_synchronize", "souffle_gpu_last_error", "souffle_gpu_stream",
     "souffle_gpu_md_profile", "souffle_gpu_kinetic_energy_noalloc", "souffle_gpu_autotune",
+    "souffle_gpu_snapshot_enqueue", "souffle_gpu_snapshot_wait", "souffle_gpu_host_alloc", "souffle_gpu_host_free",
     # include/souffle_surrogate.h
     "souffle_mlp_create", "souffle_mlp_destroy", "souffle_mlp_stream", "souffle_mlp_param_count", "souffle_mlp_get_params",
     "souffle_mlp_set_params", "souffle_mlp_forward", "souffle_mlp_forward_layered", "souffle_mlp_profile_forward", "souffle_mlp_gradients", "souffle_mlp_train_step",
@@ -132,6 +133,12 @@ def load() -> C.CDLL:
     lib.souffle_gpu_md_enqueue.argtypes = [vp, C.c_int64, C.c_int32]
     lib.souffle_gpu_md_scalars.argtypes = [vp, C.c_int32, dp, dp, dp]
     lib.souffle_gpu_synchronize.argtypes = [vp]
+    lib.souffle_gpu_snapshot_enqueue.argtypes = [vp, C.c_int32, vp, vp]
+    lib.souffle_gpu_snapshot_wait.argtypes = [vp, C.c_int32]
+    lib.souffle_gpu_host_alloc.argtypes = [C.c_int64]
+    lib.souffle_gpu_host_alloc.restype = vp
+    lib.souffle_gpu_host_free.argtypes = [vp]
+    lib.souffle_gpu_host_free.restype = None
     lib.souffle_gpu_last_error.restype = C.c_char_p
     lib.souffle_gpu_stream.restype = C.c_void_p
     lib.souffle_gpu_stream.argtypes = [vp]
@@ -255,6 +262,18 @@ class GpuSystem:
         vel = np.empty((self.n, 3))
         _check(self.lib.souffle_gpu_get_state(self.h, _dp(pos), _dp(vel)))
         return pos, vel
+
+    def snapshot_enqueue(self, slot: int, pos: np.ndarray, vel: np.ndarray) -> None:
+        """Queue a read-back of the state into pos / vel ([n][3] float64, C order; either may be
+        None) behind the queued work; the arrays must stay alive until snapshot_wait(slot)."""
+        for arr in (pos, vel):
+            if arr is not None and (arr.dtype != np.float64 or not arr.flags.c_contiguous or arr.size != 3 * self.n):
+                raise ValueError("snapshot buffers: [n][3] C-contiguous float64")
+        _check(self.lib.souffle_gpu_snapshot_enqueue(self.h, slot, pos.ctypes.data if pos is not None else None,
+                                                     vel.ctypes.data if vel is not None else None))
+
+    def snapshot_wait(self, slot: int) -> None:
+        _check(self.lib.souffle_gpu_snapshot_wait(self.h, slot))
 
     def forces(self, rebuild: bool = True, parts: bool = False):
         tf = np.empty((self.n, 3))

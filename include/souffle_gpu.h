@@ -197,6 +197,22 @@ souffle_status souffle_gpu_md_scalars(souffle_gpu_system* h, int32_t system, dou
  * of queued steps like souffle_gpu_md_steps. */
 souffle_status souffle_gpu_synchronize(souffle_gpu_system* h);
 
+/* Asynchronous state read-back for writers that overlap file output with the next MD steps (the
+ * restart and movie writers of src/md.cpp:526-546,647-678 read the state at the output step).
+ * souffle_gpu_snapshot_enqueue queues, behind all work queued so far, what souffle_gpu_get_state
+ * returns (positions; velocities with the pending centre-of-mass velocity removed) into slot 0 or
+ * 1 and from there into pos / vel (N*3 each, may be NULL; page-locked memory from
+ * souffle_gpu_host_alloc makes the copy truly asynchronous), and returns at once.  The host buffers
+ * must stay untouched until souffle_gpu_snapshot_wait(h, slot) has returned; it blocks until the
+ * copy has landed and reports the device-side errors of the work queued before it, as
+ * souffle_gpu_synchronize does.  A slot takes one snapshot at a time.  No reference counterpart. */
+souffle_status souffle_gpu_snapshot_enqueue(souffle_gpu_system* h, int32_t slot, double* pos, double* vel);
+souffle_status souffle_gpu_snapshot_wait(souffle_gpu_system* h, int32_t slot);
+/* Page-locked host memory for the snapshot buffers (NULL on failure); free with
+ * souffle_gpu_host_free. */
+void* souffle_gpu_host_alloc(int64_t bytes);
+void souffle_gpu_host_free(void* p);
+
 /* The CUDA stream (cudaStream_t) all work of the handle is queued on, so a caller can
  * order its own work or record events against it.  No reference counterpart. */
 void* souffle_gpu_stream(souffle_gpu_system* h);

@@ -141,6 +141,36 @@ def test_graph_windows_equal_single_steps():
     assert np.array_equal(p1, p2) and np.array_equal(v1, v2)
 
 
+def test_async_snapshots_equal_synchronous_state():
+    """souffle_gpu_snapshot_enqueue behind queued steps returns the state get_state returns after
+    the same steps run synchronously, in both slots, with windows queued between the snapshots."""
+    g = load_golden("bilayer_dense")
+    s1, *_ = _gpu(g)
+    s1.md_begin()
+    n = s1.n
+    p0, v0 = np.full((n, 3), np.nan), np.full((n, 3), np.nan)
+    p1, v1 = np.full((n, 3), np.nan), np.full((n, 3), np.nan)
+    s1.md_enqueue(0, 7)
+    s1.snapshot_enqueue(0, p0, v0)
+    s1.md_enqueue(7, 16)
+    s1.snapshot_enqueue(1, p1, None)
+    s1.snapshot_wait(0)
+    s1.snapshot_wait(1)
+    s2, *_ = _gpu(g)
+    s2.md_begin()
+    s2.md_steps(0, 7)
+    q0, w0 = s2.get_state()
+    s2.md_steps(7, 16)
+    q1, _ = s2.get_state()
+    assert np.array_equal(p0, q0) and np.array_equal(v0, w0) and np.array_equal(p1, q1)
+    assert np.isnan(v1).all()                        # no velocities asked for in slot 1
+    # a slot holds one snapshot at a time
+    s1.snapshot_enqueue(0, p0, None)
+    with pytest.raises(RuntimeError):
+        s1.snapshot_enqueue(0, p0, None)
+    s1.snapshot_wait(0)
+
+
 def test_batched_systems_equal_separate_runs():
     """Replicas in one handle give bitwise the same trajectories as separate handles."""
     from souffle_gb300 import gpu, workloads

@@ -67,7 +67,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if os.path.isdir(HOST) else []
     if drv_src and (force or not _newer(DRIVER, drv_src + [LIB] + headers)):
         cxx = os.environ.get("CXX", "g++")
-        _run([cxx, "-O2", "-std=c++17", "-I", INCLUDE, "-o", DRIVER] + drv_src +
+        _run([cxx, "-O2", "-std=c++17", "-pthread", "-I", INCLUDE, "-o", DRIVER] + drv_src +
              ["-L", OUT, "-lsouffle_gb300", f"-Wl,-rpath,{OUT}"])
     text = "\n".join(logs)
     if verbose:

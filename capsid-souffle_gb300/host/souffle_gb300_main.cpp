@@ -27,6 +27,7 @@
 #include <random>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "analysis_host.h"
@@ -36,6 +37,40 @@
 using namespace std;
 
 namespace {
+
+// Lines [0, n) formatted by line(os, i) on the host's cores, in chunks written into strings and
+// appended to out in order.  Each chunk's stream starts in out's state as it would be at the
+// chunk's first line: out's current precision and width for the first chunk, and the precision
+// and pending width the lines leave behind (`later_prec`, `later_width`) for the others; lines end
+// with an unformatted put('\n'), which, like endl, leaves a pending width alone.  So the bytes are
+// those of one sequential pass.
+template <class Line>
+void write_lines(std::ostream& out, long n, std::streamsize later_prec, std::streamsize later_width, Line line) {
+  const long min_chunk = 4096;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const long chunks = std::max(1L, std::min<long>((long)std::min(hw, 16u), n / min_chunk));
+  std::vector<std::string> text((size_t)chunks);
+  auto run = [&](long c) {
+    std::ostringstream os;
+    os.flags(out.flags());
+    os.fill(out.fill());
+    os.precision(c == 0 ? out.precision() : later_prec);
+    os.width(c == 0 ? out.width() : later_width);
+    const long i0 = n * c / chunks, i1 = n * (c + 1) / chunks;
+    for (long i = i0; i < i1; i++) line(os, i);
+    text[(size_t)c] = os.str();
+  };
+  std::vector<std::thread> pool;
+  for (long c = 1; c < chunks; c++) pool.emplace_back(run, c);
+  run(0);
+  for (auto& t : pool) t.join();
+  const std::streamsize w = out.width();
+  out.width(0);
+  for (const auto& t : text) out << t;
+  out.width(n > 0 ? later_width : w);
+  if (n > 0) out.precision(later_prec);
+  out.flush();
+}
 
 struct Options {
   char D = 'm';
@@ -546,11 +581,17 @@ int run_simulation(const Options& o) {
     if (at % o.w == 0) {
       rs.open(("outfiles/restart_" + to_string(at) + ".out").c_str(), ios::out);
       rs << "Velocities & Positions for " << at << endl;
-      for (long i = 0; i < N; i++)
-        rs << i << "  " << V[3 * i] << setw(25) << setprecision(12) << V[3 * i + 1] << setw(25)
+      // the first velocity of a line takes the precision the previous line left (12; the
+      // stream's earlier precision on the first line of the first file), as the reference's
+      // reused stream does
+      // (and each line leaves a width of 25 pending, which the next line's index takes)
+      write_lines(rs, N, 12, 25, [&](std::ostream& os, long i) {
+        os << i << "  " << V[3 * i] << setw(25) << setprecision(12) << V[3 * i + 1] << setw(25)
            << setprecision(12) << V[3 * i + 2] << setw(25) << setprecision(12) << P[3 * i] << setw(25)
            << setprecision(12) << P[3 * i + 1] << setw(25) << setprecision(12) << P[3 * i + 2] << setw(25)
-           << setprecision(12) << endl;
+           << setprecision(12);
+        os.put('\n');
+      });
       rs.close();
       if (o.p) {
         rs.open(("outfiles/rb_" + to_string(at) + ".out").c_str(), ios::out);
@@ -567,9 +608,11 @@ int run_simulation(const Options& o) {
             << "ITEM: BOX BOUNDS" << endl << -box_x / 2 << setw(15) << box_x / 2 << endl << -box_x / 2
             << setw(15) << box_x / 2 << endl << -box_x / 2 << setw(15) << box_x / 2 << endl
             << "ITEM: ATOMS index type x y z b charge" << endl;
-      for (long g = 0; g < N; g++)
-        ofile << g + 1 << setw(15) << in.type[g % np] << setw(15) << P[3 * g] << setw(15) << P[3 * g + 1]
-              << setw(15) << P[3 * g + 2] << setw(15) << be[g] << setw(15) << in.q[g % np] << endl;
+      write_lines(ofile, N, ofile.precision(), 0, [&](std::ostream& os, long g) {
+        os << g + 1 << setw(15) << in.type[g % np] << setw(15) << P[3 * g] << setw(15) << P[3 * g + 1]
+           << setw(15) << P[3 * g + 2] << setw(15) << be[g] << setw(15) << in.q[g % np];
+        os.put('\n');
+      });
       for (int bb = 0; bb < n_big; bb++)  // type 3, no bending energy (src/md.cpp:670-675)
         ofile << N + bb + 1 << setw(15) << 3 << setw(15) << big_pos[3 * bb] << setw(15) << big_pos[3 * bb + 1]
               << setw(15) << big_pos[3 * bb + 2] << setw(15) << 0 << setw(15) << o.G << endl;

@@ -65,7 +65,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
     drv_src = [os.path.join(HOST, f) for f in sorted(os.listdir(HOST)) if f.endswith(".cpp")] \
         if os.path.isdir(HOST) else []
-    if drv_src and (force or not _newer(DRIVER, drv_src + [LIB] + headers)):
+    drv_hdr = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")] if os.path.isdir(HOST) else []
+    if drv_src and (force or not _newer(DRIVER, drv_src + drv_hdr + [LIB] + headers)):
         cxx = os.environ.get("CXX", "g++")
         _run([cxx, "-O2", "-std=c++17", "-pthread", "-I", INCLUDE, "-o", DRIVER] + drv_src +
              ["-L", OUT, "-lsouffle_gb300", f"-Wl,-rpath,{OUT}"])

@@ -303,7 +303,8 @@ def bench_surrogate(args):
     far_cap = max(4096, args.far_per_subunit * int(w.opt.S))
     batch = 4096
     net = gpu.Mlp(64, n_out, max_batch=max(far_cap, batch), seed=7, width=getattr(args, "net_width", 128))
-    gpu.surrogate_attach(s, net, w.template.pos, far_capacity=far_cap)
+    gpu.surrogate_attach(s, net, w.template.pos, far_capacity=far_cap,
+                         switch_radius=getattr(args, "switch_radius", 3.0))
     B = int(w.opt.B)
     # training data: exact far-pair forces along the plain trajectory, one frame per rebuild window
     rows = args.train_rows
@@ -390,7 +391,7 @@ def bench_surrogate(args):
         "dtype": "bf16 network (fp32 accumulate) + f32/i64 exact path", "data": "synthetic",
         "config": {"workload": f"plain_large: {args.subunits} bilayer capsomeres x 42 beads = {w.n_beads} "
                                f"beads, {w.opt.C:g} uM, Debye length {1 / w.derived.kappa:.3g} sigma (-c {w.opt.c:.4g}), "
-                               f"switch radius 3.5 sigma (closest bead pair), judge 1 % "
+                               f"switch radius {getattr(args, 'switch_radius', 3.0):g} sigma (closest bead pair), judge 1 % "
                                f"of far pairs every 100 steps",
                    "l2": "flushed (256 MB write) before every timed step"},
         "plain": plain, "surrogate": surr, "gain": surr["value"] / plain["value"],
@@ -483,7 +484,8 @@ def surrogate_batched(args):
     far_cap = max(4096, args.far_per_subunit * S_tot)
     batch = 4096
     net = gpu.Mlp(64, n_out, max_batch=max(far_cap, batch), seed=7, width=getattr(args, "net_width", 128))
-    gpu.surrogate_attach(s, net, tpl.pos, far_capacity=far_cap)
+    gpu.surrogate_attach(s, net, tpl.pos, far_capacity=far_cap,
+                         switch_radius=getattr(args, "switch_radius", 3.0))
     ext = torch.cuda.ExternalStream(s.stream())
 
     rows = args.train_rows
@@ -555,7 +557,8 @@ def surrogate_batched(args):
         sysl = [i for i in watch for _ in range(n_seeds)]
         sw = gpu.GpuSystem(tpl, [params[i] for i in sysl])
         gpu.surrogate_attach(sw, net, tpl.pos, far_capacity=max(4096, args.far_per_subunit *
-                                                                 sum(int(reps[i].opt.S) for i in sysl)))
+                                                                 sum(int(reps[i].opt.S) for i in sysl)),
+                             switch_radius=getattr(args, "switch_radius", 3.0))
         gpu.surrogate_enable(sw, enabled)
         rng = np.random.default_rng(seed0)
         vels = []
@@ -644,8 +647,8 @@ def surrogate_batched(args):
                                f"subunits, {n} beads, subunits per system {min(sizes)}-{max(sizes)}, "
                                + ("eps 2.1, Debye length 1 sigma, 800 uM" if getattr(args, "replica_subunits", 0)
                                   else "eps 1.5-3.0, Debye length 0.5-2.0 sigma, 200-1600 uM")
-                               + f"; switch radius "
-                               f"3.5 sigma (closest bead pair), judge 1 % of far pairs every 100 steps",
+                               + f"; switch radius {getattr(args, 'switch_radius', 3.0):g} "
+                               f"sigma (closest bead pair), judge 1 % of far pairs every 100 steps",
                    "l2": "batched: working set larger than L2, whole rebuild windows; plain: L2 "
                          "flushed before each replica's window"},
         "gain": surr["value"] / plain_value,
@@ -961,6 +964,10 @@ def main():
                     help="with --replicas --surrogate: replicas timed alone for the plain path")
     ap.add_argument("--far-per-subunit", type=int, default=4,
                     help="surrogate far-pair list capacity per subunit")
+    ap.add_argument("--switch-radius", type=float, default=3.0,
+                    help="surrogate: closest bead-pair distance from which a subunit pair is far (3.0: the "
+                         "2.5 sigma LJ cut-off plus 0.5 sigma for the motion between pair-list rebuilds, more "
+                         "than the reference's own 0.3 sigma list skin; the library default is 3.5)")
     ap.add_argument("--net-width", type=int, default=128, choices=(128, 256),
                     help="hidden width of the surrogate network (128: 65 us per 118k-row forward at a "
                          "force error of ~1.2e-5; 256: 100 us at ~1.1e-5)")
@@ -1200,7 +1207,7 @@ def main():
             sb = surrogate_batched(argparse.Namespace(
                 replicas=256, far_per_subunit=16, steps=100, stat_steps=3000, plain_sample=64, profile=False,
                 train_rows=args.train_rows, max_frames=args.max_frames, epochs=args.epochs,
-                net_width=args.net_width))
+                net_width=args.net_width, switch_radius=args.switch_radius))
             out["surrogate_batched"] = {k: sb[k] for k in (
                 "metric", "value", "unit", "gain", "gain_batching", "gain_surrogate", "config",
                 "force_rms_rel_error", "force_rms_rel_error_worst_system", "far_pairs")}

@@ -1052,6 +1052,13 @@ souffle_status souffle_surrogate_attach(souffle_gpu_system* h, souffle_mlp* net,
   if (o.judge_tolerance <= 0) o.judge_tolerance = 1e-3;
   if (o.far_capacity <= 0) o.far_capacity = std::max(1024, 2 * h->S);
   if (cap < o.far_capacity) return sfail(SOUFFLE_ERR_BAD_INPUT, "network max_batch is below far_capacity");
+  // far pairs must stay beyond the LJ/WCA range until the next rebuild: the switch radius has to
+  // exceed every system's LJ cut-off (the WCA range 2^(1/6) s lies below it) by the list skin
+  for (const souffle_params& p : h->prm) {
+    const double skin = std::max(0.0, p.nlist_cutoff - std::max(p.ecut, p.ecut_el));
+    if (!(o.switch_radius >= p.ecut + skin))
+      return sfail(SOUFFLE_ERR_BAD_INPUT, "switch_radius must be at least the LJ cut-off plus the pair-list skin");
+  }
   // body frame of the rest shape: centre bead, the bead farthest from it, the bead farthest
   // from that axis
   const int cl = h->prm[0].center_local;

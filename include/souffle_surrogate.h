@@ -87,7 +87,8 @@ souffle_status souffle_mlp_train_step(souffle_mlp* h, const float* x_dev, const 
  * class whose estimate exceeds judge_tolerance / 2 in any system reverts to exact from the next
  * rebuild on, so the four classes together stay within judge_tolerance. */
 typedef struct souffle_surrogate_options {
-  double switch_radius;    /* default 3.5 */
+  double switch_radius;    /* closest bead-pair distance from which a subunit pair is far, default 3.5; at least
+                              every system's LJ cut-off plus its pair-list skin (BAD_INPUT otherwise) */
   int32_t far_capacity;    /* most far pairs (0 = max(1024, 2 x subunits)); beyond it all stay exact */
   int32_t judge_every;     /* default 100 */
   int32_t judge_stride;    /* default 100 (1 % of the far pairs) */

@@ -229,3 +229,15 @@ def test_md_with_surrogate_runs_and_holds_temperature():
     assert np.isfinite(e["temperature"]) and 0.5 < e["temperature"] < 2.0
     st = gpu.surrogate_stats(s)
     assert st["enabled"] and st["judged"] > 0
+
+
+def test_switch_radius_inside_the_lj_range_is_rejected():
+    """A far pair must stay beyond the LJ cut-off (2.5 sigma) until the next rebuild: a switch
+    radius below the cut-off plus the pair-list skin (0.3 sigma here: 2.8) is refused at attach."""
+    from souffle_gb300 import gpu
+    w, s, p = _system()
+    n_out = 6 + 3 * w.template.n_beads
+    net = gpu.Mlp(64, n_out, max_batch=CAP, seed=3)
+    with pytest.raises(RuntimeError):
+        gpu.surrogate_attach(s, net, w.template.pos, far_capacity=CAP, switch_radius=2.7)
+    gpu.surrogate_attach(s, net, w.template.pos, far_capacity=CAP, switch_radius=2.85)

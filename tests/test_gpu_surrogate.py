@@ -30,12 +30,12 @@ def _system(n_sub=300, conc=2000, seed=21):
     return w, s, p
 
 
-def _net_and_buffers(w, s):
+def _net_and_buffers(w, s, width=256, switch_radius=3.5):
     torch = _torch()
     from souffle_gb300 import gpu
     n_out = 6 + 3 * w.template.n_beads
-    net = gpu.Mlp(64, n_out, max_batch=CAP, seed=3)
-    gpu.surrogate_attach(s, net, w.template.pos, far_capacity=CAP)
+    net = gpu.Mlp(64, n_out, max_batch=CAP, seed=3, width=width)
+    gpu.surrogate_attach(s, net, w.template.pos, far_capacity=CAP, switch_radius=switch_radius)
     x = torch.zeros(CAP, 64, device="cuda")
     t = torch.zeros(CAP, n_out, device="cuda")
     return torch, net, x, t, n_out
@@ -121,13 +121,14 @@ def _train(w, s, torch, x, t, frames=12, stride=20, epochs=60):
     return total, loss
 
 
-def test_training_and_force_accuracy():
+@pytest.mark.parametrize("width,switch_radius", [(256, 3.5), (128, 3.5), (128, 3.0)])
+def test_training_and_force_accuracy(width, switch_radius):
     """Trained on exact far-pair data from a short run, the surrogate's far-field forces stay
     within 1e-3 of the exact total force (RMS, relative), and it removes most of the error that
-    dropping the far pairs would leave."""
+    dropping the far pairs would leave; both hidden widths, and the 3.0 sigma switch radius."""
     from souffle_gb300 import gpu
     w, s, p = _system()
-    torch, net, x, t, n_out = _net_and_buffers(w, s)
+    torch, net, x, t, n_out = _net_and_buffers(w, s, width, switch_radius)
     total, loss = _train(w, s, torch, x, t)
     assert total > 500 and loss < 0.5, (total, loss)
     # exact forces and the exact far-field part at the current state
@@ -136,7 +137,7 @@ def test_training_and_force_accuracy():
     np_ = w.template.n_beads
     pos, _ = s.get_state()
     L = float(w.derived.box)
-    ref = SO.far_pairs(pos, int(w.opt.S), np_, w.center_local, L, w.derived.nlist_cutoff, 3.5,
+    ref = SO.far_pairs(pos, int(w.opt.S), np_, w.center_local, L, w.derived.nlist_cutoff, switch_radius,
                        reach=max(w.derived.ecut_el, w.derived.ecut))
     assert n == len(ref)
     wts = SO.dh_weights(w.template.charge, w.template.diameter, w.derived.kappa, w.derived.lb)

@@ -158,11 +158,6 @@ __global__ void k_unpad(const float* y, int ld, int m, int n_out, float* out) {
   out[i] = y[(size_t)r * ld + c];
 }
 
-__global__ void k_to_bf16(const float* x, int n, __nv_bfloat16* y) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = __float2bfloat16_rn(x[i]);
-}
-
 int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace

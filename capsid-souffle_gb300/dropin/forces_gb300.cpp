@@ -57,7 +57,7 @@ void create_handle(vector<SUBUNIT>& protein, vector<BEAD>& beads, double lb, dou
   }
   souffle_template t{np, (int)et.size(), (int)(fb.size() / 3), (int)(lj.size() / 2),
                      type.data(), q.data(), sig.data(), m.data(), eb.data(), et.data(), l0.data(),
-                     fb.data(), lj.empty() ? nullptr : lj.data()};
+                     fb.data(), lj.empty() ? nullptr : lj.data(), nullptr /* no rest dihedral */};
   souffle_params p{};
   p.n_subunits = (int)protein.size();
   p.box = (double)beads[0].bx.x;

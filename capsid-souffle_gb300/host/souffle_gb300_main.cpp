@@ -475,7 +475,8 @@ int run_simulation(const Options& o) {
   }
 
   souffle_template t{np, in.ne, in.nf, in.na, in.type.data(), in.q.data(), in.sigma.data(), in.mass.data(),
-                     in.eb.data(), in.et.data(), in.len0.data(), in.fb.data(), in.lj.empty() ? nullptr : in.lj.data()};
+                     in.eb.data(), in.et.data(), in.len0.data(), in.fb.data(), in.lj.empty() ? nullptr : in.lj.data(),
+                     nullptr /* no rest dihedral: the reference's bending */};
   souffle_params p{};
   p.n_subunits = S;
   p.box = box_x;
